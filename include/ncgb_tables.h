@@ -1,0 +1,118 @@
+/*
+ * ncgb_tables.h -- flat, pointer-based view of one material's scattering
+ * tables, as laid out in device memory (HBM) by the host table builder.
+ *
+ * The same structs describe the tables in host memory, so the CPU oracle and
+ * the CUDA kernels read one layout.  Plain C, no CUDA or torch types.
+ *
+ * A material is NCrystal's ProcComposition for one cfg-string
+ * (NCProcImpl.hh:310-373): up to NCGB_MAX_COMP components, each with a scale,
+ * an energy domain [elow,ehigh] and a type-specific table set:
+ *
+ *   PowderBragg  two_dE[n], fdm_commul[n]            (NCPowderBragg.hh:29-95)
+ *   ElIncScatter (msd, sigma*scale) per element       (NCElIncXS.hh:127)
+ *   SABScatter   energy grid + xs, S/logS/cumulative alpha integrals on the
+ *                (beta, alpha) grid, one Alg.1 sampler per energy-grid point
+ *                (NCSABSampler.hh:91-98, NCSABSamplerModels.hh:31-79)
+ *   FreeGas      kT, target mass, sigma_free          (NCFreeGas.cc:25-42)
+ */
+#ifndef NCGB_TABLES_H
+#define NCGB_TABLES_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NCGB_MAX_COMP 8
+#define NCGB_MAX_ELINC 16
+
+enum ncgb_comp_type {
+  NCGB_COMP_NONE = 0,
+  NCGB_COMP_ELINC = 1,
+  NCGB_COMP_BRAGG = 2,
+  NCGB_COMP_SAB = 3,
+  NCGB_COMP_FREEGAS = 4
+};
+
+/* One beta row's alpha sampler at one energy-grid point
+ * (SABSamplerAtE_Alg1::AlphaSampleInfo, NCSABSamplerModels.hh:46-56). */
+typedef struct {
+  double front_alpha, front_sval, front_logsval;
+  double back_alpha, back_sval, back_logsval;
+  double prob_front;   /* 1.0: narrow range, 2.0: zero xs (sample linearly) */
+  double prob_notback; /* prob_front + prob_middle */
+  uint32_t front_idx, back_idx;
+} ncgb_alpha_info;
+
+typedef struct {
+  int64_t n;                 /* number of merged d-spacings */
+  double threshold;          /* = two_dE[0]: Bragg cut-off energy */
+  const double* two_dE;      /* ascending wl2ekin(2d) */
+  const double* fdm_commul;  /* cumulative d*|F|^2*mult*xsectfact */
+} ncgb_bragg_view;
+
+typedef struct {
+  int32_t n;
+  double msd[NCGB_MAX_ELINC];
+  double sigma[NCGB_MAX_ELINC]; /* bound incoherent xs * scale */
+} ncgb_elinc_view;
+
+typedef struct {
+  /* scalars */
+  double kT, egrid_margin, internal_scale;
+  double kext;          /* SABXSProvider: (xs(Emax)-extenderxs(Emax))*Emax */
+  double k1, k2;        /* SABSampler: xsAtEmax*Emax, extenderxs(Emax)*Emax */
+  double ext_sigma_free, ext_ca; /* free-gas extender, xs = sf*shape(ca*E) */
+  double ext_kT, ext_mass_amu;
+  double sigma_bound;
+  int32_t ne, na, nb;
+  int32_t pad0;
+  /* energy grid */
+  const double* egrid;  /* [ne] */
+  const double* xs;     /* [ne] */
+  /* kernel grid, S stored beta-major: idx = ibeta*na + ialpha */
+  const double* alpha;  /* [na] */
+  const double* beta;   /* [nb] */
+  const double* sab;    /* [nb*na] */
+  const double* logsab; /* [nb*na] */
+  const double* cumul;  /* [nb*na] cumulative alpha integrals per beta row */
+  /* per energy-grid point sampler (kind 0: no scatter, 1: Alg.1) */
+  const int32_t* smp_kind;        /* [ne] */
+  const int32_t* smp_ibetaoffset; /* [ne] */
+  const int32_t* smp_nbeta;       /* [ne] beta points in the sampler */
+  const int64_t* smp_offset;      /* [ne] offset into bx/by/bcdf/info */
+  const double* smp_fbkep;        /* [ne] first-bin kinematic endpoint (<=0) or 1.0 */
+  const double* bx;               /* beta values */
+  const double* by;               /* normalised pdf values */
+  const double* bcdf;             /* normalised cdf values */
+  const ncgb_alpha_info* info;    /* [offset + j], j < nbeta-1 */
+} ncgb_sab_view;
+
+typedef struct {
+  double kT, mass_amu, sigma_free, ca;
+} ncgb_freegas_view;
+
+typedef struct {
+  int32_t type;
+  int32_t pad0;
+  double scale, elow, ehigh;
+  ncgb_bragg_view bragg;
+  ncgb_elinc_view elinc;
+  ncgb_sab_view sab;
+  ncgb_freegas_view fg;
+} ncgb_comp_view;
+
+typedef struct {
+  int32_t ncomp;
+  int32_t pad0;
+  double dom_elow, dom_ehigh; /* union of the component domains */
+  ncgb_comp_view comp[NCGB_MAX_COMP];
+} ncgb_material_view;
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,169 @@
+/*
+ * ncrystal_gb300.h -- C ABI of the GB300 batched non-oriented scattering path.
+ *
+ * Part 1 is a drop-in for the subset of NCrystal's C interface
+ * (ncrystal_core/include/NCrystal/cinterface/ncrystal.h, NCrystal 4.4.2) that
+ * a Monte Carlo code uses to evaluate non-oriented materials: the same symbol
+ * names, handle types, argument meanings, error conventions and output
+ * sentinels.  Linking this library instead of libNCrystal moves the
+ * per-neutron work of the _many calls onto the GPU.
+ *
+ * Part 2 holds additions with no counterpart in the reference: FP32 and
+ * device-pointer batch calls, the multi-material ragged batch, and a host-only
+ * table loader used by tests.
+ *
+ * Materials: ncrystal_create_scatter() takes NCrystal cfg-strings.  The
+ * host-side loading results for a cfg-string are read from a material bundle
+ * (.ncgb) found in the directories of NCGB_BUNDLE_PATH (colon separated) or in
+ * the package's bundles/ directory; bundles are written by ncgb_export, which
+ * runs NCrystal's own material loading.  The tables are uploaded once to the
+ * current CUDA device.
+ *
+ * Random numbers: every neutron of every call owns a Philox4x32-10 stream
+ * (include/ncgb_philox.h).  Counter-based streams replace the reference's
+ * sequential per-Scatter stream: results are reproducible for a given seed,
+ * clone index and call sequence, independent of launch shape.
+ *
+ * Plain C: pointers and sizes only.
+ */
+#ifndef NCRYSTAL_GB300_H
+#define NCRYSTAL_GB300_H
+
+#include <stdint.h>
+#include "ncgb_tables.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ===================== Part 1: NCrystal C interface subset ================ */
+
+/* Handles (ncrystal.h:666-670).  Opaque; 'internal' points at a type-tagged
+ * ref-counted object like the reference's (ncrystal.cc:166-182). */
+typedef struct { void * internal; } ncrystal_process_t;
+typedef struct { void * internal; } ncrystal_scatter_t;
+
+/* Reference counting (ncrystal.h:672-676).  ncrystal_unref takes the ADDRESS
+ * of a handle and invalidates it when the count reaches 0. */
+int  ncrystal_refcount( void* object );
+void ncrystal_ref( void* object );
+void ncrystal_unref( void* object );
+int  ncrystal_valid( void* object );
+void ncrystal_invalidate( void* object );
+
+/* Factories (ncrystal.h:699, :708, :718-731). */
+ncrystal_scatter_t ncrystal_create_scatter( const char * cfgstr );
+ncrystal_scatter_t ncrystal_create_scatter_builtinrng( const char * cfgstr, unsigned long seed );
+ncrystal_scatter_t ncrystal_clone_scatter( ncrystal_scatter_t );
+ncrystal_scatter_t ncrystal_clone_scatter_rngbyidx( ncrystal_scatter_t, unsigned long rngstreamidx );
+ncrystal_scatter_t ncrystal_clone_scatter_rngforcurrentthread( ncrystal_scatter_t );
+
+/* Casts (ncrystal.h:680-686). */
+ncrystal_process_t ncrystal_cast_scat2proc( ncrystal_scatter_t );
+ncrystal_scatter_t ncrystal_cast_proc2scat( ncrystal_process_t );
+
+/* Process queries (ncrystal.h:759-775). */
+const char * ncrystal_name( ncrystal_process_t );
+int ncrystal_isnonoriented( ncrystal_process_t );
+void ncrystal_domain( ncrystal_process_t, double* ekin_low, double* ekin_high );
+
+/* Scalar evaluation (ncrystal.h:765-780). */
+void ncrystal_crosssection_nonoriented( ncrystal_process_t, double ekin, double* result );
+void ncrystal_samplescatterisotropic( ncrystal_scatter_t, double ekin,
+                                      double* ekin_final, double* cos_scat_angle );
+void ncrystal_genscatter_nonoriented( ncrystal_scatter_t, double ekin,
+                                      double* result_angle, double* result_dekin );
+
+/* Batched evaluation -- the GPU hot path.
+ * ncrystal.h:1305-1309 / ncrystal.cc:1107-1141: results[repeat*n_ekin] (barn),
+ *   -1.0 everywhere on error. */
+void ncrystal_crosssection_nonoriented_many( ncrystal_process_t,
+                                             const double * ekin,
+                                             unsigned long n_ekin,
+                                             unsigned long repeat,
+                                             double* results );
+/* ncrystal.h:1289-1294 / ncrystal.cc:1201-1245: index irepeat*n_ekin+i;
+ *   E'=-1, mu=-999 everywhere on error. */
+void ncrystal_samplescatterisotropic_many( ncrystal_scatter_t,
+                                           const double * ekin,
+                                           unsigned long n_ekin,
+                                           unsigned long repeat,
+                                           double* results_ekin,
+                                           double* results_cos_scat_angle );
+/* ncrystal.h:1355-1360 / ncrystal.cc:1301-1324 (obsolete in the reference,
+ *   warns once): angle=acos(mu), dekin=E'-E; outputs untouched on error. */
+void ncrystal_genscatter_nonoriented_many( ncrystal_scatter_t,
+                                           const double * ekin,
+                                           unsigned long n_ekin,
+                                           unsigned long repeat,
+                                           double* results_angle,
+                                           double* results_dekin );
+
+/* Error handling (ncrystal.h:1031-1051; ncrystal.cc:281-322).  As in the
+ * reference, an error prints its message and calls exit(1) unless
+ * ncrystal_sethaltonerror(0) was called first. */
+int ncrystal_sethaltonerror( int );
+int ncrystal_error( void );
+const char * ncrystal_lasterror( void );
+const char * ncrystal_lasterrortype( void );
+void ncrystal_clearerror( void );
+void ncrystal_seterrhandler( void (*handler)(char*,char*) );
+
+/* Version (ncrystal.h:1229-1230): the NCrystal version whose behaviour the
+ * path reproduces. */
+int ncrystal_version( void );
+const char * ncrystal_version_str( void );
+
+/* ===================== Part 2: additions (no reference counterpart) ======= */
+
+/* Per-neutron status codes written by the kernels. */
+#define NCGB_ST_OK 0
+#define NCGB_ST_LOOPCAP 1      /* rejection loop cap hit (reference: CalcError) */
+#define NCGB_ST_UNSUPPORTED 2  /* free-gas sampling (not yet on the GPU) */
+
+/* Fused cross-section + one isotropic scatter per neutron on device memory:
+ * d_ekin[n] -> d_xs[n], d_ekin_final[n], d_mu[n] (any output may be NULL),
+ * d_status[n] optional.  Neutron i draws from stream (seed, i, callseq, clone
+ * index) of the handle; the call sequence advances by one per call.  Runs on
+ * 'stream' (a cudaStream_t, NULL = legacy default stream); asynchronous.
+ * Returns 0, or non-zero after setting the error state. */
+int ncgb_scatter_device( ncrystal_scatter_t, const double* d_ekin, unsigned long n,
+                         double* d_xs, double* d_ekin_final, double* d_mu,
+                         int32_t* d_status, void* stream );
+
+/* Same with FP32 energies in and FP32 results out; all arithmetic in the
+ * kernel stays FP64. */
+int ncgb_scatter_device_f32( ncrystal_scatter_t, const float* d_ekin, unsigned long n,
+                             float* d_xs, float* d_ekin_final, float* d_mu,
+                             int32_t* d_status, void* stream );
+
+/* Host-pointer FP32 batch (H2D + kernel + D2H inside, synchronous). */
+void ncgb_crosssection_nonoriented_many_f32( ncrystal_process_t, const float* ekin,
+                                             unsigned long n_ekin, float* results );
+void ncgb_samplescatterisotropic_many_f32( ncrystal_scatter_t, const float* ekin,
+                                           unsigned long n_ekin, float* results_ekin,
+                                           float* results_cos_scat_angle );
+
+/* Number of neutrons whose status was not NCGB_ST_OK in the last _many call on
+ * this thread. */
+unsigned long ncgb_last_nfailed( void );
+
+/* Host-only material tables (no GPU): load a bundle and build the flat tables
+ * in host memory.  NULL on failure (ncgb_tables_lasterror() says why). */
+void* ncgb_tables_load( const char* bundle_path );
+const char* ncgb_tables_lasterror( void );
+int ncgb_tables_view( void* tables, ncgb_material_view* out );
+unsigned long ncgb_tables_bytes( void* tables );
+void ncgb_tables_free( void* tables );
+/* Test support: one named table array / scalar of component 'comp'. */
+int ncgb_tables_array( void* tables, int comp, const char* name, const void** ptr, unsigned long* count );
+int ncgb_tables_scalar( void* tables, int comp, const char* name, double* out );
+
+/* Bytes of device memory holding a handle's material tables. */
+unsigned long ncgb_device_bytes( ncrystal_scatter_t );
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,599 @@
+// Table builder: material bundle -> flat ncgb_material_view arena.
+//
+// PowderBragg, ElIncScatter and FreeGas tables are taken over as loaded.  For
+// SABScatter the bundle holds the S(alpha,beta) kernel and the energy grid;
+// the per-energy-point Alg.1 samplers and cross-sections are derived here by
+// restating NCrystal's own construction, step for step, so that the tables are
+// the ones the reference would sample from:
+//
+//   logS and cumulative alpha integrals  NCSABIntegrator.cc:111-142
+//   activeGridRanges                      NCSABUtils.cc:460-536
+//   createTailedBreakdown                 NCSABUtils.cc:538-633
+//   analyseEnergyPoint                    NCSABIntegrator.cc:352-559
+//   PointwiseDist normalisation           NCPointwiseDist.cc:28-74
+//   SABXSProvider / SABSampler constants  NCSABXSProvider.cc:35-52,
+//                                         NCSABSampler.cc:41-57
+//
+// Compiled with -ffp-contract=off so that x86-64 and aarch64 hosts produce the
+// same bits (gcc contracts a*b+c into fma on aarch64 by default).
+#include "ncgb_host.hh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+namespace ncgb {
+
+  namespace {
+
+    constexpr double kInf = std::numeric_limits<double>::infinity();
+    constexpr double kInvSqrtPi = 0.564189583547756286948079451560772585844050629;
+
+    // Neumaier summation (NCMath.hh:194-202, :526-536).
+    struct StableSum {
+      double s = 0.0, c = 0.0;
+      void add( double x )
+      {
+        double t = s + x;
+        c += ( std::fabs(s) >= std::fabs(x) ) ? (s - t) + x : (x - t) + s;
+        s = t;
+      }
+      double sum() const { return s + c; }
+    };
+
+    // Kinematic alpha limits (NCKinUtils.hh:108-124 and :82-101).
+    struct ALim { double lo, hi; };
+    ALim alphaLimits( double ekin_div_kT, double beta )
+    {
+      const double kk = ekin_div_kT + beta;
+      if ( !( kk >= 0.0 ) )
+        return { 1.0, -1.0 };
+      const double a = kk + ekin_div_kT;
+      const double b = 2.0 * std::sqrt( ekin_div_kT * kk );
+      double aminus;
+      if ( std::fabs(beta) < 0.01 * ekin_div_kT ) {
+        const double x = beta / ekin_div_kT;
+        constexpr double c9 = -715./32768.;
+        constexpr double c8 = 429./16384.;
+        constexpr double c7 = -33./1024.;
+        constexpr double c6 = 21./512.;
+        constexpr double c5 = -7./128.;
+        constexpr double c4 = 5./64.;
+        constexpr double c3 = - 1./8.;
+        constexpr double c2 = 1./4.;
+        aminus = beta*x*(c2+x*(c3+x*(c4+x*(c5+x*(c6+x*(c7+x*(c8+x*c9)))))));
+      } else {
+        aminus = std::max( 0.0, a - b );
+      }
+      return { aminus, a + b };
+    }
+
+    inline bool inInterval( double lo, double hi, double x ) { return x >= lo && x <= hi; }
+
+    // NCSABUtils.hh:240-261
+    double integrateAlphaIntervalFast( double a1, double s1, double a2, double s2, double logs1, double logs2 )
+    {
+      const double da = a2-a1;
+      const double ps = s1+s2;
+      const double ds = s2-s1;
+      if ( std::min(s1,s2) < 1e-300 )
+        return 0.5*da*ps;
+      if ( std::fabs(ds) > 0.006*ps )
+        return da*ds/(logs2-logs1);
+      const double y = ds / ps;
+      const double c1 = 0.166666666666666666666666666666666666666666667;
+      const double c2 = 0.0444444444444444444444444444444444444444444444;
+      const double c3 = 0.0232804232804232804232804232804232804232804233;
+      const double ysq = y*y;
+      return da*ps*(0.5-ysq*(c1+ysq*(c2+ysq*c3)));
+    }
+
+    // NCSABUtils.hh:180-199
+    double interpLogLinFast( double a, double fa, double b, double fb, double x, double logfa, double logfb )
+    {
+      const double bma = b - a;
+      const double midpoint = 0.5 * ( b + a );
+      const bool linlin_mode = ( fa*fb == 0.0 );
+      if ( x < midpoint ) {
+        const double r = (x-a) / bma;
+        return ( linlin_mode ? ( fa + (fb-fa)*r ) : std::exp(logfa+(logfb-logfa)*r) );
+      } else {
+        const double s = (b-x) / bma;
+        return ( linlin_mode ? ( fb + (fa-fb)*s ) : std::exp(logfb+(logfa-logfb)*s) );
+      }
+    }
+
+    struct TailPoint { double alpha = 0.0, sval = 0.0, logsval = 0.0; };
+    struct TailedBreakdown {
+      double xs_front = 0.0, xs_middle = 0.0, xs_back = 0.0;
+      unsigned imiddle_low = 0, imiddle_upp = 0;
+      TailPoint front, back;
+      bool narrow = false;
+    };
+
+    // NCSABUtils.cc:538-633.  Spans are the beta row of alpha/S/logS/cumul.
+    TailedBreakdown tailedBreakdown( const double* alphaGrid, std::size_t na,
+                                     const double* sab, const double* logsab, const double* cumul,
+                                     double alpha_low, double alpha_upp,
+                                     unsigned aidx_low, unsigned aidx_upp )
+    {
+      alpha_low = std::min( std::max( alpha_low, alphaGrid[0] ), alphaGrid[na-1] );
+      alpha_upp = std::min( std::max( alpha_upp, alphaGrid[0] ), alphaGrid[na-1] );
+      TailedBreakdown tb;
+      if ( aidx_low == aidx_upp || alpha_low == alpha_upp )
+        return tb;
+      auto setTailPoint = [&]( TailPoint& tp, unsigned aidx, double alpha )
+      {
+        tp.alpha = alpha;
+        tp.sval = interpLogLinFast( alphaGrid[aidx], sab[aidx], alphaGrid[aidx+1], sab[aidx+1], alpha,
+                                    logsab[aidx], logsab[aidx+1] );
+        constexpr double z = std::numeric_limits<double>::min();
+        tp.logsval = std::log( std::max<double>( tp.sval, z ) );
+      };
+      if ( aidx_low + 1 == aidx_upp ) {
+        tb.narrow = true;
+        setTailPoint( tb.front, aidx_low, alpha_low );
+        setTailPoint( tb.back, aidx_low, alpha_upp );
+        tb.xs_front = integrateAlphaIntervalFast( tb.front.alpha, tb.front.sval, tb.back.alpha, tb.back.sval,
+                                                  tb.front.logsval, tb.back.logsval );
+        return tb;
+      }
+      tb.imiddle_low = aidx_low;
+      tb.imiddle_upp = aidx_upp;
+      if ( alpha_low >= alphaGrid[aidx_low] ) {
+        setTailPoint( tb.front, aidx_low, alpha_low );
+        tb.xs_front = integrateAlphaIntervalFast( tb.front.alpha, tb.front.sval,
+                                                  alphaGrid[aidx_low+1], sab[aidx_low+1],
+                                                  tb.front.logsval, logsab[aidx_low+1] );
+        ++tb.imiddle_low;
+      }
+      if ( alpha_upp <= alphaGrid[aidx_upp] ) {
+        setTailPoint( tb.back, aidx_upp-1, alpha_upp );
+        tb.xs_back = integrateAlphaIntervalFast( alphaGrid[aidx_upp-1], sab[aidx_upp-1],
+                                                 tb.back.alpha, tb.back.sval,
+                                                 logsab[aidx_upp-1], tb.back.logsval );
+        --tb.imiddle_upp;
+      }
+      tb.xs_middle = ( tb.imiddle_upp > tb.imiddle_low
+                       ? cumul[tb.imiddle_upp] - cumul[tb.imiddle_low]
+                       : 0.0 );
+      return tb;
+    }
+
+    // NCSABUtils.cc:460-536
+    void activeGridRanges( const std::vector<double>& alphaGrid, const std::vector<double>& betaGrid,
+                           double ekin_div_kT,
+                           std::vector<std::pair<uint16_t,uint16_t>>& out, std::size_t& ibeta_low )
+    {
+      const std::size_t na = alphaGrid.size();
+      if ( na >= std::numeric_limits<uint16_t>::max() )
+        throw Error("alpha grid too large");
+      ibeta_low = 0;
+      out.clear();
+      const double agrid_front = alphaGrid.front();
+      const double agrid_back = alphaGrid.back();
+      const std::size_t iLast = na - 1;
+      std::size_t iLow = 0, iUpp = na - 1;
+      for ( std::size_t ib = 0; ib < betaGrid.size(); ++ib ) {
+        const double beta = betaGrid[ib];
+        double alow(-1.0), aupp(-2.0);
+        if ( beta > -ekin_div_kT ) {
+          auto al = alphaLimits( ekin_div_kT, beta );
+          alow = al.lo;
+          aupp = al.hi;
+        }
+        if ( agrid_back <= alow || agrid_front >= aupp || aupp < alow ) {
+          if ( out.empty() ) {
+            ibeta_low = ib + 1;
+          } else {
+            auto nau = static_cast<uint16_t>(na);
+            out.emplace_back(nau,nau);
+          }
+          continue;
+        }
+        while ( alphaGrid[iLow] > alow && iLow > 0 )
+          --iLow;
+        while ( iLow < iLast && alphaGrid[iLow+1] <= alow )
+          ++iLow;
+        if ( iUpp < iLow )
+          iUpp = iLow;
+        while ( alphaGrid[iUpp] < aupp && iUpp < iLast )
+          ++iUpp;
+        while ( iUpp > 0 && alphaGrid[iUpp-1] >= aupp )
+          --iUpp;
+        out.emplace_back( static_cast<uint16_t>(iLow), static_cast<uint16_t>(iUpp) );
+      }
+    }
+
+    struct EPoint {
+      double xs = 0.0;
+      int kind = 0; // 0 no-scatter, 1 Alg.1
+      std::size_t ibeta_low = 0;
+      double fbkep = 1.0;
+      std::vector<double> bvals, bweights;
+      std::vector<ncgb_alpha_info> infos;
+    };
+
+    // NCSABIntegrator.cc:352-559 (doSampler = true)
+    EPoint analyseEnergyPoint( const SABInput& in, const std::vector<double>& logsab,
+                               const std::vector<double>& cumul, double ekin )
+    {
+      const auto& betaGrid = in.beta;
+      const auto& alphaGrid = in.alpha;
+      const std::size_t na = alphaGrid.size();
+      const double kT = in.kT;
+      const double ekin_div_kT = ekin / kT;
+      double beta_lower_limit = -ekin_div_kT;
+      bool starts_at_kinematic_endpoint = true;
+      if ( beta_lower_limit < betaGrid.front() ) {
+        double c1 = betaGrid.front() - (betaGrid.at(1)-betaGrid.front()) * 1e-6;
+        double c2 = betaGrid.front() - std::fabs(betaGrid.front())*1e-13;
+        double c3 = std::nextafter( betaGrid.front(), beta_lower_limit );
+        beta_lower_limit = std::min( c1, std::min( c2, c3 ) );
+        starts_at_kinematic_endpoint = false;
+      }
+      std::vector<std::pair<uint16_t,uint16_t>> alpharanges;
+      std::size_t ibeta_low;
+      activeGridRanges( alphaGrid, betaGrid, ekin_div_kT, alpharanges, ibeta_low );
+      EPoint res;
+      if ( ibeta_low >= betaGrid.size() )
+        return res; // no-scatter sampler, xs = 0
+      if ( ibeta_low > 0 && beta_lower_limit < betaGrid[ibeta_low-1] ) {
+        beta_lower_limit = betaGrid[ibeta_low-1];
+        starts_at_kinematic_endpoint = false;
+      }
+      const std::size_t nrel = betaGrid.size() - ibeta_low;
+      double prev_first = beta_lower_limit, prev_second = 0.0;
+      res.bvals.reserve( nrel + 1 );
+      res.bweights.reserve( nrel + 1 );
+      res.infos.reserve( nrel );
+      res.bvals.push_back( prev_first );
+      res.bweights.push_back( prev_second );
+      StableSum xs_total_stable;
+      bool next_bin_has_kinematic_endpoint = starts_at_kinematic_endpoint;
+      for ( std::size_t idx = 0; idx < nrel; ++idx ) {
+        const double beta = betaGrid[ibeta_low + idx];
+        if ( beta == beta_lower_limit )
+          continue;
+        auto al = alphaLimits( ekin_div_kT, beta );
+        const double alow = al.lo, aupp = al.hi;
+        double xs_at_this_beta = 0.0;
+        unsigned aidx_low = alpharanges[idx].first, aidx_upp = alpharanges[idx].second;
+        TailedBreakdown tb;
+        if ( aidx_upp > aidx_low && aupp > alow ) {
+          const std::size_t slice = na * ( idx + ibeta_low );
+          tb = tailedBreakdown( alphaGrid.data(), na, in.sab.data() + slice, logsab.data() + slice,
+                                cumul.data() + slice, alow, aupp, aidx_low, aidx_upp );
+          xs_at_this_beta = tb.xs_front + tb.xs_back + tb.xs_middle;
+        }
+        ncgb_alpha_info info;
+        std::memset( &info, 0, sizeof(info) );
+        if ( xs_at_this_beta > 0.0 ) {
+          info.front_alpha = tb.front.alpha;
+          info.front_sval = tb.front.sval;
+          info.front_logsval = tb.front.logsval;
+          info.back_alpha = tb.back.alpha;
+          info.back_sval = tb.back.sval;
+          info.back_logsval = tb.back.logsval;
+          if ( tb.narrow ) {
+            info.prob_front = 1.0;
+          } else {
+            info.prob_front = tb.xs_front / xs_at_this_beta;
+            info.prob_notback = 1.0 - tb.xs_back / xs_at_this_beta;
+            info.front_idx = tb.imiddle_low;
+            info.back_idx = tb.imiddle_upp;
+          }
+        } else {
+          info.prob_front = 2.0;
+          info.front_alpha = alow;
+          info.back_alpha = aupp;
+        }
+        res.infos.push_back( info );
+        if ( next_bin_has_kinematic_endpoint ) {
+          next_bin_has_kinematic_endpoint = false;
+          double db_real = ( beta - prev_first );
+          prev_first -= db_real * ( 1.0 / 3.0 );
+          res.bvals.front() = prev_first;
+        }
+        xs_total_stable.add( 0.5 * ( beta - prev_first ) * ( xs_at_this_beta + prev_second ) );
+        prev_first = beta;
+        prev_second = xs_at_this_beta;
+        res.bvals.push_back( prev_first );
+        res.bweights.push_back( prev_second );
+      }
+      double xs_total = xs_total_stable.sum() * in.sigma_bound / ( 4 * ekin_div_kT );
+      if ( !( xs_total >= 0.0 ) )
+        xs_total = 0.0;
+      res.xs = xs_total;
+      if ( xs_total == 0.0 )
+        return res; // no-scatter sampler
+      res.kind = 1;
+      res.ibeta_low = ibeta_low;
+      res.fbkep = ( starts_at_kinematic_endpoint ? beta_lower_limit : 1.0 );
+      return res;
+    }
+
+    // PointwiseDist construction (NCPointwiseDist.cc:28-74): normalised y and cdf.
+    void pointwiseDist( const std::vector<double>& x, std::vector<double> y,
+                        std::vector<double>& out_y, std::vector<double>& out_cdf )
+    {
+      if ( x.size() != y.size() || y.size() < 2 )
+        throw Error("PointwiseDist: input vector size error");
+      if ( !std::is_sorted( x.begin(), x.end() ) )
+        throw Error("PointwiseDist: points of the distribution are not sorted");
+      for ( double v : y )
+        if ( v < 0.0 || std::isinf(v) )
+          throw Error("PointwiseDist: function is negative or not finite");
+      std::vector<double> cdf;
+      cdf.reserve( y.size() );
+      StableSum totalArea;
+      cdf.push_back( 0.0 );
+      for ( std::size_t i = 1; i < y.size(); ++i ) {
+        double area = ( x[i] - x[i-1] ) * 0.5 * ( y[i] + y[i-1] );
+        if ( area < 0 )
+          throw Error("PointwiseDist: negative probability density");
+        totalArea.add( area );
+        cdf.push_back( totalArea.sum() );
+      }
+      double totalAreaVal = totalArea.sum();
+      if ( !( totalAreaVal > 0.0 ) )
+        throw Error("PointwiseDist: no area in distribution");
+      double normfact = 1.0 / totalAreaVal;
+      for ( auto& e : cdf )
+        e *= normfact;
+      for ( auto& e : y )
+        e *= normfact;
+      cdf.back() = 1.0;
+      out_y = std::move(y);
+      out_cdf = std::move(cdf);
+    }
+  }
+
+  double freeGasXSShapeASq( double a_squared )
+  {
+    if ( a_squared > 36.0 )
+      return 1.0 + 0.5 / a_squared;
+    const double a = std::sqrt( a_squared );
+    if ( a < 0.1 ) {
+      if ( a == 0.0 )
+        return kInf;
+      constexpr double c1 = 2.0/3.0;
+      constexpr double c2 = 1.0/15.0;
+      constexpr double c3 = 1.0/105.0;
+      constexpr double c4 = 1.0/756.0;
+      constexpr double c5 = 1.0/5940.0;
+      const double a2 = a_squared;
+      return kInvSqrtPi * ( 2.0 / a + a *( c1- a2*(c2-a2*(c3-a2*(c4-a2*c5)))));
+    }
+    const double inva = 1.0 / a;
+    return ( 1.0 + 0.5*inva*inva ) * std::erf(a) + kInvSqrtPi * std::exp(-a_squared)*inva;
+  }
+
+  SABDerived deriveSAB( const SABInput& in )
+  {
+    const std::size_t na = in.alpha.size(), nb = in.beta.size();
+    if ( na < 2 || nb < 2 || in.sab.size() != na*nb )
+      throw Error("SAB kernel with inconsistent grid sizes");
+    if ( in.egrid.size() < 2 )
+      throw Error("SAB energy grid too small");
+    SABDerived d;
+    // logS and cumulative alpha integrals (NCSABIntegrator.cc:119-138):
+    d.logsab.reserve( in.sab.size() );
+    for ( double e : in.sab )
+      d.logsab.push_back( e > 0.0 ? std::log(e) : -kInf );
+    d.cumul.assign( in.sab.size(), 0.0 );
+    std::size_t g = 0;
+    for ( std::size_t ib = 0; ib < nb; ++ib, ++g ) {
+      double c = 0.0;
+      for ( std::size_t ai = 0; ai + 1 < na; ++ai, ++g ) {
+        double integ = integrateAlphaIntervalFast( in.alpha[ai], in.sab[g], in.alpha[ai+1], in.sab[g+1],
+                                                   d.logsab[g], d.logsab[g+1] );
+        d.cumul[g+1] = ( c += integ );
+      }
+    }
+    // One sampler + xs value per energy-grid point (NCSABIntegrator.cc:283-309):
+    const std::size_t ne = in.egrid.size();
+    d.xs.reserve(ne);
+    int64_t off = 0;
+    for ( std::size_t ie = 0; ie < ne; ++ie ) {
+      EPoint ep = analyseEnergyPoint( in, d.logsab, d.cumul, in.egrid[ie] );
+      d.xs.push_back( ep.xs );
+      d.kind.push_back( ep.kind );
+      d.offset.push_back( off );
+      if ( ep.kind == 0 ) {
+        d.ibetaoffset.push_back(0);
+        d.nbeta.push_back(0);
+        d.fbkep.push_back(0.0);
+        continue;
+      }
+      std::vector<double> ny, ncdf;
+      pointwiseDist( ep.bvals, ep.bweights, ny, ncdf );
+      d.ibetaoffset.push_back( static_cast<int32_t>( ep.ibeta_low ) );
+      d.nbeta.push_back( static_cast<int32_t>( ep.bvals.size() ) );
+      d.fbkep.push_back( ep.fbkep );
+      d.bx.insert( d.bx.end(), ep.bvals.begin(), ep.bvals.end() );
+      d.by.insert( d.by.end(), ny.begin(), ny.end() );
+      d.bcdf.insert( d.bcdf.end(), ncdf.begin(), ncdf.end() );
+      d.info.insert( d.info.end(), ep.infos.begin(), ep.infos.end() );
+      ncgb_alpha_info pad;
+      std::memset( &pad, 0, sizeof(pad) );
+      while ( d.info.size() < d.bx.size() )
+        d.info.push_back( pad );
+      off += static_cast<int64_t>( ep.bvals.size() );
+    }
+    // Extender constants (NCSABXSProvider.cc:35-52, NCSABSampler.cc:41-57):
+    const double emax = in.egrid.back();
+    const double extxs_emax = in.ext_sigma_free * freeGasXSShapeASq( in.ext_ca * emax );
+    d.kext = ( d.xs.back() - extxs_emax ) * emax;
+    d.k1 = d.xs.back() * emax;
+    d.k2 = extxs_emax * emax;
+    return d;
+  }
+
+  // ---- arena ------------------------------------------------------------------
+
+  template<class T>
+  int64_t MaterialTables::put( const T* p, std::size_t n )
+  {
+    if ( n == 0 )
+      return 0;
+    std::size_t off = ( m_arena.size() + 255 ) & ~std::size_t(255);
+    m_arena.resize( off + n * sizeof(T) );
+    std::memcpy( m_arena.data() + off, p, n * sizeof(T) );
+    return static_cast<int64_t>( off ) + 1;
+  }
+
+  template<class T>
+  int64_t MaterialTables::put( const std::vector<T>& v ) { return put( v.data(), v.size() ); }
+
+  template int64_t MaterialTables::put<double>( const std::vector<double>& );
+  template int64_t MaterialTables::put<int32_t>( const std::vector<int32_t>& );
+  template int64_t MaterialTables::put<int64_t>( const std::vector<int64_t>& );
+
+  namespace {
+    template<class T>
+    const T* encodeOff( int64_t off ) { return reinterpret_cast<const T*>( static_cast<uintptr_t>(off) ); }
+    template<class T>
+    const T* reloc( const T* enc, const char* base )
+    {
+      uintptr_t off = reinterpret_cast<uintptr_t>(enc);
+      return off ? reinterpret_cast<const T*>( base + ( off - 1 ) ) : nullptr;
+    }
+  }
+
+  std::shared_ptr<MaterialTables> MaterialTables::build( const Bundle& b )
+  {
+    auto mt = std::make_shared<MaterialTables>();
+    mt->m_cfg = b.str("cfg");
+    mt->m_temperature = b.has("temperature") ? b.f64s("temperature") : -1.0;
+    ncgb_material_view& v = mt->m_rel;
+    std::memset( &v, 0, sizeof(v) );
+    const int64_t ncomp = b.i64s("ncomp");
+    if ( ncomp < 0 || ncomp > NCGB_MAX_COMP )
+      throw Error("material has too many components for the GPU path");
+    v.ncomp = static_cast<int32_t>( ncomp );
+    v.dom_elow = b.f64s("elow");
+    v.dom_ehigh = b.f64s("ehigh");
+    if ( ncomp == 0 ) {
+      // A null process: empty domain, so xs = 0 and scatterings leave E unchanged.
+      v.dom_elow = kInf;
+      v.dom_ehigh = kInf;
+    }
+    for ( int64_t ic = 0; ic < ncomp; ++ic ) {
+      const std::string p = "c" + std::to_string(ic) + ".";
+      ncgb_comp_view& c = v.comp[ic];
+      c.scale = b.f64s(p+"scale");
+      c.elow = b.f64s(p+"elow");
+      c.ehigh = b.f64s(p+"ehigh");
+      const std::string& type = b.str(p+"type");
+      if ( type == "PowderBragg" ) {
+        c.type = NCGB_COMP_BRAGG;
+        const auto& a = b.f64(p+"two_dE");
+        const auto& f = b.f64(p+"fdm_commul");
+        if ( a.size() != f.size() )
+          throw Error("PowderBragg table size mismatch");
+        c.bragg.n = static_cast<int64_t>( a.size() );
+        c.bragg.threshold = a.empty() ? kInf : a.front();
+        c.bragg.two_dE = encodeOff<double>( mt->put(a) );
+        c.bragg.fdm_commul = encodeOff<double>( mt->put(f) );
+      } else if ( type == "ElIncScatter" ) {
+        c.type = NCGB_COMP_ELINC;
+        const auto& msd = b.f64(p+"msd");
+        const auto& sig = b.f64(p+"sigma");
+        if ( msd.size() != sig.size() || msd.size() > NCGB_MAX_ELINC || msd.empty() )
+          throw Error("ElIncScatter with unsupported element count");
+        c.elinc.n = static_cast<int32_t>( msd.size() );
+        for ( std::size_t i = 0; i < msd.size(); ++i ) {
+          c.elinc.msd[i] = msd[i];
+          c.elinc.sigma[i] = sig[i];
+        }
+      } else if ( type == "SABScatter" ) {
+        c.type = NCGB_COMP_SAB;
+        SABInput in;
+        in.alpha = b.f64(p+"alpha");
+        in.beta = b.f64(p+"beta");
+        in.sab = b.f64(p+"sab");
+        in.egrid = b.f64(p+"egrid");
+        in.kT = b.f64s(p+"sab_kT");
+        in.sigma_bound = b.f64s(p+"sigma_bound");
+        in.ext_sigma_free = b.f64s(p+"ext_sigma_free");
+        in.ext_ca = b.f64s(p+"ext_ca");
+        SABDerived d = deriveSAB( in );
+        ncgb_sab_view& s = c.sab;
+        s.kT = b.f64s(p+"kT");
+        s.egrid_margin = b.f64s(p+"egrid_margin");
+        s.internal_scale = b.f64s(p+"internal_scale");
+        s.kext = d.kext;
+        s.k1 = d.k1;
+        s.k2 = d.k2;
+        s.ext_sigma_free = in.ext_sigma_free;
+        s.ext_ca = in.ext_ca;
+        s.ext_kT = in.kT;
+        s.ext_mass_amu = b.f64s(p+"ext_mass_amu");
+        s.sigma_bound = in.sigma_bound;
+        s.ne = static_cast<int32_t>( in.egrid.size() );
+        s.na = static_cast<int32_t>( in.alpha.size() );
+        s.nb = static_cast<int32_t>( in.beta.size() );
+        s.egrid = encodeOff<double>( mt->put(in.egrid) );
+        s.xs = encodeOff<double>( mt->put(d.xs) );
+        s.alpha = encodeOff<double>( mt->put(in.alpha) );
+        s.beta = encodeOff<double>( mt->put(in.beta) );
+        s.sab = encodeOff<double>( mt->put(in.sab) );
+        s.logsab = encodeOff<double>( mt->put(d.logsab) );
+        s.cumul = encodeOff<double>( mt->put(d.cumul) );
+        s.smp_kind = encodeOff<int32_t>( mt->put(d.kind) );
+        s.smp_ibetaoffset = encodeOff<int32_t>( mt->put(d.ibetaoffset) );
+        s.smp_nbeta = encodeOff<int32_t>( mt->put(d.nbeta) );
+        s.smp_offset = encodeOff<int64_t>( mt->put(d.offset) );
+        s.smp_fbkep = encodeOff<double>( mt->put(d.fbkep) );
+        s.bx = encodeOff<double>( mt->put(d.bx) );
+        s.by = encodeOff<double>( mt->put(d.by) );
+        s.bcdf = encodeOff<double>( mt->put(d.bcdf) );
+        s.info = encodeOff<ncgb_alpha_info>( mt->put( d.info.data(), d.info.size() ) );
+      } else if ( type == "FreeGas" ) {
+        c.type = NCGB_COMP_FREEGAS;
+        c.fg.kT = b.f64s(p+"kT");
+        c.fg.mass_amu = b.f64s(p+"mass_amu");
+        c.fg.sigma_free = b.f64s(p+"sigma_free");
+        c.fg.ca = b.f64s(p+"ca");
+      } else {
+        throw Error("unsupported component type in material bundle: " + type);
+      }
+    }
+    // Pad the arena so that it can be uploaded in 256-byte units.
+    mt->m_arena.resize( ( mt->m_arena.size() + 255 ) & ~std::size_t(255) );
+    return mt;
+  }
+
+  template int64_t MaterialTables::put<ncgb_alpha_info>( const ncgb_alpha_info*, std::size_t );
+
+  ncgb_material_view MaterialTables::relocate( const void* basev ) const
+  {
+    const char* base = static_cast<const char*>( basev );
+    ncgb_material_view v = m_rel;
+    for ( int ic = 0; ic < v.ncomp; ++ic ) {
+      ncgb_comp_view& c = v.comp[ic];
+      c.bragg.two_dE = reloc( c.bragg.two_dE, base );
+      c.bragg.fdm_commul = reloc( c.bragg.fdm_commul, base );
+      ncgb_sab_view& s = c.sab;
+      s.egrid = reloc( s.egrid, base );
+      s.xs = reloc( s.xs, base );
+      s.alpha = reloc( s.alpha, base );
+      s.beta = reloc( s.beta, base );
+      s.sab = reloc( s.sab, base );
+      s.logsab = reloc( s.logsab, base );
+      s.cumul = reloc( s.cumul, base );
+      s.smp_kind = reloc( s.smp_kind, base );
+      s.smp_ibetaoffset = reloc( s.smp_ibetaoffset, base );
+      s.smp_nbeta = reloc( s.smp_nbeta, base );
+      s.smp_offset = reloc( s.smp_offset, base );
+      s.smp_fbkep = reloc( s.smp_fbkep, base );
+      s.bx = reloc( s.bx, base );
+      s.by = reloc( s.by, base );
+      s.bcdf = reloc( s.bcdf, base );
+      s.info = reloc( s.info, base );
+    }
+    return v;
+  }
+}

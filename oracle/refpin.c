@@ -1,0 +1,64 @@
+/*
+ * refpin.c -- drives the reference NCrystal library (oracle/_ref) with the
+ * GPU path's per-neutron Philox streams.  TEST INFRASTRUCTURE ONLY.
+ *
+ * ncrystal_setrandgen (ncrystal.h, ncrystal.cc:1993-2001) installs a plain C
+ * function as the random source of every Scatter created afterwards.  The
+ * function below returns draw j of the stream of the neutron currently being
+ * scattered, so each call of the reference's scalar
+ * ncrystal_samplescatterisotropic (ncrystal.cc:1168-1199) consumes exactly the
+ * numbers that the oracle and the CUDA kernels consume for that neutron.  The
+ * result pins (E', mu), cross-sections and draw counts per neutron, not just
+ * in distribution.
+ *
+ * Built only where the reference sources exist (links oracle/_ref/libNCrystal).
+ */
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "NCrystal/cinterface/ncrystal.h"
+#include "ncgb_philox.h"
+
+static ncgb_rng g_rng;
+static int64_t g_ndraws;
+
+static double refpin_rand( void )
+{
+  ++g_ndraws;
+  return ncgb_rng_generate( &g_rng );
+}
+
+/* Returns 0 on success; status[i] is 1 if the reference raised an error for
+ * neutron i (its outputs then hold the reference's sentinels). */
+int refpin_run( const char* cfg, uint64_t seed, uint32_t callseq, uint32_t stream,
+                const double* ekin, int64_t n,
+                double* out_xs, double* out_ef, double* out_mu,
+                int32_t* out_ndraws, int32_t* out_status )
+{
+  ncrystal_sethaltonerror( 0 );
+  ncrystal_setmsghandler( NULL );
+  ncrystal_setrandgen( refpin_rand );
+  ncrystal_scatter_t sc = ncrystal_create_scatter( cfg );
+  if ( ncrystal_error() ) {
+    fprintf( stderr, "refpin: could not create %s: %s\n", cfg, ncrystal_lasterror() );
+    ncrystal_clearerror();
+    return 1;
+  }
+  ncrystal_process_t pr = ncrystal_cast_scat2proc( sc );
+  for ( int64_t i = 0; i < n; ++i ) {
+    ncrystal_crosssection_nonoriented( pr, ekin[i], &out_xs[i] );
+    ncgb_rng_init( &g_rng, seed, (uint32_t)i, callseq, stream );
+    g_ndraws = 0;
+    ncrystal_samplescatterisotropic( sc, ekin[i], &out_ef[i], &out_mu[i] );
+    out_status[i] = 0;
+    if ( ncrystal_error() ) {
+      out_status[i] = 1;
+      ncrystal_clearerror();
+    }
+    out_ndraws[i] = (int32_t)g_ndraws;
+  }
+  ncrystal_unref( &sc );
+  ncrystal_setrandgen( NULL );
+  return 0;
+}
