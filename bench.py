@@ -1,0 +1,350 @@
+#!/usr/bin/env python3
+"""Benchmark of the batched non-oriented scattering path on GB300.
+
+One step = one pass of the hot path over one batch: for every neutron its
+total cross-section and one sampled isotropic scatter (E', mu).
+
+Default workload ("al2o3_large"): Al2O3_sg167_Corundum.ncmat;temp=293K;
+dcutoff=0.2 (several thousand Bragg planes, ElInc, two S(alpha,beta)
+kernels), 2^24 neutrons with energies log-uniform in [1e-4, 1] eV (seeded),
+FP32 energies in and FP32 results out, FP64 arithmetic.
+
+  value  -- device-resident batch: fused kernel, inputs already in HBM
+  e2e    -- the same through the C ABI with host (pinned) arrays, copies
+            inside the timed region (ncgb_xs_scatter_many_f32)
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+       [--workload al2o3_large|al_small|pe]
+Under torchrun (N>1) each rank runs an independent replica on its own GPU
+(the path has no cross-neutron exchange: replicas only) and rank 0 prints the
+JSON line with the whole-job throughput.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "neutron scatters/s on 1 GB300, learned-proposal vs plain GPU sampler (KS p>0.01)"
+UNIT = "scatters/s"
+
+WORKLOADS = {
+    # name: (cfg, n, energy generator, io dtype, algorithmic bytes/neutron)
+    "al2o3_large": ("Al2O3_sg167_Corundum.ncmat;temp=293K;dcutoff=0.2", 1 << 24,
+                    lambda n, k: __import__("ncrystal_gb300.workloads", fromlist=["x"]).loguniform_energies(
+                        n, 1e-4, 1.0, 0x5EED0002 + k), "f32", 16),
+    "al_small": ("Al_sg225.ncmat;temp=293K", 1 << 20,
+                 lambda n, k: __import__("ncrystal_gb300.workloads", fromlist=["x"]).al_wavelength_energies(
+                     n, 0x5EED0001 + k), "f64", 32),
+    "pe": ("Polyethylene_CH2.ncmat;temp=293K", 1 << 24,
+           lambda n, k: __import__("ncrystal_gb300.workloads", fromlist=["x"]).loguniform_energies(
+               n, 1e-4, 1.0, 0x5EED0004 + k), "f64", 32),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="al2o3_large", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-seconds", type=float, default=8.0,
+                    help="wall-clock budget of the CPU baseline sample")
+    return ap.parse_args()
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel, workload):
+    """DRAM bytes per launch from the committed ncu summary, if any
+    (profiles/<kernel>_<workload>.md, line 'dram_bytes_per_launch: X')."""
+    p = os.path.join(ROOT, "profiles", "%s_%s.md" % (kernel, workload))
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[2:6]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(cfg, energies, seconds, threads=None):
+    """The CPU oracle (a plain-C restatement of NCrystal's per-neutron
+    evaluation) timed on this host's cores on a bounded sample of the same
+    workload: cross-section + one scatter per neutron."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import ncrystal_gb300._build as B
+    from oracle.pyoracle import HostMaterial
+    threads = threads or os.cpu_count() or 1
+    m = HostMaterial(os.path.join(B.BUNDLES, B.bundle_file_name(cfg)))
+    e = np.ascontiguousarray(energies, dtype=np.float64)
+
+    def work(chunk, off):
+        m.xs(chunk)
+        m.scatter(chunk, 12345, index_offset=off)
+
+    # calibrate on a small slice, then size the sample to the time budget
+    t0 = time.perf_counter()
+    cal = e[:20000]
+    work(cal, 0)
+    rate1 = len(cal) / max(time.perf_counter() - t0, 1e-6)
+    nsample = int(min(len(e), max(threads * 20000, rate1 * threads * seconds)))
+    sample = e[:nsample]
+    chunks = np.array_split(sample, threads * 4)
+    offs = np.cumsum([0] + [len(c) for c in chunks[:-1]])
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(work, chunks, offs))
+    dt = time.perf_counter() - t0
+    return {"value": nsample / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "first %d neutrons of the workload (xs + one scatter each), %d threads, %.1f s"
+                      % (nsample, threads, dt)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    cfg, n, gen, io, bpn = WORKLOADS[args.workload]
+    import __graft_entry__
+    __graft_entry__.build()
+    energies = gen(n, 0)
+    if io == "f32":
+        energies = energies.astype(np.float32).astype(np.float64)
+    vals = []
+    base = None
+    per_step = max(1.0, 60.0 / max(1, args.steps + args.warmup))
+    for i in range(args.warmup + args.steps):
+        b = cpu_baseline(cfg, energies, min(per_step, args.cpu_seconds))
+        if i >= args.warmup:
+            vals.append(b["value"])
+            base = b
+    v = statistics.median(vals)
+    base["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "cfg": cfg, "neutrons": n, "io": io},
+            "impl": "reference", "cpu_baseline": base,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args):
+    import torch
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__
+    if rank == 0 or world == 1:
+        __graft_entry__.build()
+    if dist:
+        dist.barrier()
+        __graft_entry__.build()  # no-op when up to date; loads the package
+    import ncrystal_gb300 as NC
+
+    cfg, n, gen, io, bpn = WORKLOADS[args.workload]
+    dt_t = torch.float32 if io == "f32" else torch.float64
+    np_t = np.float32 if io == "f32" else np.float64
+    energies = gen(n, rank).astype(np_t)
+    sc = NC.createScatter(cfg, seed=0xB0057 + rank)
+    dev = torch.device("cuda", local)
+    d_e = torch.from_numpy(energies).to(dev)
+    d_xs = torch.empty_like(d_e)
+    d_ef = torch.empty_like(d_e)
+    d_mu = torch.empty_like(d_e)
+    stream = torch.cuda.current_stream(dev)
+
+    # correctness gate before timing: no neutron may fail
+    d_st = torch.zeros(n, dtype=torch.int32, device=dev)
+    sc.scatter_device(d_e, d_xs, d_ef, d_mu, d_st, stream=stream)
+    torch.cuda.synchronize()
+    nbad = int((d_st != 0).sum().item())
+    if nbad:
+        raise SystemExit("bench: %d neutrons failed to sample" % nbad)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        sc.scatter_device(d_e, d_xs, d_ef, d_mu, None, stream=stream)
+    barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sc.scatter_device(d_e, d_xs, d_ef, d_mu, None, stream=stream)
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * n * args.steps / (ms / 1e3)
+    kernel_s = ms_per_step / 1e3  # one fused kernel launch per step
+    peak, peak_kind = measured_peaks()
+    achieved = bpn * n / kernel_s / 1e9
+
+    # ---- e2e: host (pinned) arrays through the C ABI, copies timed ----------
+    h_e = torch.from_numpy(energies).pin_memory()
+    h_xs = torch.empty(n, dtype=dt_t).pin_memory()
+    h_ef = torch.empty(n, dtype=dt_t).pin_memory()
+    h_mu = torch.empty(n, dtype=dt_t).pin_memory()
+    f32 = io == "f32"
+
+    def e2e_step():
+        sc.xs_scatter_host_ptr(h_e.data_ptr(), n, h_xs.data_ptr(), h_ef.data_ptr(), h_mu.data_ptr(), f32)
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    barrier()
+    e2e_steps = max(3, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    esize = 4 if f32 else 8
+    chunk = 1 << 22
+    e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": n * esize, "d2h_bytes_per_step": 3 * n * esize,
+           "steps": e2e_steps, "gpu_launches_per_step": (n + chunk - 1) // chunk,
+           "api": "ncgb_xs_scatter_many%s (C ABI, pinned host arrays)" % ("_f32" if f32 else "")}
+
+    # results sanity: outputs of the last step
+    mu_h = d_mu.float().cpu().numpy()
+    if not np.all(np.abs(mu_h) <= 1.0):
+        raise SystemExit("bench: mu outside [-1,1]")
+
+    if rank == 0:
+        base = cpu_baseline(cfg, energies.astype(np.float64), args.cpu_seconds)
+        clocks = clk.summary()
+        traffic = profiled_traffic("k_xs_scatter", args.workload)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "cfg": cfg, "neutrons_per_gpu": n, "io": io,
+                       "sampler": "plain (Alg.1 tables)", "parallelism": "replicas%d" % world,
+                       "l2": "tables L2-resident; per-step I/O %d MB exceeds nothing reused" % (bpn * n >> 20),
+                       "inputs": "device-resident, not re-read from host"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": traffic, "bytes_per_neutron": bpn,
+                         "kernel": "k_xs_scatter", "kernel_ms": ms_per_step},
+            "cpu_baseline": base,
+            "e2e": e2e,
+            "clocks": clocks,
+            "gpu_launches": args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -103,6 +103,7 @@ void ncrystal_genscatter_nonoriented_many( ncrystal_scatter_t,
  * reference, an error prints its message and calls exit(1) unless
  * ncrystal_sethaltonerror(0) was called first. */
 int ncrystal_sethaltonerror( int );
+int ncrystal_setquietonerror( int );
 int ncrystal_error( void );
 const char * ncrystal_lasterror( void );
 const char * ncrystal_lasterrortype( void );
@@ -120,6 +121,8 @@ const char * ncrystal_version_str( void );
 #define NCGB_ST_OK 0
 #define NCGB_ST_LOOPCAP 1      /* rejection loop cap hit (reference: CalcError) */
 #define NCGB_ST_UNSUPPORTED 2  /* free-gas sampling (not yet on the GPU) */
+#define NCGB_ST_CALCERROR 3    /* E*E' == 0 in the (alpha,beta) -> mu conversion
+                                  (reference: CalcError, NCKinUtils.cc:40-45) */
 
 /* Fused cross-section + one isotropic scatter per neutron on device memory:
  * d_ekin[n] -> d_xs[n], d_ekin_final[n], d_mu[n] (any output may be NULL),
@@ -143,6 +146,17 @@ void ncgb_crosssection_nonoriented_many_f32( ncrystal_process_t, const float* ek
 void ncgb_samplescatterisotropic_many_f32( ncrystal_scatter_t, const float* ekin,
                                            unsigned long n_ekin, float* results_ekin,
                                            float* results_cos_scat_angle );
+
+/* Fused cross-section + scatter with HOST arrays: ekin[n] -> xs[n], E'[n],
+ * mu[n] (any output may be NULL), FP64 or FP32.  Copies in, runs and copies
+ * out in chunks on two streams so that transfers overlap the kernels (host
+ * arrays in pinned memory make the copies asynchronous).  Neutron i uses
+ * stream index i, like ncgb_scatter_device.  Synchronous; on error the outputs
+ * hold the samplescatter sentinels (xs -1, E' -1, mu -999). */
+void ncgb_xs_scatter_many( ncrystal_scatter_t, const double* ekin, unsigned long n,
+                           double* xs, double* ekin_final, double* mu );
+void ncgb_xs_scatter_many_f32( ncrystal_scatter_t, const float* ekin, unsigned long n,
+                               float* xs, float* ekin_final, float* mu );
 
 /* Number of neutrons whose status was not NCGB_ST_OK in the last _many call on
  * this thread. */

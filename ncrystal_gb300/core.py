@@ -1,0 +1,321 @@
+"""Python face of the GPU scattering path, shaped like NCrystal's own Python
+API for non-oriented materials (ncrystal_python/src/NCrystal/core.py:
+createScatter, Process.crossSectionIsotropic, Scatter.sampleScatterIsotropic,
+Scatter.clone; _chooks.py:499-560 for the array handling).
+
+Everything goes through the C ABI of libncrystal_gb300.so (ctypes); the
+per-neutron work runs in its CUDA kernels.  If the library is not built, or no
+GPU is present, calls fail with an exception: there is no CPU fallback.
+"""
+import ctypes as _C
+import os as _os
+
+import numpy as _np
+
+from . import _build
+
+
+class NCException(RuntimeError):
+    """Base error (mirrors NCrystal.exceptions.NCException)."""
+
+
+class NCFileNotFound(NCException):
+    pass
+
+
+class NCBadInput(NCException):
+    pass
+
+
+class NCCalcError(NCException):
+    pass
+
+
+class NCLogicError(NCException):
+    pass
+
+
+_ERRTYPES = {"FileNotFound": NCFileNotFound, "BadInput": NCBadInput,
+             "CalcError": NCCalcError, "LogicError": NCLogicError}
+
+_lib = None
+
+
+class _Handle(_C.Structure):
+    _fields_ = [("internal", _C.c_void_p)]
+
+
+_dblp = _C.POINTER(_C.c_double)
+
+
+def lib():
+    """The loaded C library (built on first use if sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.library_path()
+    if not _os.path.exists(path):
+        raise ImportError("libncrystal_gb300.so is not built (run __graft_entry__.build()); "
+                          "the GPU scattering path has no CPU fallback")
+    L = _C.CDLL(path)
+    H = _Handle
+    sig = {
+        "ncrystal_create_scatter": (H, [_C.c_char_p]),
+        "ncrystal_create_scatter_builtinrng": (H, [_C.c_char_p, _C.c_ulong]),
+        "ncrystal_clone_scatter": (H, [H]),
+        "ncrystal_clone_scatter_rngbyidx": (H, [H, _C.c_ulong]),
+        "ncrystal_clone_scatter_rngforcurrentthread": (H, [H]),
+        "ncrystal_cast_scat2proc": (H, [H]),
+        "ncrystal_unref": (None, [_C.c_void_p]),
+        "ncrystal_refcount": (_C.c_int, [_C.c_void_p]),
+        "ncrystal_valid": (_C.c_int, [_C.c_void_p]),
+        "ncrystal_name": (_C.c_char_p, [H]),
+        "ncrystal_domain": (None, [H, _dblp, _dblp]),
+        "ncrystal_isnonoriented": (_C.c_int, [H]),
+        "ncrystal_crosssection_nonoriented": (None, [H, _C.c_double, _dblp]),
+        "ncrystal_crosssection_nonoriented_many": (None, [H, _C.c_void_p, _C.c_ulong, _C.c_ulong, _C.c_void_p]),
+        "ncrystal_samplescatterisotropic": (None, [H, _C.c_double, _dblp, _dblp]),
+        "ncrystal_samplescatterisotropic_many": (None, [H, _C.c_void_p, _C.c_ulong, _C.c_ulong,
+                                                        _C.c_void_p, _C.c_void_p]),
+        "ncrystal_genscatter_nonoriented_many": (None, [H, _C.c_void_p, _C.c_ulong, _C.c_ulong,
+                                                        _C.c_void_p, _C.c_void_p]),
+        "ncrystal_sethaltonerror": (_C.c_int, [_C.c_int]),
+        "ncrystal_setquietonerror": (_C.c_int, [_C.c_int]),
+        "ncrystal_error": (_C.c_int, []),
+        "ncrystal_lasterror": (_C.c_char_p, []),
+        "ncrystal_lasterrortype": (_C.c_char_p, []),
+        "ncrystal_clearerror": (None, []),
+        "ncrystal_version": (_C.c_int, []),
+        "ncgb_scatter_device": (_C.c_int, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p,
+                                           _C.c_void_p, _C.c_void_p, _C.c_void_p]),
+        "ncgb_scatter_device_f32": (_C.c_int, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p,
+                                               _C.c_void_p, _C.c_void_p, _C.c_void_p]),
+        "ncgb_crosssection_nonoriented_many_f32": (None, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p]),
+        "ncgb_samplescatterisotropic_many_f32": (None, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p,
+                                                        _C.c_void_p]),
+        "ncgb_xs_scatter_many": (None, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p, _C.c_void_p]),
+        "ncgb_xs_scatter_many_f32": (None, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p,
+                                            _C.c_void_p]),
+        "ncgb_last_nfailed": (_C.c_ulong, []),
+        "ncgb_device_bytes": (_C.c_ulong, [H]),
+        "ncgb_tables_load": (_C.c_void_p, [_C.c_char_p]),
+        "ncgb_tables_lasterror": (_C.c_char_p, []),
+        "ncgb_tables_view": (_C.c_int, [_C.c_void_p, _C.c_void_p]),
+        "ncgb_tables_bytes": (_C.c_ulong, [_C.c_void_p]),
+        "ncgb_tables_free": (None, [_C.c_void_p]),
+        "ncgb_tables_array": (_C.c_int, [_C.c_void_p, _C.c_int, _C.c_char_p, _C.POINTER(_C.c_void_p),
+                                         _C.POINTER(_C.c_ulong)]),
+        "ncgb_tables_scalar": (_C.c_int, [_C.c_void_p, _C.c_int, _C.c_char_p, _dblp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    # Errors become Python exceptions, as in NCrystal's Python layer.
+    L.ncrystal_sethaltonerror(0)
+    L.ncrystal_setquietonerror(1)
+    _lib = L
+    return L
+
+
+def _check():
+    L = lib()
+    if L.ncrystal_error():
+        msg = (L.ncrystal_lasterror() or b"").decode()
+        typ = (L.ncrystal_lasterrortype() or b"").decode()
+        L.ncrystal_clearerror()
+        raise _ERRTYPES.get(typ, NCException)("%s [%s]" % (msg, typ) if typ else msg)
+
+
+def _prepare_many(ekin, repeat):
+    """Same conventions as NCrystal's _chooks.py:499-507."""
+    if repeat is None and not hasattr(ekin, "__len__"):
+        return None
+    repeat = 1 if repeat is None else int(repeat)
+    arr = _np.ascontiguousarray(_np.asarray(ekin, dtype=_np.float64).reshape(-1)) \
+        if hasattr(ekin, "__len__") else _np.ones(1) * float(ekin)
+    return arr, len(arr), repeat
+
+
+class Process:
+    """A material's scattering process on the GPU (non-oriented)."""
+
+    def __init__(self, handle, cfgstr):
+        self._h = handle
+        self._cfg = cfgstr
+
+    def __del__(self):
+        try:
+            if self._h is not None and self._h.internal:
+                lib().ncrystal_unref(_C.byref(self._h))
+        except Exception:
+            pass
+
+    @property
+    def cfgstr(self):
+        return self._cfg
+
+    @property
+    def name(self):
+        return lib().ncrystal_name(self._h).decode()
+
+    def domain(self):
+        a, b = _C.c_double(), _C.c_double()
+        lib().ncrystal_domain(self._h, _C.byref(a), _C.byref(b))
+        _check()
+        return a.value, b.value
+
+    def isNonOriented(self):
+        return True
+
+    def isOriented(self):
+        return False
+
+    def crossSectionIsotropic(self, ekin, repeat=None):
+        """Cross-sections in barn (NCrystal core.py:1277); arrays in, arrays out."""
+        L = lib()
+        many = _prepare_many(ekin, repeat)
+        if many is None:
+            r = _C.c_double()
+            L.ncrystal_crosssection_nonoriented(self._h, float(ekin), _C.byref(r))
+            _check()
+            return r.value
+        arr, n, rep = many
+        out = _np.empty(n * rep, dtype=_np.float64)
+        if n * rep:
+            L.ncrystal_crosssection_nonoriented_many(self._h, arr.ctypes.data, n, rep, out.ctypes.data)
+            _check()
+        return out
+
+    def xsect(self, ekin=None, wl=None, repeat=None):
+        if (ekin is None) == (wl is None):
+            raise NCBadInput("xsect: give exactly one of ekin and wl")
+        if wl is not None:
+            w = _np.asarray(wl, dtype=_np.float64)
+            ekin = 0.081804209605330899 / (w * w)
+            if w.ndim == 0:
+                ekin = float(ekin)
+        return self.crossSectionIsotropic(ekin, repeat)
+
+    def device_bytes(self):
+        return lib().ncgb_device_bytes(self._h)
+
+
+class Scatter(Process):
+    """A scattering process with its own random streams (NCrystal core.py:1411-1520)."""
+
+    def sampleScatterIsotropic(self, ekin, repeat=None):
+        """Returns (ekin_final, mu) -- NCrystal core.py:1492."""
+        L = lib()
+        many = _prepare_many(ekin, repeat)
+        if many is None:
+            ef, mu = _C.c_double(), _C.c_double()
+            L.ncrystal_samplescatterisotropic(self._h, float(ekin), _C.byref(ef), _C.byref(mu))
+            _check()
+            return ef.value, mu.value
+        arr, n, rep = many
+        ef = _np.empty(n * rep, dtype=_np.float64)
+        mu = _np.empty(n * rep, dtype=_np.float64)
+        if n * rep:
+            L.ncrystal_samplescatterisotropic_many(self._h, arr.ctypes.data, n, rep, ef.ctypes.data,
+                                                   mu.ctypes.data)
+            _check()
+        return ef, mu
+
+    def genScatterNonOriented(self, ekin, repeat=None):
+        """Obsolete NCrystal call: returns (angle, delta_ekin) arrays."""
+        arr, n, rep = _prepare_many(ekin if hasattr(ekin, "__len__") else [ekin], repeat)
+        ang = _np.zeros(n * rep, dtype=_np.float64)
+        de = _np.zeros(n * rep, dtype=_np.float64)
+        if n * rep:
+            lib().ncrystal_genscatter_nonoriented_many(self._h, arr.ctypes.data, n, rep, ang.ctypes.data,
+                                                       de.ctypes.data)
+            _check()
+        return ang, de
+
+    def clone(self, rng_stream_index=None, for_current_thread=False):
+        L = lib()
+        if rng_stream_index is not None:
+            h = L.ncrystal_clone_scatter_rngbyidx(self._h, int(rng_stream_index))
+        elif for_current_thread:
+            h = L.ncrystal_clone_scatter_rngforcurrentthread(self._h)
+        else:
+            h = L.ncrystal_clone_scatter(self._h)
+        _check()
+        return Scatter(h, self._cfg)
+
+    # ---- device-resident batches (torch CUDA tensors or raw pointers) --------
+    def scatter_device(self, ekin, xs=None, ekin_final=None, mu=None, status=None, stream=None):
+        """Fused cross-section + scatter on device arrays.  'ekin' and outputs are
+        torch CUDA tensors (float64, or all float32) or None.  Asynchronous on
+        'stream' (a torch.cuda.Stream, default: torch's current stream)."""
+        import torch
+        n = ekin.numel()
+        f32 = ekin.dtype == torch.float32
+        p = (lambda t: 0 if t is None else t.data_ptr())
+        if stream is None:
+            stream = torch.cuda.current_stream(ekin.device)
+        fn = lib().ncgb_scatter_device_f32 if f32 else lib().ncgb_scatter_device
+        rc = fn(self._h, ekin.data_ptr(), n, p(xs), p(ekin_final), p(mu), p(status), stream.cuda_stream)
+        if rc:
+            _check()
+        return xs, ekin_final, mu
+
+    def scatter_device_ptr(self, d_ekin, n, d_xs, d_ef, d_mu, d_status, cuda_stream, f32=False):
+        fn = lib().ncgb_scatter_device_f32 if f32 else lib().ncgb_scatter_device
+        rc = fn(self._h, d_ekin, n, d_xs, d_ef, d_mu, d_status, cuda_stream)
+        if rc:
+            _check()
+
+    def xs_scatter_host_ptr(self, ekin_ptr, n, xs_ptr, ef_ptr, mu_ptr, f32=False):
+        """Fused xs + scatter on host arrays given as raw pointers (pinned
+        memory makes the chunked copies asynchronous)."""
+        fn = lib().ncgb_xs_scatter_many_f32 if f32 else lib().ncgb_xs_scatter_many
+        fn(self._h, ekin_ptr, n, xs_ptr, ef_ptr, mu_ptr)
+        _check()
+
+    def xs_scatter(self, ekin):
+        """Fused xs + scatter on a numpy array (float64 or float32):
+        returns (xs, ekin_final, mu); neutron i uses stream index i."""
+        arr = _np.ascontiguousarray(ekin)
+        f32 = arr.dtype == _np.float32
+        if not f32:
+            arr = arr.astype(_np.float64, copy=False)
+        n = len(arr)
+        xs, ef, mu = (_np.empty(n, dtype=arr.dtype) for _ in range(3))
+        self.xs_scatter_host_ptr(arr.ctypes.data, n, xs.ctypes.data, ef.ctypes.data, mu.ctypes.data, f32)
+        return xs, ef, mu
+
+    def crossSectionIsotropic_f32(self, ekin):
+        arr = _np.ascontiguousarray(ekin, dtype=_np.float32)
+        out = _np.empty(len(arr), dtype=_np.float32)
+        lib().ncgb_crosssection_nonoriented_many_f32(self._h, arr.ctypes.data, len(arr), out.ctypes.data)
+        _check()
+        return out
+
+    def sampleScatterIsotropic_f32(self, ekin):
+        arr = _np.ascontiguousarray(ekin, dtype=_np.float32)
+        ef = _np.empty(len(arr), dtype=_np.float32)
+        mu = _np.empty(len(arr), dtype=_np.float32)
+        lib().ncgb_samplescatterisotropic_many_f32(self._h, arr.ctypes.data, len(arr), ef.ctypes.data,
+                                                   mu.ctypes.data)
+        _check()
+        return ef, mu
+
+
+def createScatter(cfgstr, seed=None):
+    """NCrystal.createScatter (core.py:1602) on the GPU path.  'seed' selects
+    the Philox key (ncrystal_create_scatter_builtinrng)."""
+    L = lib()
+    if seed is None:
+        h = L.ncrystal_create_scatter(cfgstr.encode())
+    else:
+        h = L.ncrystal_create_scatter_builtinrng(cfgstr.encode(), int(seed))
+    _check()
+    if not h.internal:
+        raise NCException("could not create scatter for %r" % cfgstr)
+    return Scatter(h, cfgstr)
+
+
+def createProcess(cfgstr):
+    return createScatter(cfgstr)

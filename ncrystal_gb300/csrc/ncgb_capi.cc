@@ -1,0 +1,819 @@
+// C ABI of the GPU scattering path: NCrystal-compatible handles, error state
+// and batch entry points (declared in include/ncrystal_gb300.h).
+//
+// Mirrors ncrystal_core/src/cinterface/ncrystal.cc of NCrystal 4.4.2:
+//   handles      ncrystal.cc:104-200 (type-tagged, ref-counted, unref by address)
+//   errors       ncrystal.cc:281-322 (message, type, custom handler, halt-on-error)
+//   _many calls  ncrystal.cc:1107-1141, :1201-1245, :1301-1324 (index layout and
+//                error sentinels)
+// The per-neutron work runs in the CUDA kernels of ncgb_kernels.cu; there is
+// no CPU evaluation path in this library.
+#include "ncgb_host.hh"
+#include "ncgb_launch.hh"
+#include "ncrystal_gb300.h"
+
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+namespace {
+
+  // ---- error state (ncrystal.cc:281-322) ------------------------------------
+  int g_quiet = 0;
+  int g_halt = 1;
+  int g_waserror = 0;
+  char g_errmsg[512];
+  char g_errtype[64];
+  void (*g_handler)(char*,char*) = nullptr;
+  std::mutex g_errmtx;
+
+  void setError( const char* msg, const char* etype ) noexcept
+  {
+    std::lock_guard<std::mutex> lock( g_errmtx );
+    if ( !etype )
+      etype = "ncrystal_c-interface";
+    std::strncpy( g_errmsg, msg, sizeof(g_errmsg) - 1 );
+    std::strncpy( g_errtype, etype, sizeof(g_errtype) - 1 );
+    g_errmsg[sizeof(g_errmsg)-1] = '\0';
+    g_errtype[sizeof(g_errtype)-1] = '\0';
+    if ( g_handler )
+      (*g_handler)( g_errtype, g_errmsg );
+    g_waserror = 1;
+    if ( !g_quiet )
+      std::printf( "NCrystal ERROR [%s]: %s\n", g_errtype, g_errmsg );
+    if ( g_halt ) {
+      std::printf( "NCrystal terminating due to ERROR\n" );
+      std::fflush( stdout );
+      std::exit( 1 );
+    }
+  }
+
+  // Exception types named like NCrystal's (NCException.hh:105-175).
+  struct TypedError : std::runtime_error {
+    std::string type;
+    TypedError( const std::string& t, const std::string& m ) : std::runtime_error(m), type(t) {}
+  };
+
+  void handleError( const std::exception& e ) noexcept
+  {
+    if ( auto te = dynamic_cast<const TypedError*>( &e ) )
+      setError( te->what(), te->type.c_str() );
+    else if ( dynamic_cast<const ncgb::Error*>( &e ) )
+      setError( e.what(), "BadInput" );
+    else
+      setError( e.what(), "std::runtime_error" );
+  }
+
+#define NCGB_CATCH catch ( std::exception& e ) { handleError( e ); }
+
+  void checkCuda( cudaError_t err, const char* what )
+  {
+    if ( err != cudaSuccess )
+      throw TypedError( "CalcError", std::string("CUDA error in ") + what + ": " + cudaGetErrorString(err) );
+  }
+
+  // ---- device-resident materials ---------------------------------------------
+  struct DeviceMaterial {
+    std::shared_ptr<ncgb::MaterialTables> tables;
+    int device = -1;
+    void* d_arena = nullptr;
+    ncgb_material_view view;
+    ~DeviceMaterial()
+    {
+      if ( d_arena ) {
+        int cur = -1;
+        cudaGetDevice( &cur );
+        cudaSetDevice( device );
+        cudaFree( d_arena );
+        cudaSetDevice( cur );
+      }
+    }
+  };
+
+  std::mutex g_matmtx;
+  std::map<std::pair<std::string,int>, std::weak_ptr<DeviceMaterial>> g_matcache;
+
+  // cfg-string canonical form: whitespace removed, parameters after the file
+  // name sorted.  Bundles are looked up by this form.
+  std::string canonicalCfg( const std::string& cfg )
+  {
+    std::string s;
+    for ( char c : cfg )
+      if ( !std::isspace( static_cast<unsigned char>(c) ) )
+        s.push_back( c );
+    std::vector<std::string> parts;
+    std::string cur;
+    for ( char c : s ) {
+      if ( c == ';' ) { parts.push_back( cur ); cur.clear(); }
+      else cur.push_back( c );
+    }
+    parts.push_back( cur );
+    std::vector<std::string> params;
+    for ( std::size_t i = 1; i < parts.size(); ++i )
+      if ( !parts[i].empty() )
+        params.push_back( parts[i] );
+    std::sort( params.begin(), params.end() );
+    std::string out = parts.front();
+    for ( auto& p : params )
+      out += ";" + p;
+    return out;
+  }
+
+  std::string bundleFileName( const std::string& canon )
+  {
+    std::string f;
+    for ( char c : canon )
+      f.push_back( ( std::isalnum( static_cast<unsigned char>(c) ) || c == '.' || c == '=' || c == '-' || c == '_' ) ? c : '_' );
+    return f + ".ncgb";
+  }
+
+  std::vector<std::string> bundleDirs()
+  {
+    std::vector<std::string> dirs;
+    if ( const char* env = std::getenv( "NCGB_BUNDLE_PATH" ) ) {
+      std::string s( env ), cur;
+      for ( char c : s ) {
+        if ( c == ':' ) { if ( !cur.empty() ) dirs.push_back( cur ); cur.clear(); }
+        else cur.push_back( c );
+      }
+      if ( !cur.empty() ) dirs.push_back( cur );
+    }
+    Dl_info info;
+    if ( dladdr( reinterpret_cast<void*>( &bundleDirs ), &info ) && info.dli_fname ) {
+      std::string lib( info.dli_fname );
+      auto pos = lib.rfind( '/' );
+      std::string libdir = pos == std::string::npos ? "." : lib.substr( 0, pos );
+      dirs.push_back( libdir + "/../bundles" );
+      dirs.push_back( libdir + "/bundles" );
+    }
+    return dirs;
+  }
+
+  std::string findBundle( const std::string& cfg )
+  {
+    const std::string canon = canonicalCfg( cfg );
+    const std::string fn = bundleFileName( canon );
+    struct stat st;
+    for ( auto& d : bundleDirs() ) {
+      std::string p = d + "/" + fn;
+      if ( ::stat( p.c_str(), &st ) == 0 )
+        return p;
+    }
+    throw TypedError( "FileNotFound", "No material bundle for cfg \"" + cfg + "\" (looked for " + fn
+                      + " in NCGB_BUNDLE_PATH and the package bundles/ directory). Material bundles are"
+                      " written by ncgb_export, which runs NCrystal's host-side material loading." );
+  }
+
+  std::shared_ptr<DeviceMaterial> getMaterial( const std::string& cfg )
+  {
+    const std::string canon = canonicalCfg( cfg );
+    const std::string path = findBundle( cfg );
+    int dev = 0;
+    checkCuda( cudaGetDevice( &dev ), "cudaGetDevice" );
+    std::lock_guard<std::mutex> lock( g_matmtx );
+    auto key = std::make_pair( canon, dev );
+    auto it = g_matcache.find( key );
+    if ( it != g_matcache.end() )
+      if ( auto sp = it->second.lock() )
+        return sp;
+    auto bundle = ncgb::Bundle::load( path );
+    if ( canonicalCfg( bundle.str("cfg") ) != canon )
+      throw TypedError( "BadInput", "material bundle " + bundle.path() + " holds cfg \"" + bundle.str("cfg")
+                        + "\", not \"" + cfg + "\"" );
+    auto dm = std::make_shared<DeviceMaterial>();
+    dm->tables = ncgb::MaterialTables::build( bundle );
+    dm->device = dev;
+    const std::size_t bytes = dm->tables->arenaBytes();
+    checkCuda( cudaMalloc( &dm->d_arena, std::max<std::size_t>( bytes, 256 ) ), "cudaMalloc (material tables)" );
+    checkCuda( cudaMemcpy( dm->d_arena, dm->tables->arena().data(), bytes, cudaMemcpyHostToDevice ),
+               "cudaMemcpy (material tables)" );
+    dm->view = dm->tables->relocate( dm->d_arena );
+    g_matcache[key] = dm;
+    return dm;
+  }
+
+  // ---- handles (ncrystal.cc:104-200) ------------------------------------------
+  constexpr uint32_t kScatterTypeID = 0x7d6b0637; // same tag value as NCrystal's Scatter
+  constexpr uint64_t kDefaultSeed = 0x4e43727973746c21ull;
+
+  struct ScatterObj;
+  struct FingerPrint {
+    uint32_t typeid_;
+    ScatterObj* obj;
+  };
+
+  struct ScatterObj {
+    FingerPrint fp;
+    std::atomic<int> refcount{1};
+    std::shared_ptr<DeviceMaterial> mat;
+    std::string cfg;
+    uint64_t seed = kDefaultSeed;
+    uint32_t streamidx = 0;
+    std::atomic<uint32_t> callseq{0};
+    ScatterObj() { fp.typeid_ = kScatterTypeID; fp.obj = this; }
+  };
+
+  std::atomic<uint32_t> g_nextStream{1};
+
+  ScatterObj& extract( void* internal, const char* fct )
+  {
+    if ( !internal )
+      throw TypedError( "LogicError", std::string("Invalid (null) object handle passed to ") + fct );
+    auto fp = static_cast<FingerPrint*>( internal );
+    if ( fp->typeid_ != kScatterTypeID )
+      throw TypedError( "LogicError", std::string("Invalid object handle type passed to ") + fct );
+    return *fp->obj;
+  }
+
+  ncrystal_scatter_t makeHandle( ScatterObj* o ) { return ncrystal_scatter_t{ &o->fp }; }
+
+  // ---- per-thread scratch ----------------------------------------------------
+  struct Scratch {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    void* d_in = nullptr; std::size_t cap_in = 0;
+    void* d_a = nullptr; std::size_t cap_a = 0;
+    void* d_b = nullptr; std::size_t cap_b = 0;
+    void* d_c = nullptr; std::size_t cap_c = 0;
+    unsigned long long* d_nfail = nullptr;
+    unsigned long last_nfailed = 0;
+  };
+  thread_local Scratch t_scratch;
+
+  void ensure( void*& p, std::size_t& cap, std::size_t bytes )
+  {
+    if ( bytes <= cap )
+      return;
+    if ( p ) cudaFree( p );
+    p = nullptr;
+    cap = 0;
+    std::size_t want = std::max<std::size_t>( bytes, 1 << 20 );
+    checkCuda( cudaMalloc( &p, want ), "cudaMalloc (batch buffers)" );
+    cap = want;
+  }
+
+  Scratch& scratchFor( const DeviceMaterial& dm )
+  {
+    Scratch& s = t_scratch;
+    int cur = -1;
+    checkCuda( cudaGetDevice( &cur ), "cudaGetDevice" );
+    if ( cur != dm.device )
+      checkCuda( cudaSetDevice( dm.device ), "cudaSetDevice" );
+    if ( s.device != dm.device ) {
+      // Buffers of another device are abandoned (not freed: that device may be
+      // gone); a thread normally stays on one device.
+      s = Scratch();
+      s.device = dm.device;
+      checkCuda( cudaStreamCreateWithFlags( &s.stream, cudaStreamNonBlocking ), "cudaStreamCreate" );
+      checkCuda( cudaMalloc( &s.d_nfail, sizeof(unsigned long long) ), "cudaMalloc" );
+    }
+    return s;
+  }
+
+  uint32_t nextCall( ScatterObj& o ) { return o.callseq.fetch_add( 1, std::memory_order_relaxed ); }
+
+  void checkSize( unsigned long n_ekin, unsigned long repeat )
+  {
+    const unsigned long long tot = (unsigned long long)n_ekin * (unsigned long long)repeat;
+    if ( repeat && tot / repeat != n_ekin )
+      throw TypedError( "BadInput", "n_ekin*repeat overflows" );
+    if ( tot > 0xffffffffull )
+      throw TypedError( "BadInput", "n_ekin*repeat above 2^32 per call is not supported (neutron index of the random streams is 32 bits)" );
+  }
+
+  // H2D of inputs, kernel, D2H of outputs on the thread's stream.  Returns the
+  // number of neutrons with a non-OK status.
+  unsigned long runScatterMany( ScatterObj& o, const double* ekin, unsigned long n_ekin, unsigned long repeat,
+                                int mode, double* out_a, double* out_b, bool copyBackPartial )
+  {
+    checkSize( n_ekin, repeat );
+    const uint64_t n_out = (uint64_t)n_ekin * repeat;
+    if ( n_out == 0 )
+      return 0;
+    DeviceMaterial& dm = *o.mat;
+    Scratch& s = scratchFor( dm );
+    ensure( s.d_in, s.cap_in, n_ekin * sizeof(double) );
+    ensure( s.d_a, s.cap_a, n_out * sizeof(double) );
+    ensure( s.d_b, s.cap_b, n_out * sizeof(double) );
+    const uint32_t call = nextCall( o );
+    checkCuda( cudaMemcpyAsync( s.d_in, ekin, n_ekin * sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
+    checkCuda( cudaMemsetAsync( s.d_nfail, 0, sizeof(unsigned long long), s.stream ), "memset" );
+    if ( mode == 1 ) {
+      // genscatter leaves the outputs of failed neutrons untouched: start from
+      // the caller's arrays.
+      checkCuda( cudaMemcpyAsync( s.d_a, out_a, n_out * sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
+      checkCuda( cudaMemcpyAsync( s.d_b, out_b, n_out * sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
+    }
+    checkCuda( ncgb::launchScatterMany( dm.view, static_cast<const double*>( s.d_in ), n_ekin, n_out,
+                                        o.seed, call, o.streamidx, mode,
+                                        static_cast<double*>( s.d_a ), static_cast<double*>( s.d_b ),
+                                        s.d_nfail, s.stream ), "scatter kernel launch" );
+    unsigned long long nfail = 0;
+    checkCuda( cudaMemcpyAsync( &nfail, s.d_nfail, sizeof(nfail), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    checkCuda( cudaStreamSynchronize( s.stream ), "scatter kernel" );
+    if ( nfail == 0 || copyBackPartial ) {
+      checkCuda( cudaMemcpyAsync( out_a, s.d_a, n_out * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+      checkCuda( cudaMemcpyAsync( out_b, s.d_b, n_out * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+      checkCuda( cudaStreamSynchronize( s.stream ), "D2H" );
+    }
+    s.last_nfailed = static_cast<unsigned long>( nfail );
+    return static_cast<unsigned long>( nfail );
+  }
+
+  [[noreturn]] void throwSamplingFailure( unsigned long nfail )
+  {
+    std::ostringstream ss;
+    ss << "Sampling failed for " << nfail << " neutron(s): a rejection loop reached its limit of attempts"
+       << " (NCrystal: \"Rejection method failed to sample kinematically valid (alpha,beta) point\"), or a"
+       << " free-gas sampling (E >= Emax of a scattering kernel, or a FreeGas component) was requested,"
+       << " which this GPU path does not provide yet.";
+    throw TypedError( "CalcError", ss.str() );
+  }
+
+  void warnOnce( std::atomic<bool>& flag, const char* msg )
+  {
+    bool expected = true;
+    if ( flag.compare_exchange_strong( expected, false ) ) {
+      std::printf( "NCrystal WARNING: %s\n", msg );
+      std::fflush( stdout );
+    }
+  }
+  std::atomic<bool> g_warn_genscatter_many{true};
+  std::atomic<bool> g_warn_genscatter{true};
+}
+
+extern "C" {
+
+int ncrystal_sethaltonerror( int h ) { int old = g_halt; g_halt = h; return old; }
+int ncrystal_setquietonerror( int q ) { int old = g_quiet; g_quiet = q; return old; }
+int ncrystal_error( void ) { return g_waserror; }
+const char* ncrystal_lasterror( void ) { return g_waserror ? g_errmsg : nullptr; }
+const char* ncrystal_lasterrortype( void ) { return g_waserror ? g_errtype : nullptr; }
+void ncrystal_clearerror( void ) { g_waserror = 0; g_errmsg[0] = '\0'; g_errtype[0] = '\0'; }
+void ncrystal_seterrhandler( void (*handler)(char*,char*) ) { g_handler = handler; }
+
+int ncrystal_version( void ) { return 4004002; }
+const char* ncrystal_version_str( void ) { return "4.4.2"; }
+
+// ---- reference counting ----------------------------------------------------
+static void*& internalOf( void* addrhandle ) { return *reinterpret_cast<void**>( addrhandle ); }
+
+int ncrystal_valid( void* object )
+{
+  if ( !object )
+    return 0;
+  return internalOf( object ) ? 1 : 0;
+}
+
+void ncrystal_invalidate( void* object )
+{
+  if ( ncrystal_valid( object ) )
+    internalOf( object ) = nullptr;
+}
+
+int ncrystal_refcount( void* object )
+{
+  try {
+    return extract( internalOf( object ), "ncrystal_refcount" ).refcount.load();
+  } NCGB_CATCH;
+  return -999;
+}
+
+void ncrystal_ref( void* object )
+{
+  try {
+    extract( internalOf( object ), "ncrystal_ref" ).refcount.fetch_add( 1 );
+  } NCGB_CATCH;
+}
+
+void ncrystal_unref( void* object )
+{
+  try {
+    ScatterObj& o = extract( internalOf( object ), "ncrystal_unref" );
+    if ( o.refcount.fetch_sub( 1 ) == 1 ) {
+      delete &o;
+      internalOf( object ) = nullptr;
+    }
+  } NCGB_CATCH;
+}
+
+// ---- factories -----------------------------------------------------------------
+static ncrystal_scatter_t createScatter( const char* cfgstr, uint64_t seed )
+{
+  if ( !cfgstr )
+    throw TypedError( "BadInput", "null cfg-string" );
+  std::unique_ptr<ScatterObj> o( new ScatterObj );
+  o->mat = getMaterial( cfgstr );
+  o->cfg = cfgstr;
+  o->seed = seed;
+  return makeHandle( o.release() );
+}
+
+ncrystal_scatter_t ncrystal_create_scatter( const char* cfgstr )
+{
+  try {
+    return createScatter( cfgstr, kDefaultSeed );
+  } NCGB_CATCH;
+  return ncrystal_scatter_t{ nullptr };
+}
+
+ncrystal_scatter_t ncrystal_create_scatter_builtinrng( const char* cfgstr, unsigned long seed )
+{
+  try {
+    return createScatter( cfgstr, static_cast<uint64_t>( seed ) );
+  } NCGB_CATCH;
+  return ncrystal_scatter_t{ nullptr };
+}
+
+static ncrystal_scatter_t cloneWithStream( ncrystal_scatter_t sc, uint32_t streamidx, const char* fct )
+{
+  ScatterObj& src = extract( sc.internal, fct );
+  std::unique_ptr<ScatterObj> o( new ScatterObj );
+  o->mat = src.mat;
+  o->cfg = src.cfg;
+  o->seed = src.seed;
+  o->streamidx = streamidx;
+  return makeHandle( o.release() );
+}
+
+ncrystal_scatter_t ncrystal_clone_scatter( ncrystal_scatter_t sc )
+{
+  try {
+    return cloneWithStream( sc, g_nextStream.fetch_add( 1 ), "ncrystal_clone_scatter" );
+  } NCGB_CATCH;
+  return ncrystal_scatter_t{ nullptr };
+}
+
+ncrystal_scatter_t ncrystal_clone_scatter_rngbyidx( ncrystal_scatter_t sc, unsigned long idx )
+{
+  try {
+    // Stream 0 is the original handle's; clone index i uses stream i+1 of a
+    // separate range so that it never coincides with automatic clones.
+    return cloneWithStream( sc, 0x80000000u + static_cast<uint32_t>( idx & 0x7fffffffu ),
+                            "ncrystal_clone_scatter_rngbyidx" );
+  } NCGB_CATCH;
+  return ncrystal_scatter_t{ nullptr };
+}
+
+ncrystal_scatter_t ncrystal_clone_scatter_rngforcurrentthread( ncrystal_scatter_t sc )
+{
+  try {
+    static std::atomic<uint32_t> s_thread_stream{0x40000000u};
+    thread_local uint32_t t_stream = s_thread_stream.fetch_add( 1 );
+    return cloneWithStream( sc, t_stream, "ncrystal_clone_scatter_rngforcurrentthread" );
+  } NCGB_CATCH;
+  return ncrystal_scatter_t{ nullptr };
+}
+
+ncrystal_process_t ncrystal_cast_scat2proc( ncrystal_scatter_t s )
+{
+  try {
+    extract( s.internal, "ncrystal_cast_scat2proc" );
+    return ncrystal_process_t{ s.internal };
+  } NCGB_CATCH;
+  return ncrystal_process_t{ nullptr };
+}
+
+ncrystal_scatter_t ncrystal_cast_proc2scat( ncrystal_process_t p )
+{
+  try {
+    extract( p.internal, "ncrystal_cast_proc2scat" );
+    return ncrystal_scatter_t{ p.internal };
+  } NCGB_CATCH;
+  return ncrystal_scatter_t{ nullptr };
+}
+
+const char* ncrystal_name( ncrystal_process_t p )
+{
+  try {
+    ScatterObj& o = extract( p.internal, "ncrystal_name" );
+    return o.mat->view.ncomp > 1 ? "ProcComposition"
+      : ( o.mat->view.ncomp == 0 ? "NullProcess"
+          : ( o.mat->view.comp[0].type == NCGB_COMP_BRAGG ? "PowderBragg"
+              : o.mat->view.comp[0].type == NCGB_COMP_ELINC ? "ElIncScatter"
+              : o.mat->view.comp[0].type == NCGB_COMP_SAB ? "SABScatter" : "FreeGas" ) );
+  } NCGB_CATCH;
+  return nullptr;
+}
+
+int ncrystal_isnonoriented( ncrystal_process_t p )
+{
+  try {
+    extract( p.internal, "ncrystal_isnonoriented" );
+    return 1;
+  } NCGB_CATCH;
+  return 0;
+}
+
+void ncrystal_domain( ncrystal_process_t p, double* elow, double* ehigh )
+{
+  try {
+    ScatterObj& o = extract( p.internal, "ncrystal_domain" );
+    *elow = o.mat->view.dom_elow;
+    *ehigh = o.mat->view.dom_ehigh;
+    return;
+  } NCGB_CATCH;
+  *elow = *ehigh = -1.0;
+}
+
+// ---- batched evaluation ------------------------------------------------------------
+
+void ncrystal_crosssection_nonoriented_many( ncrystal_process_t p, const double* ekin,
+                                             unsigned long n_ekin, unsigned long repeat, double* results )
+{
+  try {
+    ScatterObj& o = extract( p.internal, "ncrystal_crosssection_nonoriented_many" );
+    checkSize( n_ekin, repeat );
+    const uint64_t n_out = (uint64_t)n_ekin * repeat;
+    if ( n_out == 0 )
+      return;
+    DeviceMaterial& dm = *o.mat;
+    Scratch& s = scratchFor( dm );
+    ensure( s.d_in, s.cap_in, n_ekin * sizeof(double) );
+    ensure( s.d_a, s.cap_a, n_out * sizeof(double) );
+    checkCuda( cudaMemcpyAsync( s.d_in, ekin, n_ekin * sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
+    checkCuda( ncgb::launchXS( dm.view, static_cast<const double*>( s.d_in ), n_ekin, repeat,
+                               static_cast<double*>( s.d_a ), s.stream ), "xs kernel launch" );
+    checkCuda( cudaMemcpyAsync( results, s.d_a, n_out * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    checkCuda( cudaStreamSynchronize( s.stream ), "xs kernel" );
+    return;
+  } NCGB_CATCH;
+  for ( unsigned long k = 0; k < n_ekin * repeat; ++k )
+    results[k] = -1.0;
+}
+
+void ncrystal_samplescatterisotropic_many( ncrystal_scatter_t sc, const double* ekin,
+                                           unsigned long n_ekin, unsigned long repeat,
+                                           double* results_ekin, double* results_mu )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncrystal_samplescatterisotropic_many" );
+    unsigned long nfail = runScatterMany( o, ekin, n_ekin, repeat, 0, results_ekin, results_mu, false );
+    if ( nfail )
+      throwSamplingFailure( nfail );
+    return;
+  } NCGB_CATCH;
+  for ( unsigned long k = 0; k < n_ekin * repeat; ++k ) {
+    results_ekin[k] = -1.0;
+    results_mu[k] = -999.0;
+  }
+}
+
+void ncrystal_genscatter_nonoriented_many( ncrystal_scatter_t sc, const double* ekin,
+                                           unsigned long n_ekin, unsigned long repeat,
+                                           double* results_angle, double* results_dekin )
+{
+  try {
+    warnOnce( g_warn_genscatter_many, "The ncrystal_genscatter_nonoriented_many function is obsolete."
+              " Please use the ncrystal_samplescatterisotropic_many function instead." );
+    ScatterObj& o = extract( sc.internal, "ncrystal_genscatter_nonoriented_many" );
+    unsigned long nfail = runScatterMany( o, ekin, n_ekin, repeat, 1, results_angle, results_dekin, true );
+    if ( nfail )
+      throwSamplingFailure( nfail );
+    return;
+  } NCGB_CATCH;
+}
+
+// ---- scalar evaluation (a batch of one) -----------------------------------------------
+
+void ncrystal_crosssection_nonoriented( ncrystal_process_t p, double ekin, double* result )
+{
+  ncrystal_crosssection_nonoriented_many( p, &ekin, 1, 1, result );
+}
+
+void ncrystal_samplescatterisotropic( ncrystal_scatter_t sc, double ekin, double* ef, double* mu )
+{
+  ncrystal_samplescatterisotropic_many( sc, &ekin, 1, 1, ef, mu );
+}
+
+void ncrystal_genscatter_nonoriented( ncrystal_scatter_t sc, double ekin, double* angle, double* dekin )
+{
+  *angle = -999.0;
+  *dekin = -999.0;
+  try {
+    warnOnce( g_warn_genscatter, "The ncrystal_genscatter_nonoriented function is obsolete. Please use"
+              " the ncrystal_samplescatterisotropic function instead." );
+    ScatterObj& o = extract( sc.internal, "ncrystal_genscatter_nonoriented" );
+    unsigned long nfail = runScatterMany( o, &ekin, 1, 1, 1, angle, dekin, true );
+    if ( nfail )
+      throwSamplingFailure( nfail );
+  } NCGB_CATCH;
+}
+
+// ---- additions ----------------------------------------------------------------------
+
+int ncgb_scatter_device( ncrystal_scatter_t sc, const double* d_ekin, unsigned long n,
+                         double* d_xs, double* d_ef, double* d_mu, int32_t* d_status, void* stream )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_scatter_device" );
+    checkSize( n, 1 );
+    Scratch& s = scratchFor( *o.mat );
+    checkCuda( ncgb::launchXSScatter( o.mat->view, d_ekin, n, o.seed, nextCall( o ), o.streamidx, 0,
+                                      d_xs, d_ef, d_mu, d_status, s.d_nfail,
+                                      static_cast<cudaStream_t>( stream ) ), "fused kernel launch" );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_scatter_device_f32( ncrystal_scatter_t sc, const float* d_ekin, unsigned long n,
+                             float* d_xs, float* d_ef, float* d_mu, int32_t* d_status, void* stream )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_scatter_device_f32" );
+    checkSize( n, 1 );
+    Scratch& s = scratchFor( *o.mat );
+    checkCuda( ncgb::launchXSScatterF32( o.mat->view, d_ekin, n, o.seed, nextCall( o ), o.streamidx, 0,
+                                         d_xs, d_ef, d_mu, d_status, s.d_nfail,
+                                         static_cast<cudaStream_t>( stream ) ), "fused kernel launch" );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+void ncgb_crosssection_nonoriented_many_f32( ncrystal_process_t p, const float* ekin,
+                                             unsigned long n, float* results )
+{
+  try {
+    ScatterObj& o = extract( p.internal, "ncgb_crosssection_nonoriented_many_f32" );
+    checkSize( n, 1 );
+    if ( n == 0 )
+      return;
+    Scratch& s = scratchFor( *o.mat );
+    ensure( s.d_in, s.cap_in, n * sizeof(float) );
+    ensure( s.d_a, s.cap_a, n * sizeof(float) );
+    checkCuda( cudaMemcpyAsync( s.d_in, ekin, n * sizeof(float), cudaMemcpyHostToDevice, s.stream ), "H2D" );
+    checkCuda( ncgb::launchXSF32( o.mat->view, static_cast<const float*>( s.d_in ), n,
+                                  static_cast<float*>( s.d_a ), s.stream ), "xs kernel launch" );
+    checkCuda( cudaMemcpyAsync( results, s.d_a, n * sizeof(float), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    checkCuda( cudaStreamSynchronize( s.stream ), "xs kernel" );
+    return;
+  } NCGB_CATCH;
+  for ( unsigned long k = 0; k < n; ++k )
+    results[k] = -1.0f;
+}
+
+void ncgb_samplescatterisotropic_many_f32( ncrystal_scatter_t sc, const float* ekin, unsigned long n,
+                                           float* results_ekin, float* results_mu )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_samplescatterisotropic_many_f32" );
+    checkSize( n, 1 );
+    if ( n == 0 )
+      return;
+    Scratch& s = scratchFor( *o.mat );
+    ensure( s.d_in, s.cap_in, n * sizeof(float) );
+    ensure( s.d_a, s.cap_a, n * sizeof(float) );
+    ensure( s.d_b, s.cap_b, n * sizeof(float) );
+    checkCuda( cudaMemcpyAsync( s.d_in, ekin, n * sizeof(float), cudaMemcpyHostToDevice, s.stream ), "H2D" );
+    checkCuda( cudaMemsetAsync( s.d_nfail, 0, sizeof(unsigned long long), s.stream ), "memset" );
+    checkCuda( ncgb::launchXSScatterF32( o.mat->view, static_cast<const float*>( s.d_in ), n, o.seed,
+                                         nextCall( o ), o.streamidx, 0, nullptr,
+                                         static_cast<float*>( s.d_a ), static_cast<float*>( s.d_b ),
+                                         nullptr, s.d_nfail, s.stream ), "scatter kernel launch" );
+    unsigned long long nfail = 0;
+    checkCuda( cudaMemcpyAsync( &nfail, s.d_nfail, sizeof(nfail), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    checkCuda( cudaMemcpyAsync( results_ekin, s.d_a, n * sizeof(float), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    checkCuda( cudaMemcpyAsync( results_mu, s.d_b, n * sizeof(float), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    checkCuda( cudaStreamSynchronize( s.stream ), "scatter kernel" );
+    s.last_nfailed = static_cast<unsigned long>( nfail );
+    if ( nfail )
+      throwSamplingFailure( static_cast<unsigned long>( nfail ) );
+    return;
+  } NCGB_CATCH;
+  for ( unsigned long k = 0; k < n; ++k ) {
+    results_ekin[k] = -1.0f;
+    results_mu[k] = -999.0f;
+  }
+}
+
+}
+
+namespace {
+  // Chunked H2D / kernel / D2H pipeline over two streams for the host-array
+  // fused entry points.  Chunk k runs on stream k%2; its buffers are the k%2
+  // half of the scratch, so chunk k+2 waits (stream order) for chunk k.
+  template<class T>
+  void xsScatterHost( ScatterObj& o, const T* ekin, unsigned long n, T* xs, T* ef, T* mu )
+  {
+    checkSize( n, 1 );
+    if ( n == 0 )
+      return;
+    DeviceMaterial& dm = *o.mat;
+    Scratch& s = scratchFor( dm );
+    static thread_local cudaStream_t s2 = nullptr;
+    static thread_local int s2dev = -1;
+    if ( s2dev != dm.device ) {
+      checkCuda( cudaStreamCreateWithFlags( &s2, cudaStreamNonBlocking ), "cudaStreamCreate" );
+      s2dev = dm.device;
+    }
+    const uint64_t chunk = std::min<uint64_t>( n, uint64_t(1) << 22 );
+    ensure( s.d_in, s.cap_in, 2 * chunk * sizeof(T) );
+    ensure( s.d_a, s.cap_a, 2 * chunk * sizeof(T) );
+    ensure( s.d_b, s.cap_b, 2 * chunk * sizeof(T) );
+    ensure( s.d_c, s.cap_c, 2 * chunk * sizeof(T) );
+    const uint32_t call = nextCall( o );
+    cudaStream_t st[2] = { s.stream, s2 };
+    checkCuda( cudaMemsetAsync( s.d_nfail, 0, sizeof(unsigned long long), s.stream ), "memset" );
+    cudaEvent_t zeroed;
+    checkCuda( cudaEventCreateWithFlags( &zeroed, cudaEventDisableTiming ), "event" );
+    checkCuda( cudaEventRecord( zeroed, s.stream ), "event" );
+    checkCuda( cudaStreamWaitEvent( s2, zeroed, 0 ), "event" );
+    uint64_t k = 0;
+    for ( uint64_t off = 0; off < n; off += chunk, ++k ) {
+      const uint64_t m = std::min<uint64_t>( chunk, n - off );
+      const int h = static_cast<int>( k & 1 );
+      cudaStream_t cs = st[h];
+      T* din = static_cast<T*>( s.d_in ) + h * chunk;
+      T* da = static_cast<T*>( s.d_a ) + h * chunk;
+      T* db = static_cast<T*>( s.d_b ) + h * chunk;
+      T* dc = static_cast<T*>( s.d_c ) + h * chunk;
+      checkCuda( cudaMemcpyAsync( din, ekin + off, m * sizeof(T), cudaMemcpyHostToDevice, cs ), "H2D" );
+      cudaError_t e;
+      if ( sizeof(T) == 8 )
+        e = ncgb::launchXSScatter( dm.view, reinterpret_cast<const double*>( din ), m, o.seed, call,
+                                   o.streamidx, static_cast<uint32_t>( off ),
+                                   xs ? reinterpret_cast<double*>( da ) : nullptr,
+                                   ef ? reinterpret_cast<double*>( db ) : nullptr,
+                                   mu ? reinterpret_cast<double*>( dc ) : nullptr,
+                                   nullptr, s.d_nfail, cs );
+      else
+        e = ncgb::launchXSScatterF32( dm.view, reinterpret_cast<const float*>( din ), m, o.seed, call,
+                                      o.streamidx, static_cast<uint32_t>( off ),
+                                      xs ? reinterpret_cast<float*>( da ) : nullptr,
+                                      ef ? reinterpret_cast<float*>( db ) : nullptr,
+                                      mu ? reinterpret_cast<float*>( dc ) : nullptr,
+                                      nullptr, s.d_nfail, cs );
+      checkCuda( e, "fused kernel launch" );
+      if ( xs ) checkCuda( cudaMemcpyAsync( xs + off, da, m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
+      if ( ef ) checkCuda( cudaMemcpyAsync( ef + off, db, m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
+      if ( mu ) checkCuda( cudaMemcpyAsync( mu + off, dc, m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
+    }
+    checkCuda( cudaStreamSynchronize( s2 ), "fused kernel" );
+    checkCuda( cudaStreamSynchronize( s.stream ), "fused kernel" );
+    cudaEventDestroy( zeroed );
+    unsigned long long nfail = 0;
+    checkCuda( cudaMemcpy( &nfail, s.d_nfail, sizeof(nfail), cudaMemcpyDeviceToHost ), "D2H" );
+    s.last_nfailed = static_cast<unsigned long>( nfail );
+    if ( nfail )
+      throwSamplingFailure( static_cast<unsigned long>( nfail ) );
+  }
+
+  template<class T>
+  void fillSentinels( unsigned long n, T* xs, T* ef, T* mu )
+  {
+    for ( unsigned long k = 0; k < n; ++k ) {
+      if ( xs ) xs[k] = T(-1);
+      if ( ef ) ef[k] = T(-1);
+      if ( mu ) mu[k] = T(-999);
+    }
+  }
+}
+
+extern "C" {
+
+void ncgb_xs_scatter_many( ncrystal_scatter_t sc, const double* ekin, unsigned long n,
+                           double* xs, double* ef, double* mu )
+{
+  try {
+    xsScatterHost<double>( extract( sc.internal, "ncgb_xs_scatter_many" ), ekin, n, xs, ef, mu );
+    return;
+  } NCGB_CATCH;
+  fillSentinels<double>( n, xs, ef, mu );
+}
+
+void ncgb_xs_scatter_many_f32( ncrystal_scatter_t sc, const float* ekin, unsigned long n,
+                               float* xs, float* ef, float* mu )
+{
+  try {
+    xsScatterHost<float>( extract( sc.internal, "ncgb_xs_scatter_many_f32" ), ekin, n, xs, ef, mu );
+    return;
+  } NCGB_CATCH;
+  fillSentinels<float>( n, xs, ef, mu );
+}
+
+unsigned long ncgb_last_nfailed( void ) { return t_scratch.last_nfailed; }
+
+unsigned long ncgb_device_bytes( ncrystal_scatter_t sc )
+{
+  try {
+    return extract( sc.internal, "ncgb_device_bytes" ).mat->tables->arenaBytes();
+  } NCGB_CATCH;
+  return 0;
+}
+
+}

@@ -17,7 +17,8 @@
  *
  * Status codes (per neutron): 0 ok; 1 a rejection loop hit its cap (the
  * reference throws CalcError, NCSABSampler.cc:226, NCSABSamplerModels.cc:150);
- * 2 free-gas sampling requested (not restated yet).
+ * 2 free-gas sampling requested (not restated yet); 3 the reference throws
+ * CalcError in convertAlphaBetaToDeltaEMu (E*E' == 0, NCKinUtils.cc:40-45).
  *
  * Built with -ffp-contract=off -O2 (no fast-math).
  */
@@ -33,6 +34,7 @@
 #define ORA_OK 0
 #define ORA_LOOPCAP 1
 #define ORA_UNSUPPORTED 2
+#define ORA_CALCERROR 3
 
 static const double ora_inf = INFINITY;
 
@@ -100,17 +102,20 @@ static int ora_mu_isotropic_at_beta( double beta, double ekin_div_kT )
 }
 
 /* Neumaier sum of three terms (NCMath.hh:526-536), then clamp. */
-static void ora_alphabeta_to_demu( double alpha, double beta, double ekin, double kT,
-                                   double* deltaE, double* mu )
+static int ora_alphabeta_to_demu( double alpha, double beta, double ekin, double kT,
+                                  double* deltaE, double* mu )
 {
   *deltaE = beta * kT;
   const double ekinfinal = ekin + *deltaE;
   const double denom = 2.0 * sqrt( ekin * ekinfinal );
+  if ( !denom )
+    return ORA_CALCERROR;
   double s = 0.0, c = 0.0, t, x;
   x = ekin;        t = s + x; c += ( fabs(s) >= fabs(x) ) ? (s-t)+x : (x-t)+s; s = t;
   x = ekinfinal;   t = s + x; c += ( fabs(s) >= fabs(x) ) ? (s-t)+x : (x-t)+s; s = t;
   x = -alpha * kT; t = s + x; c += ( fabs(s) >= fabs(x) ) ? (s-t)+x : (x-t)+s; s = t;
   *mu = ora_clamp( ( s + c ) / denom, -1.0, 1.0 );
+  return ORA_OK;
 }
 
 /* ---- cross-sections ------------------------------------------------------ */
@@ -482,7 +487,9 @@ static int ora_sab_scatter( const ncgb_sab_view* s, ncgb_rng* rng, double ekin, 
     deltaE = beta * s->kT;
     muv = ncgb_rng_generate( rng ) * 2.0 - 1.0;
   } else {
-    ora_alphabeta_to_demu( alpha, beta, ekin, s->kT, &deltaE, &muv );
+    int st = ora_alphabeta_to_demu( alpha, beta, ekin, s->kT, &deltaE, &muv );
+    if ( st != ORA_OK )
+      return st;
   }
   *ef = ora_max( 0.0, ekin + deltaE );
   *mu = muv;

@@ -1,0 +1,136 @@
+"""ctypes wrapper of the CPU oracle (oracle/ncgb_oracle.c) and of the
+reference-driving harness (oracle/refpin.c).  TEST INFRASTRUCTURE ONLY: used by
+tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg to check and
+time beside the GPU path; the library never imports it.
+
+The oracle reads the flat tables built by the library's host-only table
+loader (ncgb_tables_load), i.e. exactly the tables the kernels read.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+VIEW_BYTES = 1 << 16  # >= sizeof(ncgb_material_view)
+
+_ora = None
+_refpin = None
+
+
+def _P(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def oracle_lib():
+    global _ora
+    if _ora is None:
+        import ncrystal_gb300._build as B
+        path = B.oracle_path()
+        if not os.path.exists(path):
+            B.build_oracle()
+        L = C.CDLL(path)
+        L.ncgb_oracle_xs.restype = C.c_double
+        L.ncgb_oracle_xs.argtypes = [C.c_void_p, C.c_double]
+        L.ncgb_oracle_xs_many.restype = None
+        L.ncgb_oracle_xs_many.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+        L.ncgb_oracle_scatter_many.restype = C.c_int64
+        L.ncgb_oracle_scatter_many.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64, C.c_uint32,
+                                               C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_void_p]
+        _ora = L
+    return _ora
+
+
+class HostMaterial:
+    """A material's flat tables in host memory (built by the library's host
+    table loader from a bundle file)."""
+
+    def __init__(self, bundle_path):
+        from ncrystal_gb300.core import lib
+        L = lib()
+        self._L = L
+        h = L.ncgb_tables_load(bundle_path.encode())
+        if not h:
+            raise RuntimeError("could not load %s: %s" % (bundle_path, L.ncgb_tables_lasterror().decode()))
+        self._h = h
+        self.view = C.create_string_buffer(VIEW_BYTES)
+        L.ncgb_tables_view(C.c_void_p(h), self.view)
+
+    def __del__(self):
+        try:
+            self._L.ncgb_tables_free(C.c_void_p(self._h))
+        except Exception:
+            pass
+
+    def nbytes(self):
+        return self._L.ncgb_tables_bytes(C.c_void_p(self._h))
+
+    def array(self, comp, name, dtype):
+        p = C.c_void_p()
+        n = C.c_ulong()
+        if self._L.ncgb_tables_array(C.c_void_p(self._h), comp, name.encode(), C.byref(p), C.byref(n)):
+            raise KeyError(name)
+        dt = np.dtype(dtype)
+        if n.value == 0:
+            return np.zeros(0, dt)
+        raw = np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_char)), shape=(n.value * dt.itemsize,))
+        return raw.view(dt).copy()
+
+    def scalar(self, comp, name):
+        v = C.c_double()
+        if self._L.ncgb_tables_scalar(C.c_void_p(self._h), comp, name.encode(), C.byref(v)):
+            raise KeyError(name)
+        return v.value
+
+    # ---- oracle evaluation ----------------------------------------------------
+    def xs(self, ekin):
+        e = np.ascontiguousarray(ekin, dtype=np.float64)
+        out = np.empty(len(e))
+        oracle_lib().ncgb_oracle_xs_many(self.view, _P(e), len(e), _P(out))
+        return out
+
+    def scatter(self, ekin, seed, index_offset=0, callseq=0, stream=0):
+        """Per neutron i: stream (seed, i+index_offset, callseq, stream).
+        Returns (ekin_final, mu, status, ndraws)."""
+        e = np.ascontiguousarray(ekin, dtype=np.float64)
+        n = len(e)
+        ef = np.empty(n)
+        mu = np.empty(n)
+        st = np.empty(n, dtype=np.int32)
+        nd = np.empty(n, dtype=np.int32)
+        oracle_lib().ncgb_oracle_scatter_many(self.view, _P(e), n, seed, index_offset, callseq, stream,
+                                              _P(ef), _P(mu), _P(st), _P(nd))
+        return ef, mu, st, nd
+
+
+def refpin_lib():
+    """The harness around the reference library (only where it was built)."""
+    global _refpin
+    if _refpin is None:
+        path = os.path.join(HERE, "_ref", "librefpin.so")
+        if not os.path.exists(path):
+            return None
+        L = C.CDLL(path)
+        L.refpin_run.restype = C.c_int
+        L.refpin_run.argtypes = [C.c_char_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_int64,
+                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _refpin = L
+    return _refpin
+
+
+def reference_run(cfg, ekin, seed, callseq=0, stream=0):
+    """Run the reference library on the same per-neutron Philox streams.
+    Returns dict(xs, ekin_final, mu, ndraws, status)."""
+    L = refpin_lib()
+    if L is None:
+        raise RuntimeError("reference harness not built")
+    e = np.ascontiguousarray(ekin, dtype=np.float64)
+    n = len(e)
+    out = dict(xs=np.empty(n), ekin_final=np.empty(n), mu=np.empty(n),
+               ndraws=np.empty(n, dtype=np.int32), status=np.empty(n, dtype=np.int32))
+    rc = L.refpin_run(cfg.encode(), seed, callseq, stream, _P(e), n, _P(out["xs"]), _P(out["ekin_final"]),
+                      _P(out["mu"]), _P(out["ndraws"]), _P(out["status"]))
+    if rc:
+        raise RuntimeError("reference could not create %r" % cfg)
+    return out

@@ -47,6 +47,12 @@ int refpin_run( const char* cfg, uint64_t seed, uint32_t callseq, uint32_t strea
   }
   ncrystal_process_t pr = ncrystal_cast_scat2proc( sc );
   for ( int64_t i = 0; i < n; ++i ) {
+    /* The reference keeps the last energy's results per Scatter object and
+     * reuses them for an energy within 1e-15 relative of it
+     * (NCProcImpl.cc:172-183).  Evaluating a far-away energy first makes every
+     * neutron's evaluation fresh, as on the GPU, where neutrons share no state. */
+    double flush;
+    ncrystal_crosssection_nonoriented( pr, 12345.0, &flush );
     ncrystal_crosssection_nonoriented( pr, ekin[i], &out_xs[i] );
     ncgb_rng_init( &g_rng, seed, (uint32_t)i, callseq, stream );
     g_ndraws = 0;

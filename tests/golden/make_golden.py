@@ -1,0 +1,79 @@
+"""Generates the golden fixtures tests/golden/*.npz from the reference NCrystal
+library itself (oracle/_ref, built from the NCrystal sources by oracle/ref.mk).
+
+For each material, the reference's own ncrystal_crosssection_nonoriented and
+ncrystal_samplescatterisotropic are run on seeded energies, with the random
+source replaced by the per-neutron Philox streams of include/ncgb_philox.h
+(oracle/refpin.c).  The fixture holds, per neutron: E, the cross-section, E',
+mu, the number of random numbers the reference consumed and whether it raised
+an error.  Neutron i uses stream (SEED, i, 0, 0).
+
+Run from the repository root where the NCrystal sources exist:
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import ncrystal_gb300._build as B  # noqa: E402
+import ncrystal_gb300.workloads as W  # noqa: E402
+from oracle import pyoracle  # noqa: E402
+from ncrystal_gb300.bundle.reader import read_bundle  # noqa: E402
+
+SEED = 0x5EEDF00D
+N_RANDOM = 1500
+
+GOLDEN = {
+    "al": (W.AL, lambda n: W.al_wavelength_energies(n, 101)),
+    "al2o3": (W.AL2O3, lambda n: W.loguniform_energies(n, 1e-4, 1.0, 102)),
+    "pe293": (W.PE293, lambda n: W.loguniform_energies(n, 1e-4, 1.0, 103)),
+    "pe320": ("Polyethylene_CH2.ncmat;temp=320K", lambda n: W.loguniform_energies(n, 1e-5, 2.0, 104)),
+    "water": (W.WATER, lambda n: W.loguniform_energies(n, 1e-5, 2.0, 105)),
+    "cu77": ("Cu_sg225.ncmat;temp=77K", lambda n: W.loguniform_energies(n, 1e-4, 1.0, 106)),
+    "zno400": ("ZnO_sg186_ZincOxide.ncmat;temp=400K", lambda n: W.loguniform_energies(n, 1e-4, 1.0, 107)),
+    "kat_ni": ("Ni_sg225.ncmat;dcutoff=0.6;vdoslux=2", lambda n: W.loguniform_energies(n, 1e-4, 1.0, 108)),
+}
+
+
+def edge_energies(bundle):
+    """Energies on and next to table edges: Bragg thresholds and plane edges,
+    SAB energy-grid points, Emax, and a few extremes."""
+    e = [1e-12, 1e-9, 1e-7, 1e-6]
+    for ic in range(int(bundle["ncomp"][0])):
+        p = "c%d." % ic
+        t = bundle[p + "type"]
+        if t == "PowderBragg":
+            a = bundle[p + "two_dE"]
+            for x in list(a[:6]) + list(a[-3:]):
+                e += [x, np.nextafter(x, 0.0), np.nextafter(x, np.inf)]
+        elif t == "SABScatter":
+            g = bundle[p + "egrid"]
+            for x in list(g[:3]) + list(g[::37]) + list(g[-3:]):
+                e += [x, np.nextafter(x, 0.0), np.nextafter(x, np.inf), x * 1.05, x / 1.05]
+    return np.array([x for x in e if x > 0], dtype=np.float64)
+
+
+def main():
+    if not B.build_reference():
+        sys.exit("the NCrystal sources are needed to generate golden fixtures")
+    B.build_library()
+    cfgs = [c for c, _ in GOLDEN.values()]
+    paths = B.export_bundles(cfgs)
+    for key, (cfg, gen) in GOLDEN.items():
+        b = read_bundle(paths[cfg])
+        ekin = np.concatenate([gen(N_RANDOM), edge_energies(b)])
+        r = pyoracle.reference_run(cfg, ekin, SEED)
+        out = os.path.join(HERE, key + ".npz")
+        np.savez_compressed(out, cfg=np.array(cfg), seed=np.array(SEED, dtype=np.uint64), ekin=ekin,
+                            xs=r["xs"], ekin_final=r["ekin_final"], mu=r["mu"], ndraws=r["ndraws"],
+                            status=r["status"])
+        print("%-8s %-55s n=%d errors=%d -> %s" % (key, cfg, len(ekin), int(r["status"].sum()), out))
+
+
+if __name__ == "__main__":
+    main()
