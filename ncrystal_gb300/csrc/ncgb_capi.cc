@@ -241,14 +241,22 @@ namespace {
   ncrystal_scatter_t makeHandle( ScatterObj* o ) { return ncrystal_scatter_t{ &o->fp }; }
 
   // ---- per-thread scratch ----------------------------------------------------
+  // Device buffers of one host thread: staging for host-array calls, and the
+  // SAB queue + counters that every scatter batch uses.  Grow-only.  Batches
+  // from one thread are ordered through 'done' (an event recorded after each
+  // batch that the next batch's stream waits for), so the scratch is never
+  // shared by two batches in flight.
   struct Scratch {
     int device = -1;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t done = nullptr;
     void* d_in = nullptr; std::size_t cap_in = 0;
     void* d_a = nullptr; std::size_t cap_a = 0;
     void* d_b = nullptr; std::size_t cap_b = 0;
     void* d_c = nullptr; std::size_t cap_c = 0;
-    unsigned long long* d_nfail = nullptr;
+    void* d_queue = nullptr; std::size_t cap_queue = 0;
+    ncgb::Work* d_work = nullptr;
     unsigned long last_nfailed = 0;
   };
   thread_local Scratch t_scratch;
@@ -257,7 +265,10 @@ namespace {
   {
     if ( bytes <= cap )
       return;
-    if ( p ) cudaFree( p );
+    if ( p ) {
+      checkCuda( cudaDeviceSynchronize(), "synchronize before re-allocating scratch" );
+      cudaFree( p );
+    }
     p = nullptr;
     cap = 0;
     std::size_t want = std::max<std::size_t>( bytes, 1 << 20 );
@@ -278,7 +289,12 @@ namespace {
       s = Scratch();
       s.device = dm.device;
       checkCuda( cudaStreamCreateWithFlags( &s.stream, cudaStreamNonBlocking ), "cudaStreamCreate" );
-      checkCuda( cudaMalloc( &s.d_nfail, sizeof(unsigned long long) ), "cudaMalloc" );
+      checkCuda( cudaStreamCreateWithFlags( &s.stream2, cudaStreamNonBlocking ), "cudaStreamCreate" );
+      checkCuda( cudaEventCreateWithFlags( &s.done, cudaEventDisableTiming ), "cudaEventCreate" );
+      checkCuda( cudaEventRecord( s.done, s.stream ), "cudaEventRecord" );
+      void* w = nullptr;
+      checkCuda( cudaMalloc( &w, sizeof(ncgb::Work) ), "cudaMalloc" );
+      s.d_work = static_cast<ncgb::Work*>( w );
     }
     return s;
   }
@@ -294,7 +310,47 @@ namespace {
       throw TypedError( "BadInput", "n_ekin*repeat above 2^32 per call is not supported (neutron index of the random streams is 32 bits)" );
   }
 
-  // H2D of inputs, kernel, D2H of outputs on the thread's stream.  Returns the
+  ncgb::Batch makeBatch( ScatterObj& o, Scratch& s, uint32_t call )
+  {
+    ncgb::Batch b;
+    std::memset( &b, 0, sizeof(b) );
+    b.seed = o.seed;
+    b.callseq = call;
+    b.stream = o.streamidx;
+    b.work = s.d_work;
+    b.queue = static_cast<ncgb::QEntry*>( s.d_queue );
+    return b;
+  }
+
+  // Scatter batch on stream 'st', ordered after the thread's previous batch.
+  void runBatch( const DeviceMaterial& dm, Scratch& s, ncgb::Batch& b, cudaStream_t st )
+  {
+    ensure( s.d_queue, s.cap_queue, b.n_out * sizeof(ncgb::QEntry) );
+    b.queue = static_cast<ncgb::QEntry*>( s.d_queue );
+    checkCuda( cudaStreamWaitEvent( st, s.done, 0 ), "cudaStreamWaitEvent" );
+    checkCuda( ncgb::launchScatter( dm.view, b, st ), "scatter kernels" );
+    checkCuda( cudaEventRecord( s.done, st ), "cudaEventRecord" );
+  }
+
+  // The failure counter accumulates over the batches of one call; the
+  // per-batch queue counters are reset by launchScatter.
+  void resetNFail( Scratch& s, cudaStream_t st )
+  {
+    checkCuda( cudaStreamWaitEvent( st, s.done, 0 ), "cudaStreamWaitEvent" );
+    checkCuda( cudaMemsetAsync( &s.d_work->nfail, 0, sizeof(unsigned long long), st ), "memset" );
+    checkCuda( cudaEventRecord( s.done, st ), "cudaEventRecord" );
+  }
+
+  unsigned long readNFail( Scratch& s, cudaStream_t st )
+  {
+    unsigned long long nfail = 0;
+    checkCuda( cudaMemcpyAsync( &nfail, &s.d_work->nfail, sizeof(nfail), cudaMemcpyDeviceToHost, st ), "D2H" );
+    checkCuda( cudaStreamSynchronize( st ), "scatter kernels" );
+    s.last_nfailed = static_cast<unsigned long>( nfail );
+    return s.last_nfailed;
+  }
+
+  // Host arrays in; H2D, kernels, D2H on the thread's stream.  Returns the
   // number of neutrons with a non-OK status.
   unsigned long runScatterMany( ScatterObj& o, const double* ekin, unsigned long n_ekin, unsigned long repeat,
                                 int mode, double* out_a, double* out_b, bool copyBackPartial )
@@ -308,38 +364,38 @@ namespace {
     ensure( s.d_in, s.cap_in, n_ekin * sizeof(double) );
     ensure( s.d_a, s.cap_a, n_out * sizeof(double) );
     ensure( s.d_b, s.cap_b, n_out * sizeof(double) );
-    const uint32_t call = nextCall( o );
+    ncgb::Batch b = makeBatch( o, s, nextCall( o ) );
+    b.ekin = s.d_in;
+    b.n_ekin = n_ekin;
+    b.n_out = n_out;
+    b.mode = mode;
+    b.out_a = s.d_a;
+    b.out_b = s.d_b;
+    resetNFail( s, s.stream );
     checkCuda( cudaMemcpyAsync( s.d_in, ekin, n_ekin * sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
-    checkCuda( cudaMemsetAsync( s.d_nfail, 0, sizeof(unsigned long long), s.stream ), "memset" );
     if ( mode == 1 ) {
       // genscatter leaves the outputs of failed neutrons untouched: start from
       // the caller's arrays.
       checkCuda( cudaMemcpyAsync( s.d_a, out_a, n_out * sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
       checkCuda( cudaMemcpyAsync( s.d_b, out_b, n_out * sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
     }
-    checkCuda( ncgb::launchScatterMany( dm.view, static_cast<const double*>( s.d_in ), n_ekin, n_out,
-                                        o.seed, call, o.streamidx, mode,
-                                        static_cast<double*>( s.d_a ), static_cast<double*>( s.d_b ),
-                                        s.d_nfail, s.stream ), "scatter kernel launch" );
-    unsigned long long nfail = 0;
-    checkCuda( cudaMemcpyAsync( &nfail, s.d_nfail, sizeof(nfail), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
-    checkCuda( cudaStreamSynchronize( s.stream ), "scatter kernel" );
+    runBatch( dm, s, b, s.stream );
+    const unsigned long nfail = readNFail( s, s.stream );
     if ( nfail == 0 || copyBackPartial ) {
       checkCuda( cudaMemcpyAsync( out_a, s.d_a, n_out * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
       checkCuda( cudaMemcpyAsync( out_b, s.d_b, n_out * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
       checkCuda( cudaStreamSynchronize( s.stream ), "D2H" );
     }
-    s.last_nfailed = static_cast<unsigned long>( nfail );
-    return static_cast<unsigned long>( nfail );
+    return nfail;
   }
 
   [[noreturn]] void throwSamplingFailure( unsigned long nfail )
   {
     std::ostringstream ss;
     ss << "Sampling failed for " << nfail << " neutron(s): a rejection loop reached its limit of attempts"
-       << " (NCrystal: \"Rejection method failed to sample kinematically valid (alpha,beta) point\"), or a"
-       << " free-gas sampling (E >= Emax of a scattering kernel, or a FreeGas component) was requested,"
-       << " which this GPU path does not provide yet.";
+       << " (NCrystal: \"Rejection method failed to sample kinematically valid (alpha,beta) point\"), the"
+       << " (alpha,beta) -> mu conversion met E*E'=0, or a free-gas sampling (E >= Emax of a scattering"
+       << " kernel, or a FreeGas component) was requested, which this GPU path does not provide yet.";
     throw TypedError( "CalcError", ss.str() );
   }
 
@@ -353,6 +409,67 @@ namespace {
   }
   std::atomic<bool> g_warn_genscatter_many{true};
   std::atomic<bool> g_warn_genscatter{true};
+
+  // Chunked H2D / kernels / D2H pipeline over two streams for the host-array
+  // fused entry points.  Chunk k runs on stream k%2 with the k%2 half of the
+  // staging buffers; the SAB queue and counters are shared, so the kernels of
+  // consecutive chunks are ordered through the 'done' event while the copies
+  // of one chunk overlap the kernels of the other.
+  template<class T>
+  void xsScatterHost( ScatterObj& o, const T* ekin, unsigned long n, T* xs, T* ef, T* mu )
+  {
+    checkSize( n, 1 );
+    if ( n == 0 )
+      return;
+    DeviceMaterial& dm = *o.mat;
+    Scratch& s = scratchFor( dm );
+    const uint64_t chunk = std::min<uint64_t>( n, uint64_t(1) << 22 );
+    ensure( s.d_in, s.cap_in, 2 * chunk * sizeof(T) );
+    ensure( s.d_a, s.cap_a, 2 * chunk * sizeof(T) );
+    ensure( s.d_b, s.cap_b, 2 * chunk * sizeof(T) );
+    ensure( s.d_c, s.cap_c, 2 * chunk * sizeof(T) );
+    ensure( s.d_queue, s.cap_queue, chunk * sizeof(ncgb::QEntry) );
+    const uint32_t call = nextCall( o );
+    cudaStream_t st[2] = { s.stream, s.stream2 };
+    resetNFail( s, s.stream );
+    uint64_t k = 0;
+    for ( uint64_t off = 0; off < n; off += chunk, ++k ) {
+      const uint64_t m = std::min<uint64_t>( chunk, n - off );
+      const int h = static_cast<int>( k & 1 );
+      cudaStream_t cs = st[h];
+      T* din = static_cast<T*>( s.d_in ) + h * chunk;
+      T* da = static_cast<T*>( s.d_a ) + h * chunk;
+      T* db = static_cast<T*>( s.d_b ) + h * chunk;
+      T* dc = static_cast<T*>( s.d_c ) + h * chunk;
+      checkCuda( cudaMemcpyAsync( din, ekin + off, m * sizeof(T), cudaMemcpyHostToDevice, cs ), "H2D" );
+      ncgb::Batch b = makeBatch( o, s, call );
+      b.ekin = din;
+      b.in_f32 = b.out_f32 = ( sizeof(T) == 4 );
+      b.n_ekin = b.n_out = m;
+      b.index_offset = static_cast<uint32_t>( off );
+      b.out_xs = xs ? da : nullptr;
+      b.out_a = ef ? db : nullptr;
+      b.out_b = mu ? dc : nullptr;
+      runBatch( dm, s, b, cs );
+      if ( xs ) checkCuda( cudaMemcpyAsync( xs + off, da, m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
+      if ( ef ) checkCuda( cudaMemcpyAsync( ef + off, db, m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
+      if ( mu ) checkCuda( cudaMemcpyAsync( mu + off, dc, m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
+    }
+    checkCuda( cudaStreamSynchronize( s.stream2 ), "scatter kernels" );
+    const unsigned long bad = readNFail( s, s.stream );
+    if ( bad )
+      throwSamplingFailure( bad );
+  }
+
+  template<class T>
+  void fillSentinels( unsigned long n, T* xs, T* ef, T* mu )
+  {
+    for ( unsigned long k = 0; k < n; ++k ) {
+      if ( xs ) xs[k] = T(-1);
+      if ( ef ) ef[k] = T(-1);
+      if ( mu ) mu[k] = T(-999);
+    }
+  }
 }
 
 extern "C" {
@@ -544,10 +661,16 @@ void ncrystal_crosssection_nonoriented_many( ncrystal_process_t p, const double*
     Scratch& s = scratchFor( dm );
     ensure( s.d_in, s.cap_in, n_ekin * sizeof(double) );
     ensure( s.d_a, s.cap_a, n_out * sizeof(double) );
+    ncgb::Batch b = makeBatch( o, s, 0 );
+    b.ekin = s.d_in;
+    b.n_ekin = n_ekin;
+    b.n_out = n_out;
+    b.out_xs = s.d_a;
+    checkCuda( cudaStreamWaitEvent( s.stream, s.done, 0 ), "cudaStreamWaitEvent" );
     checkCuda( cudaMemcpyAsync( s.d_in, ekin, n_ekin * sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
-    checkCuda( ncgb::launchXS( dm.view, static_cast<const double*>( s.d_in ), n_ekin, repeat,
-                               static_cast<double*>( s.d_a ), s.stream ), "xs kernel launch" );
+    checkCuda( ncgb::launchXS( dm.view, b, repeat, s.stream ), "xs kernel" );
     checkCuda( cudaMemcpyAsync( results, s.d_a, n_out * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    checkCuda( cudaEventRecord( s.done, s.stream ), "cudaEventRecord" );
     checkCuda( cudaStreamSynchronize( s.stream ), "xs kernel" );
     return;
   } NCGB_CATCH;
@@ -615,34 +738,40 @@ void ncrystal_genscatter_nonoriented( ncrystal_scatter_t sc, double ekin, double
 
 // ---- additions ----------------------------------------------------------------------
 
-int ncgb_scatter_device( ncrystal_scatter_t sc, const double* d_ekin, unsigned long n,
-                         double* d_xs, double* d_ef, double* d_mu, int32_t* d_status, void* stream )
+static int scatterDevice( ncrystal_scatter_t sc, const void* d_ekin, unsigned long n, void* d_xs, void* d_ef,
+                          void* d_mu, int32_t* d_status, void* stream, bool f32, const char* fct )
 {
   try {
-    ScatterObj& o = extract( sc.internal, "ncgb_scatter_device" );
+    ScatterObj& o = extract( sc.internal, fct );
     checkSize( n, 1 );
-    Scratch& s = scratchFor( *o.mat );
-    checkCuda( ncgb::launchXSScatter( o.mat->view, d_ekin, n, o.seed, nextCall( o ), o.streamidx, 0,
-                                      d_xs, d_ef, d_mu, d_status, s.d_nfail,
-                                      static_cast<cudaStream_t>( stream ) ), "fused kernel launch" );
+    if ( n == 0 )
+      return 0;
+    DeviceMaterial& dm = *o.mat;
+    Scratch& s = scratchFor( dm );
+    ncgb::Batch b = makeBatch( o, s, nextCall( o ) );
+    b.ekin = d_ekin;
+    b.in_f32 = b.out_f32 = f32 ? 1 : 0;
+    b.n_ekin = b.n_out = n;
+    b.out_xs = d_xs;
+    b.out_a = d_ef;
+    b.out_b = d_mu;
+    b.status = d_status;
+    runBatch( dm, s, b, static_cast<cudaStream_t>( stream ) );
     return 0;
   } NCGB_CATCH;
   return 1;
 }
 
+int ncgb_scatter_device( ncrystal_scatter_t sc, const double* d_ekin, unsigned long n,
+                         double* d_xs, double* d_ef, double* d_mu, int32_t* d_status, void* stream )
+{
+  return scatterDevice( sc, d_ekin, n, d_xs, d_ef, d_mu, d_status, stream, false, "ncgb_scatter_device" );
+}
+
 int ncgb_scatter_device_f32( ncrystal_scatter_t sc, const float* d_ekin, unsigned long n,
                              float* d_xs, float* d_ef, float* d_mu, int32_t* d_status, void* stream )
 {
-  try {
-    ScatterObj& o = extract( sc.internal, "ncgb_scatter_device_f32" );
-    checkSize( n, 1 );
-    Scratch& s = scratchFor( *o.mat );
-    checkCuda( ncgb::launchXSScatterF32( o.mat->view, d_ekin, n, o.seed, nextCall( o ), o.streamidx, 0,
-                                         d_xs, d_ef, d_mu, d_status, s.d_nfail,
-                                         static_cast<cudaStream_t>( stream ) ), "fused kernel launch" );
-    return 0;
-  } NCGB_CATCH;
-  return 1;
+  return scatterDevice( sc, d_ekin, n, d_xs, d_ef, d_mu, d_status, stream, true, "ncgb_scatter_device_f32" );
 }
 
 void ncgb_crosssection_nonoriented_many_f32( ncrystal_process_t p, const float* ekin,
@@ -653,13 +782,20 @@ void ncgb_crosssection_nonoriented_many_f32( ncrystal_process_t p, const float* 
     checkSize( n, 1 );
     if ( n == 0 )
       return;
-    Scratch& s = scratchFor( *o.mat );
+    DeviceMaterial& dm = *o.mat;
+    Scratch& s = scratchFor( dm );
     ensure( s.d_in, s.cap_in, n * sizeof(float) );
     ensure( s.d_a, s.cap_a, n * sizeof(float) );
+    ncgb::Batch b = makeBatch( o, s, 0 );
+    b.ekin = s.d_in;
+    b.in_f32 = b.out_f32 = 1;
+    b.n_ekin = b.n_out = n;
+    b.out_xs = s.d_a;
+    checkCuda( cudaStreamWaitEvent( s.stream, s.done, 0 ), "cudaStreamWaitEvent" );
     checkCuda( cudaMemcpyAsync( s.d_in, ekin, n * sizeof(float), cudaMemcpyHostToDevice, s.stream ), "H2D" );
-    checkCuda( ncgb::launchXSF32( o.mat->view, static_cast<const float*>( s.d_in ), n,
-                                  static_cast<float*>( s.d_a ), s.stream ), "xs kernel launch" );
+    checkCuda( ncgb::launchXS( dm.view, b, 1, s.stream ), "xs kernel" );
     checkCuda( cudaMemcpyAsync( results, s.d_a, n * sizeof(float), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    checkCuda( cudaEventRecord( s.done, s.stream ), "cudaEventRecord" );
     checkCuda( cudaStreamSynchronize( s.stream ), "xs kernel" );
     return;
   } NCGB_CATCH;
@@ -671,120 +807,12 @@ void ncgb_samplescatterisotropic_many_f32( ncrystal_scatter_t sc, const float* e
                                            float* results_ekin, float* results_mu )
 {
   try {
-    ScatterObj& o = extract( sc.internal, "ncgb_samplescatterisotropic_many_f32" );
-    checkSize( n, 1 );
-    if ( n == 0 )
-      return;
-    Scratch& s = scratchFor( *o.mat );
-    ensure( s.d_in, s.cap_in, n * sizeof(float) );
-    ensure( s.d_a, s.cap_a, n * sizeof(float) );
-    ensure( s.d_b, s.cap_b, n * sizeof(float) );
-    checkCuda( cudaMemcpyAsync( s.d_in, ekin, n * sizeof(float), cudaMemcpyHostToDevice, s.stream ), "H2D" );
-    checkCuda( cudaMemsetAsync( s.d_nfail, 0, sizeof(unsigned long long), s.stream ), "memset" );
-    checkCuda( ncgb::launchXSScatterF32( o.mat->view, static_cast<const float*>( s.d_in ), n, o.seed,
-                                         nextCall( o ), o.streamidx, 0, nullptr,
-                                         static_cast<float*>( s.d_a ), static_cast<float*>( s.d_b ),
-                                         nullptr, s.d_nfail, s.stream ), "scatter kernel launch" );
-    unsigned long long nfail = 0;
-    checkCuda( cudaMemcpyAsync( &nfail, s.d_nfail, sizeof(nfail), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
-    checkCuda( cudaMemcpyAsync( results_ekin, s.d_a, n * sizeof(float), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
-    checkCuda( cudaMemcpyAsync( results_mu, s.d_b, n * sizeof(float), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
-    checkCuda( cudaStreamSynchronize( s.stream ), "scatter kernel" );
-    s.last_nfailed = static_cast<unsigned long>( nfail );
-    if ( nfail )
-      throwSamplingFailure( static_cast<unsigned long>( nfail ) );
+    xsScatterHost<float>( extract( sc.internal, "ncgb_samplescatterisotropic_many_f32" ), ekin, n,
+                          nullptr, results_ekin, results_mu );
     return;
   } NCGB_CATCH;
-  for ( unsigned long k = 0; k < n; ++k ) {
-    results_ekin[k] = -1.0f;
-    results_mu[k] = -999.0f;
-  }
+  fillSentinels<float>( n, nullptr, results_ekin, results_mu );
 }
-
-}
-
-namespace {
-  // Chunked H2D / kernel / D2H pipeline over two streams for the host-array
-  // fused entry points.  Chunk k runs on stream k%2; its buffers are the k%2
-  // half of the scratch, so chunk k+2 waits (stream order) for chunk k.
-  template<class T>
-  void xsScatterHost( ScatterObj& o, const T* ekin, unsigned long n, T* xs, T* ef, T* mu )
-  {
-    checkSize( n, 1 );
-    if ( n == 0 )
-      return;
-    DeviceMaterial& dm = *o.mat;
-    Scratch& s = scratchFor( dm );
-    static thread_local cudaStream_t s2 = nullptr;
-    static thread_local int s2dev = -1;
-    if ( s2dev != dm.device ) {
-      checkCuda( cudaStreamCreateWithFlags( &s2, cudaStreamNonBlocking ), "cudaStreamCreate" );
-      s2dev = dm.device;
-    }
-    const uint64_t chunk = std::min<uint64_t>( n, uint64_t(1) << 22 );
-    ensure( s.d_in, s.cap_in, 2 * chunk * sizeof(T) );
-    ensure( s.d_a, s.cap_a, 2 * chunk * sizeof(T) );
-    ensure( s.d_b, s.cap_b, 2 * chunk * sizeof(T) );
-    ensure( s.d_c, s.cap_c, 2 * chunk * sizeof(T) );
-    const uint32_t call = nextCall( o );
-    cudaStream_t st[2] = { s.stream, s2 };
-    checkCuda( cudaMemsetAsync( s.d_nfail, 0, sizeof(unsigned long long), s.stream ), "memset" );
-    cudaEvent_t zeroed;
-    checkCuda( cudaEventCreateWithFlags( &zeroed, cudaEventDisableTiming ), "event" );
-    checkCuda( cudaEventRecord( zeroed, s.stream ), "event" );
-    checkCuda( cudaStreamWaitEvent( s2, zeroed, 0 ), "event" );
-    uint64_t k = 0;
-    for ( uint64_t off = 0; off < n; off += chunk, ++k ) {
-      const uint64_t m = std::min<uint64_t>( chunk, n - off );
-      const int h = static_cast<int>( k & 1 );
-      cudaStream_t cs = st[h];
-      T* din = static_cast<T*>( s.d_in ) + h * chunk;
-      T* da = static_cast<T*>( s.d_a ) + h * chunk;
-      T* db = static_cast<T*>( s.d_b ) + h * chunk;
-      T* dc = static_cast<T*>( s.d_c ) + h * chunk;
-      checkCuda( cudaMemcpyAsync( din, ekin + off, m * sizeof(T), cudaMemcpyHostToDevice, cs ), "H2D" );
-      cudaError_t e;
-      if ( sizeof(T) == 8 )
-        e = ncgb::launchXSScatter( dm.view, reinterpret_cast<const double*>( din ), m, o.seed, call,
-                                   o.streamidx, static_cast<uint32_t>( off ),
-                                   xs ? reinterpret_cast<double*>( da ) : nullptr,
-                                   ef ? reinterpret_cast<double*>( db ) : nullptr,
-                                   mu ? reinterpret_cast<double*>( dc ) : nullptr,
-                                   nullptr, s.d_nfail, cs );
-      else
-        e = ncgb::launchXSScatterF32( dm.view, reinterpret_cast<const float*>( din ), m, o.seed, call,
-                                      o.streamidx, static_cast<uint32_t>( off ),
-                                      xs ? reinterpret_cast<float*>( da ) : nullptr,
-                                      ef ? reinterpret_cast<float*>( db ) : nullptr,
-                                      mu ? reinterpret_cast<float*>( dc ) : nullptr,
-                                      nullptr, s.d_nfail, cs );
-      checkCuda( e, "fused kernel launch" );
-      if ( xs ) checkCuda( cudaMemcpyAsync( xs + off, da, m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
-      if ( ef ) checkCuda( cudaMemcpyAsync( ef + off, db, m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
-      if ( mu ) checkCuda( cudaMemcpyAsync( mu + off, dc, m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
-    }
-    checkCuda( cudaStreamSynchronize( s2 ), "fused kernel" );
-    checkCuda( cudaStreamSynchronize( s.stream ), "fused kernel" );
-    cudaEventDestroy( zeroed );
-    unsigned long long nfail = 0;
-    checkCuda( cudaMemcpy( &nfail, s.d_nfail, sizeof(nfail), cudaMemcpyDeviceToHost ), "D2H" );
-    s.last_nfailed = static_cast<unsigned long>( nfail );
-    if ( nfail )
-      throwSamplingFailure( static_cast<unsigned long>( nfail ) );
-  }
-
-  template<class T>
-  void fillSentinels( unsigned long n, T* xs, T* ef, T* mu )
-  {
-    for ( unsigned long k = 0; k < n; ++k ) {
-      if ( xs ) xs[k] = T(-1);
-      if ( ef ) ef[k] = T(-1);
-      if ( mu ) mu[k] = T(-999);
-    }
-  }
-}
-
-extern "C" {
 
 void ncgb_xs_scatter_many( ncrystal_scatter_t sc, const double* ekin, unsigned long n,
                            double* xs, double* ef, double* mu )

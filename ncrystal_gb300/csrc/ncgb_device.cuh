@@ -1,15 +1,19 @@
-// Device-side evaluation of one neutron against one material: cross-section
+// Device-side evaluation of neutrons against one material: cross-section
 // (ProcComposition over PowderBragg / ElIncScatter / SABScatter / FreeGas) and
-// one isotropic scatter (E', mu).  FP64 throughout, so that the results agree
-// with NCrystal's own to rounding; the control flow and the order of random
-// draws follow the reference function for function (each cites its source).
+// one isotropic scatter (E', mu).  FP64 arithmetic, so that results agree with
+// NCrystal's own to rounding; the control flow and the order of random draws
+// follow the reference function for function (each cites its source).
 //
-// GB300 notes:
+// GB300 notes (its FP64 pipe is 1/64 of the FP32 rate, and every warp
+// instruction occupies it for the full warp whatever the number of active
+// lanes):
 //   * Binary searches over non-negative tables (energy grids, cumulative sums,
-//     CDFs) compare the IEEE-754 bit patterns as 64-bit integers, which orders
-//     non-negative doubles exactly like a floating-point compare but runs on
-//     the integer pipe: GB300's FP64 pipe is narrow and stays free for the
-//     arithmetic.
+//     CDFs) compare IEEE-754 bit patterns as 64-bit integers: same order as a
+//     floating-point compare for non-negative doubles, on the integer pipe.
+//   * Uniform doubles are assembled from the Philox bits with integer ops.
+//   * The S(alpha,beta) sampler is a per-lane state machine (one Alg.1
+//     attempt per step), driven by a persistent kernel that refills finished
+//     lanes from a queue, so that warps stay full through the rejection loops.
 //   * Every loop is bounded.  A neutron whose rejection loop hits the
 //     reference's cap (100 tries) ends with status NCGB_ST_LOOPCAP, which the
 //     host reports as the reference's CalcError.
@@ -26,6 +30,28 @@ namespace ncgb_dev {
   __device__ __forceinline__ double ldg( const double* p ) { return __ldg(p); }
   __device__ __forceinline__ long long ldgbits( const double* p ) { return __double_as_longlong( __ldg(p) ); }
   __device__ __forceinline__ long long bits( double x ) { return __double_as_longlong(x); }
+
+  // Uniform double in (0,1]: same value as ncgb_rng_generate, built with
+  // integer ops (k in [1, 2^53] -> k * 2^-53, exact).
+  __device__ __forceinline__ double rand01( ncgb_rng& r )
+  {
+    if ( r.have == 0 ) {
+      uint32_t ctr[4] = { r.block, r.ctr1, r.ctr2, r.ctr3 };
+      uint32_t o[4];
+      ncgb_philox4x32_10( ctr, r.key0, r.key1, o );
+      r.block += 1;
+      r.cache[0] = (uint64_t)o[0] | ( (uint64_t)o[1] << 32 );
+      r.cache[1] = (uint64_t)o[2] | ( (uint64_t)o[3] << 32 );
+      r.have = 2;
+    }
+    const uint64_t k = ( r.cache[2 - r.have] >> 11 ) + 1;
+    r.have -= 1;
+    const int p = 63 - __clzll( (long long)k );           // highest set bit, 0..53
+    const uint64_t mant = ( k << ( 52 - ( p < 52 ? p : 52 ) ) ) & 0xFFFFFFFFFFFFFull;
+    const uint64_t b = ( p == 53 ) ? 0x3FF0000000000000ull
+                                   : ( ( (uint64_t)( p + 970 ) << 52 ) | mant );
+    return __longlong_as_double( (long long)b );
+  }
 
   // std::upper_bound on [a, a+n) for x >= 0 and a[] >= 0 (not NaN): first i
   // with a[i] > x.
@@ -57,6 +83,8 @@ namespace ncgb_dev {
   __device__ __forceinline__ double clampd( double x, double lo, double hi ) { return x < lo ? lo : ( x > hi ? hi : x ); }
   __device__ __forceinline__ double maxd( double a, double b ) { return a < b ? b : a; }
   __device__ __forceinline__ bool contains( double lo, double hi, double e ) { return e >= lo && e <= hi; }
+  __device__ __forceinline__ bool finited( double x ) { return ( bits(x) & 0x7FF0000000000000LL ) != 0x7FF0000000000000LL; }
+  __device__ __forceinline__ double infd() { return __longlong_as_double( 0x7FF0000000000000LL ); }
 
   // ---- kinematics (NCKinUtils.hh:64-124, NCKinUtils.cc:25-58) ---------------
   struct ALim { double lo, hi; };
@@ -87,8 +115,8 @@ namespace ncgb_dev {
     s = t;
   }
 
-  // Returns NCGB_ST_CALCERROR where the reference throws (E*E' == 0,
-  // NCKinUtils.cc:40-45).
+  // convertAlphaBetaToDeltaEMu, NCKinUtils.cc:25-58.  Returns
+  // NCGB_ST_CALCERROR where the reference throws (E*E' == 0).
   __device__ __forceinline__ int alphaBetaToDeltaEMu( double alpha, double beta, double ekin, double kT,
                                                       double& deltaE, double& mu )
   {
@@ -121,15 +149,13 @@ namespace ncgb_dev {
   constexpr double kElIncXS = 16.0 * 9.86960440108935861883449099987615113531369941 * 12.22430978582345950656;
   constexpr double kElIncMu = 8.0 * 9.86960440108935861883449099987615113531369941 * 12.22430978582345950656;
 
-  // ElIncXS::evalXSContribsCommul, NCElIncXS.cc:130-141
-  __device__ __forceinline__ double elincXS( const ncgb_elinc_view& v, double ekin, double* commul )
+  // ElIncXS::evaluate (NCElIncXS.cc:117-128)
+  __device__ __forceinline__ double elincXS( const ncgb_elinc_view& v, double ekin )
   {
     const double e = kElIncXS * ekin;
     double xs = 0.0;
-    for ( int i = 0; i < v.n && i < NCGB_MAX_ELINC; ++i ) {
+    for ( int i = 0; i < v.n && i < NCGB_MAX_ELINC; ++i )
       xs += v.sigma[i] * oneMinusExpMtDivT( v.msd[i] * e );
-      if ( commul ) commul[i] = xs;
-    }
     return xs;
   }
 
@@ -137,7 +163,7 @@ namespace ncgb_dev {
   __device__ __forceinline__ double braggXS( const ncgb_bragg_view& v, double ekin, int64_t& idx_out )
   {
     idx_out = 0;
-    if ( v.n == 0 || ekin < v.threshold || !isfinite(ekin) )
+    if ( v.n == 0 || ekin < v.threshold || !finited(ekin) )
       return 0.0;
     const int64_t idx = upper_bound_nn( v.two_dE + 1, v.n - 1, ekin );
     idx_out = idx;
@@ -152,7 +178,7 @@ namespace ncgb_dev {
     const double a = sqrt( a_squared );
     if ( a < 0.1 ) {
       if ( a == 0.0 )
-        return __longlong_as_double(0x7ff0000000000000LL);
+        return infd();
       const double a2 = a_squared;
       return 0.564189583547756286948079451560772585844050629
         * ( 2.0 / a + a *( (2.0/3.0)- a2*((1.0/15.0)-a2*((1.0/105.0)-a2*((1.0/756.0)-a2*(1.0/5940.0))))));
@@ -171,7 +197,7 @@ namespace ncgb_dev {
     if ( iu == ne ) {
       xs = s.kext / ekin + s.ext_sigma_free * freeGasShape( s.ext_ca * ekin );
     } else if ( iu == 0 ) {
-      xs = ekin > 0.0 ? sqrt( ldg(s.egrid) / ekin ) * ldg(s.xs) : __longlong_as_double(0x7ff0000000000000LL);
+      xs = ekin > 0.0 ? sqrt( ldg(s.egrid) / ekin ) * ldg(s.xs) : infd();
     } else {
       const double el = ldg( s.egrid + iu - 1 ), eu = ldg( s.egrid + iu );
       const double xl = ldg( s.xs + iu - 1 ), xu = ldg( s.xs + iu );
@@ -180,58 +206,65 @@ namespace ncgb_dev {
     return xs * s.internal_scale;
   }
 
-  // ProcComposition::updateCacheIsotropic, NCProcImpl.cc:166-204.  Also
-  // returns the last valid Bragg plane of each Bragg component.
-  __device__ __forceinline__ double xsCommul( const ncgb_material_view& m, double ekin,
-                                              double* commul, int64_t* braggIdx )
+  __device__ __forceinline__ double compXS( const ncgb_comp_view& c, double ekin )
   {
+    if ( !contains( c.elow, c.ehigh, ekin ) )
+      return 0.0;
+    int64_t dummy;
+    switch ( c.type ) {
+      case NCGB_COMP_ELINC: return elincXS( c.elinc, ekin );
+      case NCGB_COMP_BRAGG: return braggXS( c.bragg, ekin, dummy );
+      case NCGB_COMP_SAB: return sabXS( c.sab, ekin );
+      case NCGB_COMP_FREEGAS: return c.fg.sigma_free * freeGasShape( c.fg.ca * ekin );
+      default: return 0.0;
+    }
+  }
+
+  // ProcComposition::updateCacheIsotropic (NCProcImpl.cc:166-204) and
+  // pickRandIdxByWeight (NCRandUtils.hh:130-133, NCRandUtils.cc:198-222),
+  // with the cumulative cross-sections in registers (fully unrolled).
+  struct XSPick { double xs; int comp; };
+
+  template<bool Pick>
+  __device__ __forceinline__ XSPick xsAndPick( const ncgb_material_view& m, double ekin, ncgb_rng& rng )
+  {
+    double commul[NCGB_MAX_COMP];
     double tot = 0.0;
-    for ( int i = 0; i < m.ncomp; ++i ) {
-      const ncgb_comp_view& c = m.comp[i];
-      double xs = 0.0;
-      braggIdx[i] = 0;
-      if ( contains( c.elow, c.ehigh, ekin ) ) {
-        switch ( c.type ) {
-          case NCGB_COMP_ELINC: xs = elincXS( c.elinc, ekin, nullptr ); break;
-          case NCGB_COMP_BRAGG: xs = braggXS( c.bragg, ekin, braggIdx[i] ); break;
-          case NCGB_COMP_SAB: xs = sabXS( c.sab, ekin ); break;
-          case NCGB_COMP_FREEGAS: xs = c.fg.sigma_free * freeGasShape( c.fg.ca * ekin ); break;
-          default: break;
-        }
-      }
-      commul[i] = ( tot += ( c.scale * xs ) );
+#pragma unroll
+    for ( int i = 0; i < NCGB_MAX_COMP; ++i ) {
+      if ( i < m.ncomp )
+        tot += m.comp[i].scale * compXS( m.comp[i], ekin );
+      commul[i] = tot;
     }
-    return tot;
-  }
-
-  // pickRandIdxByWeight (NCRandUtils.hh:130-133, NCRandUtils.cc:198-222)
-  __device__ __forceinline__ int pickIdx( ncgb_rng& rng, const double* commul, int n )
-  {
-    if ( n == 1 )
-      return 0;
-    const double r = ncgb_rng_generate( &rng );
-    const double choice = commul[n-1] * r;
+    XSPick r{ tot, 0 };
+    if ( !Pick || m.ncomp <= 1 )
+      return r;
+    const double choice = tot * rand01( rng );
+    const int n = m.ncomp;
+    int pick = n - 1;
     if ( n < 5 ) {
-      for ( int i = 0; i < n; ++i )
-        if ( commul[i] > choice )
-          return i;
-      return n - 1;
+      // linear search: first commul > choice
+#pragma unroll
+      for ( int i = NCGB_MAX_COMP - 1; i >= 0; --i )
+        if ( i < n && commul[i] > choice )
+          pick = i;
+    } else {
+      // lower_bound: first commul >= choice, capped at n-1
+#pragma unroll
+      for ( int i = NCGB_MAX_COMP - 1; i >= 0; --i )
+        if ( i < n && commul[i] >= choice )
+          pick = i;
     }
-    int lo = 0, len = n;
-    while ( len > 0 ) {
-      int half = len >> 1;
-      if ( commul[lo+half] < choice ) { lo += half + 1; len -= half + 1; }
-      else len = half;
-    }
-    return lo < n - 1 ? lo : n - 1;
+    r.comp = pick;
+    return r;
   }
 
-  // ---- samplers -----------------------------------------------------------------
+  // ---- non-SAB samplers -----------------------------------------------------------
 
   // PowderBragg::genScatterMu, NCPowderBragg.cc:178-200
   __device__ __forceinline__ double braggMu( const ncgb_bragg_view& v, ncgb_rng& rng, double ekin, int64_t idx )
   {
-    const double r = ncgb_rng_generate( &rng );
+    const double r = rand01( rng );
     const int64_t k = lower_bound_nn( v.fdm_commul, idx, r * ldg( v.fdm_commul + idx ) );
     return 1.0 - 2.0 * ( ldg( v.two_dE + k ) / ekin );
   }
@@ -247,32 +280,44 @@ namespace ncgb_dev {
   // ElIncXS::sampleMuMonoAtomic, NCElIncXS.cc:81-115.  The reference's
   // rejection loop is unbounded; its acceptance is above 98% here, and the
   // cap only guards the GPU.
-  __device__ __forceinline__ double elincMuMono( ncgb_rng& rng, double ekin, double msd, int& status )
+  __device__ __noinline__ double elincMuMono( ncgb_rng& rng, double ekin, double msd, int& status )
   {
     const double a = ( kElIncMu * ekin ) * msd;
     if ( a < 0.01 ) {
       const double maxval = expSmall( a );
       for ( int it = 0; it < 100000; ++it ) {
-        const double mu = ncgb_rng_generate( &rng ) * 2.0 - 1.0;
-        if ( ncgb_rng_generate( &rng ) * maxval < expSmall( a * mu ) )
+        const double mu = rand01( rng ) * 2.0 - 1.0;
+        if ( rand01( rng ) * maxval < expSmall( a * mu ) )
           return mu;
       }
       status = NCGB_ST_LOOPCAP;
       return 1.0;
     }
-    return clampd( log1p( ncgb_rng_generate( &rng ) * expm1( 2.0 * a ) ) / a - 1.0, -1.0, 1.0 );
+    return clampd( log1p( rand01( rng ) * expm1( 2.0 * a ) ) / a - 1.0, -1.0, 1.0 );
   }
 
-  // ElIncXS::EPointAnalysis::sampleMu, NCElIncXS.cc:178-191
-  __device__ __forceinline__ double elincMu( const ncgb_elinc_view& v, ncgb_rng& rng, double ekin, int& status )
+  // ElIncXS::EPointAnalysis::sampleMu, NCElIncXS.cc:178-191 (element picked
+  // by pickRandIdxByWeight on the cumulative contributions).
+  __device__ __noinline__ double elincMu( const ncgb_elinc_view& v, ncgb_rng& rng, double ekin, int& status )
   {
     if ( v.n == 1 )
       return elincMuMono( rng, ekin, v.msd[0], status );
-    double commul[NCGB_MAX_ELINC];
-    elincXS( v, ekin, commul );
-    const int i = pickIdx( rng, commul, v.n );
-    return elincMuMono( rng, ekin, v.msd[i], status );
+    const double e = kElIncXS * ekin;
+    double tot = 0.0;
+    for ( int i = 0; i < v.n && i < NCGB_MAX_ELINC; ++i )
+      tot += v.sigma[i] * oneMinusExpMtDivT( v.msd[i] * e );
+    const double choice = tot * rand01( rng );
+    int pick = v.n - 1;
+    double c = 0.0;
+    const bool linear = v.n < 5;
+    for ( int i = 0; i < v.n && i < NCGB_MAX_ELINC; ++i ) {
+      c += v.sigma[i] * oneMinusExpMtDivT( v.msd[i] * e );
+      if ( linear ? ( c > choice ) : ( c >= choice ) ) { pick = i; break; }
+    }
+    return elincMuMono( rng, ekin, v.msd[pick], status );
   }
+
+  // ---- S(alpha,beta) sampling (Alg.1) -----------------------------------------------
 
   // PointwiseDist::percentileWithIndex, NCPointwiseDist.cc:76-110
   __device__ __forceinline__ double percentile( const double* x, const double* y, const double* cdf, int64_t n,
@@ -301,15 +346,17 @@ namespace ncgb_dev {
     return clampd( x0 + zdx, x0, x1 );
   }
 
-  // SABUtils::sampleLogLinDist_fast, NCSABUtils.hh:282-304
+  // SABUtils::sampleLogLinDist_fast, NCSABUtils.hh:282-304.  The reference's
+  // a_sub_b*log(fa*exp(a*L/a_sub_b)/(fa+r*df))/L, with L = logfb-logfa, is
+  // evaluated as a + (b-a)*log1p(r*df/fa)/L: the same value algebraically,
+  // one transcendental instead of two, and no cancellation at small r.
   __device__ __forceinline__ double logLin( double a, double fa, double b, double fb, double rnd, double logfa, double logfb )
   {
     double df = fb - fa;
     if ( fa * fb * df != 0.0 ) {
-      const double a_sub_b = a - b;
-      const double logfa_fb = logfb - logfa;
-      if ( a_sub_b * logfa_fb != 0.0 )
-        return a_sub_b * log( fa * exp( a * logfa_fb / a_sub_b ) / ( fa + rnd * df ) ) / logfa_fb;
+      const double L = logfb - logfa;
+      if ( ( a - b ) * L != 0.0 )
+        return a + ( b - a ) * ( log1p( rnd * df / fa ) / L );
       df = 0.0;
     }
     if ( !df )
@@ -369,167 +416,163 @@ namespace ncgb_dev {
                    p2, ldg( logsab + bi ), ldg( &info->back_logsval ) );
   }
 
-  // SABSamplerAtE_Alg1::sampleAlphaBeta, NCSABSamplerModels.cc:48-155
-  __device__ __forceinline__ int alg1( const ncgb_sab_view& s, int64_t ie, double x, ncgb_rng& rng,
-                                       double& alpha_out, double& beta_out )
+  // First beta bin with a kinematic endpoint (NCSABSamplerModels.cc:69-116):
+  // beta uniform in the bin, alpha from the first row, up to 30 tries.
+  // Returns 1 if (alpha, beta) is accepted, 0 if the attempt is rejected.
+  __device__ __noinline__ int alg1FirstBin( const ncgb_sab_view& s, const ncgb_alpha_info* infos, int64_t ioff,
+                                            double fbkep, double b1, double x, ncgb_rng& rng,
+                                            double& alpha_out, double& beta_out )
+  {
+    const double b0 = fbkep;
+    if ( b1 < -x )
+      return 0;
+    const double delta_beta = b1 - b0;
+    double alphaval = 0.0;
+    double beta = b0;
+    for ( int iii = 0; iii < 30; ++iii ) {
+      beta = maxd( fbkep, b0 + delta_beta * rand01( rng ) );
+      if ( beta < -x )
+        break;
+      alphaval = sampleAlpha( s, infos, ioff, ioff, rand01( rng ) );
+      const ALim al = alphaLimits( -fbkep, beta );
+      if ( inInterval( al.lo, al.hi, alphaval ) )
+        break;
+      if ( iii == 29 ) {
+        alphaval = 0.5 * ( al.lo + al.hi );
+        break;
+      }
+    }
+    if ( beta < -x )
+      return 0;
+    const ALim al2 = alphaLimits( x, beta );
+    if ( inInterval( al2.lo, al2.hi, alphaval ) ) {
+      alpha_out = alphaval;
+      beta_out = beta;
+      return 1;
+    }
+    return 0;
+  }
+
+  // One attempt of SABSamplerAtE_Alg1::sampleAlphaBeta's loop
+  // (NCSABSamplerModels.cc:59-148) at energy-grid point ie, sampling energy
+  // x = E/kT.  Returns 1 with (alpha, beta) on acceptance, 0 on rejection.
+  __device__ __forceinline__ int alg1Attempt( const ncgb_sab_view& s, int64_t ie, double x, ncgb_rng& rng,
+                                              double& alpha_out, double& beta_out )
   {
     const int64_t off = __ldg( s.smp_offset + ie );
     const int64_t nbs = __ldg( s.smp_nbeta + ie );
     const double* bx = s.bx + off;
-    const double* by = s.by + off;
-    const double* bcdf = s.bcdf + off;
     const ncgb_alpha_info* infos = s.info + off;
     const int64_t ioff = __ldg( s.smp_ibetaoffset + ie );
+    int64_t ibs;
+    const double beta = percentile( bx, s.by + off, s.bcdf + off, nbs, rand01( rng ), ibs );
     const double fbkep = ldg( s.smp_fbkep + ie );
-    const double bg0 = ldg( s.beta );
-    for ( int iloop = 0; iloop < 100; ++iloop ) {
-      int64_t ibs;
-      double beta = percentile( bx, by, bcdf, nbs, ncgb_rng_generate( &rng ), ibs );
-      if ( ibs == 0 && fbkep <= 0.0 ) {
-        const double b0 = fbkep;
-        const double b1 = ldg( bx + 1 );
-        if ( b1 < -x )
-          continue;
-        const double delta_beta = b1 - b0;
-        double alphaval = 0.0;
-        for ( int iii = 0; iii < 30; ++iii ) {
-          beta = maxd( fbkep, b0 + delta_beta * ncgb_rng_generate( &rng ) );
-          if ( beta < -x )
-            break;
-          alphaval = sampleAlpha( s, infos, ioff, ioff, ncgb_rng_generate( &rng ) );
-          const ALim al = alphaLimits( -fbkep, beta );
-          if ( inInterval( al.lo, al.hi, alphaval ) )
-            break;
-          if ( iii == 29 ) {
-            alphaval = 0.5 * ( al.lo + al.hi );
-            break;
-          }
-        }
-        if ( beta < -x )
-          continue;
-        const ALim al2 = alphaLimits( x, beta );
-        if ( inInterval( al2.lo, al2.hi, alphaval ) ) {
-          alpha_out = alphaval; beta_out = beta; return NCGB_ST_OK;
-        }
-        continue;
-      }
-      if ( beta <= maxd( -x, bg0 ) )
-        continue;
-      const double rp = ncgb_rng_generate( &rng );
-      const int64_t ibeta = ioff + ibs;
-      if ( ibeta < 1 )
-        continue; // cannot happen (beta > beta grid front); keeps indexing in bounds
-      const double bl = ldg( s.beta + ibeta - 1 );
-      const double alphal = sampleAlpha( s, infos, ioff, ibeta - 1, rp );
-      const double bh = ldg( s.beta + ibeta );
-      const double alphah = sampleAlpha( s, infos, ioff, ibeta, rp );
-      const double alpha = alphal + ( alphah - alphal ) * ( beta - bl ) / ( bh - bl );
-      const ALim al = alphaLimits( x, beta );
-      if ( inInterval( al.lo, al.hi, alpha ) ) {
-        alpha_out = alpha; beta_out = beta; return NCGB_ST_OK;
-      }
+    if ( ibs == 0 && fbkep <= 0.0 )
+      return alg1FirstBin( s, infos, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+    if ( beta <= maxd( -x, ldg( s.beta ) ) )
+      return 0;
+    const double rp = rand01( rng );
+    const int64_t ibeta = ioff + ibs;
+    if ( ibeta < 1 )
+      return 0; // cannot happen (beta above the beta grid front); keeps indices in bounds
+    const double bl = ldg( s.beta + ibeta - 1 );
+    const double alphal = sampleAlpha( s, infos, ioff, ibeta - 1, rp );
+    const double bh = ldg( s.beta + ibeta );
+    const double alphah = sampleAlpha( s, infos, ioff, ibeta, rp );
+    const double alpha = alphal + ( alphah - alphal ) * ( beta - bl ) / ( bh - bl );
+    const ALim al = alphaLimits( x, beta );
+    if ( inInterval( al.lo, al.hi, alpha ) ) {
+      alpha_out = alpha;
+      beta_out = beta;
+      return 1;
     }
-    return NCGB_ST_LOOPCAP;
+    return 0;
   }
 
-  // SABSampler::sampleAlphaBeta + sampleDeltaEMu (NCSABSampler.cc:158-236),
-  // SABScatter::sampleScatterIsotropic (NCSABScatter.cc:92-101).
-  __device__ __forceinline__ int sabScatter( const ncgb_sab_view& s, ncgb_rng& rng, double ekin, double& ef, double& mu )
+  // Per-neutron state of SABSampler::sampleAlphaBeta (NCSABSampler.cc:158-227)
+  // with its two nested rejection loops flattened: 'outer' counts Alg.1 calls
+  // (<=100), 'inner' the attempts of the current call (<=100).
+  struct SABLane {
+    double ekin, x, xsamp;
+    int64_t ie;
+    int inner, outer;
+    bool ultra_small;
+  };
+
+  // Set-up of a SAB scatter at energy ekin (NCSABSampler.cc:163-197).
+  // Returns NCGB_ST_UNSUPPORTED for E >= Emax (free-gas extender).
+  __device__ __forceinline__ int sabBegin( const ncgb_sab_view& s, double ekin, SABLane& L )
   {
     const int64_t ne = s.ne;
     int64_t iu = upper_bound_nn( s.egrid, ne, ekin );
-    bool ultra_small = false;
-    int64_t ie;
-    if ( iu == ne ) {
-      return NCGB_ST_UNSUPPORTED; // E >= Emax: free-gas extender (NCSABSampler.cc:59-156)
-    } else if ( iu == 0 ) {
-      ie = 0;
-      ultra_small = ( ekin < ldg( s.egrid ) );
+    L.ekin = ekin;
+    L.ultra_small = false;
+    L.inner = 0;
+    L.outer = 0;
+    L.ie = 0;
+    L.x = 0.0;
+    L.xsamp = 0.0;
+    if ( iu == ne )
+      return NCGB_ST_UNSUPPORTED;
+    if ( iu == 0 ) {
+      L.ie = 0;
+      L.ultra_small = ( ekin < ldg( s.egrid ) );
     } else {
       if ( s.egrid_margin > 1.0 ) {
         const double em = ekin * s.egrid_margin;
         while ( iu + 1 != ne && em > ldg( s.egrid + iu ) )
           ++iu;
       }
-      ie = iu;
+      L.ie = iu;
     }
-    const double x = ekin / s.kT;
-    const double xs_ = ultra_small ? ldg( s.egrid ) / s.kT : x;
-    const int kind = __ldg( s.smp_kind + ie );
-    double alpha = 0.0, beta = 0.0;
-    bool found = false;
-    for ( int loop = 0; loop < 100; ++loop ) {
-      if ( kind == 0 ) {
-        alpha = 0.0; beta = 0.0;
-      } else {
-        const int st = alg1( s, ie, xs_, rng, alpha, beta );
-        if ( st != NCGB_ST_OK )
-          return st;
-      }
-      if ( beta < -x )
-        continue;
-      const ALim al = alphaLimits( x, beta );
-      if ( inInterval( al.lo, al.hi, alpha ) ) { found = true; break; }
-      if ( ultra_small ) {
-        alpha = al.lo + ncgb_rng_generate( &rng ) * ( al.hi - al.lo );
-        found = true;
-        break;
-      }
-    }
-    if ( !found )
-      return NCGB_ST_LOOPCAP;
-    double deltaE, muv;
-    if ( beta <= x * ( -1.0 + 1e-14 ) ) { // muIsotropicAtBeta, NCKinUtils.hh:64-70
-      deltaE = beta * s.kT;
-      muv = ncgb_rng_generate( &rng ) * 2.0 - 1.0;
-    } else {
-      const int st = alphaBetaToDeltaEMu( alpha, beta, ekin, s.kT, deltaE, muv );
-      if ( st != NCGB_ST_OK )
-        return st;
-    }
-    ef = maxd( 0.0, ekin + deltaE );
-    mu = muv;
+    L.x = ekin / s.kT;
+    L.xsamp = L.ultra_small ? ldg( s.egrid ) / s.kT : L.x;
     return NCGB_ST_OK;
   }
 
-  // One neutron: cross-section (ProcComposition::crossSectionIsotropic,
-  // NCProcImpl.cc:353-362) and, if wanted, one scatter
-  // (ProcComposition::sampleScatterIsotropic, NCProcImpl.cc:379-389).
-  template<bool DoXS, bool DoScatter>
-  __device__ __forceinline__ int evalNeutron( const ncgb_material_view& m, ncgb_rng& rng, double ekin,
-                                              double& xs, double& ef, double& mu )
+  // One step of the flattened loops.  Returns -1 to continue, NCGB_ST_OK when
+  // (ef, mu) are final, or an error status.
+  __device__ __forceinline__ int sabStep( const ncgb_sab_view& s, SABLane& L, ncgb_rng& rng, double& ef, double& mu )
   {
-    xs = 0.0; ef = ekin; mu = 1.0;
-    if ( !contains( m.dom_elow, m.dom_ehigh, ekin ) )
-      return NCGB_ST_OK;
-    double commul[NCGB_MAX_COMP];
-    int64_t braggIdx[NCGB_MAX_COMP];
-    xs = xsCommul( m, ekin, commul, braggIdx );
-    if ( !DoScatter )
-      return NCGB_ST_OK;
-    const int ic = pickIdx( rng, commul, m.ncomp );
-    const ncgb_comp_view& c = m.comp[ic];
-    int st = NCGB_ST_OK;
-    switch ( c.type ) {
-      case NCGB_COMP_BRAGG:
-        // PowderBragg::sampleScatterIsotropic, NCPowderBragg.cc:202-216
-        if ( !( c.bragg.n == 0 || ekin < c.bragg.threshold || !isfinite(ekin) ) )
-          mu = braggMu( c.bragg, rng, ekin, braggIdx[ic] );
-        break;
-      case NCGB_COMP_ELINC:
-        mu = elincMu( c.elinc, rng, ekin, st );
-        break;
-      case NCGB_COMP_SAB:
-        st = sabScatter( c.sab, rng, ekin, ef, mu );
-        break;
-      case NCGB_COMP_FREEGAS:
-        st = NCGB_ST_UNSUPPORTED;
-        break;
-      default:
-        break;
+    double alpha = 0.0, beta = 0.0;
+    if ( __ldg( s.smp_kind + L.ie ) != 0 ) {
+      if ( !alg1Attempt( s, L.ie, L.xsamp, rng, alpha, beta ) ) {
+        if ( ++L.inner >= 100 )
+          return NCGB_ST_LOOPCAP;
+        return -1;
+      }
+    } // else SABSamplerAtE_NoScatter: (alpha, beta) = (0, 0), no draws
+    // an Alg.1 call completed: the outer loop's tests
+    L.inner = 0;
+    const double x = L.x;
+    bool accept = false;
+    if ( !( beta < -x ) ) {
+      const ALim al = alphaLimits( x, beta );
+      if ( inInterval( al.lo, al.hi, alpha ) ) {
+        accept = true;
+      } else if ( L.ultra_small ) {
+        alpha = al.lo + rand01( rng ) * ( al.hi - al.lo );
+        accept = true;
+      }
     }
-    if ( st != NCGB_ST_OK ) { ef = -1.0; mu = -999.0; }
-    return st;
+    if ( !accept ) {
+      if ( ++L.outer >= 100 )
+        return NCGB_ST_LOOPCAP;
+      return -1;
+    }
+    // SABSampler::sampleDeltaEMu (NCSABSampler.cc:229-236), SABScatter (NCSABScatter.cc:92-101)
+    double deltaE, muv;
+    if ( beta <= x * ( -1.0 + 1e-14 ) ) { // muIsotropicAtBeta, NCKinUtils.hh:64-70
+      deltaE = beta * s.kT;
+      muv = rand01( rng ) * 2.0 - 1.0;
+    } else {
+      const int st = alphaBetaToDeltaEMu( alpha, beta, L.ekin, s.kT, deltaE, muv );
+      if ( st != NCGB_ST_OK )
+        return st;
+    }
+    ef = maxd( 0.0, L.ekin + deltaE );
+    mu = muv;
+    return NCGB_ST_OK;
   }
 }
 

@@ -1,10 +1,21 @@
 // CUDA kernels of the batched non-oriented scattering path (sm_103a).
 //
-// One thread per output element.  The material's flat table view (~5 KB) is
-// passed by value as a __grid_constant__ kernel parameter, so its scalars sit
-// in the constant bank and every warp reads them with broadcast loads; the
-// tables themselves stay in HBM / L2.  Inputs and outputs are contiguous
-// arrays (structure of arrays), read and written once, coalesced.
+// A batch of neutrons is scattered in two launches:
+//
+//   k_pick   one thread per neutron: composition cross-section, component
+//            pick, and the short samplers (PowderBragg, ElIncScatter) done in
+//            place.  Neutrons that picked an S(alpha,beta) component are
+//            appended to a queue (warp-aggregated atomics, 16 B per entry).
+//   k_sab    persistent warps over the queue: each lane runs the SAB
+//            sampler's flattened rejection loops one Alg.1 attempt per step
+//            and takes the next queued neutron as soon as its own finishes,
+//            so warps stay full while neutrons need different numbers of
+//            attempts.
+//
+// The material's flat table view (~5 KB) is a __grid_constant__ kernel
+// parameter: its scalars sit in the constant bank and warps read them with
+// broadcast loads; the tables stay in HBM / L2.  Inputs and outputs are
+// contiguous arrays, read and written once.
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -13,95 +24,208 @@
 
 namespace {
 
-  template<class T> __device__ __forceinline__ double toD( T v ) { return static_cast<double>(v); }
-  template<class T> __device__ __forceinline__ T fromD( double v ) { return static_cast<T>(v); }
+  using namespace ncgb_dev;
 
-  // Fused: xs + one scatter per neutron, neutron index = i.
-  template<class InT, class OutT>
-  __global__ void __launch_bounds__(256)
-  k_xs_scatter( const __grid_constant__ ncgb_material_view m,
-                const InT* __restrict__ ekin, uint64_t n,
-                uint64_t seed, uint32_t callseq, uint32_t stream, uint32_t index_offset,
-                OutT* __restrict__ out_xs, OutT* __restrict__ out_ef, OutT* __restrict__ out_mu,
-                int32_t* __restrict__ out_status, unsigned long long* __restrict__ nfail )
+  __device__ __forceinline__ double loadE( const ncgb::Batch& b, uint64_t i )
   {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for ( uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride ) {
-      const double e = toD( ekin[i] );
-      ncgb_rng rng;
-      ncgb_rng_init( &rng, seed, (uint32_t)i + index_offset, callseq, stream );
-      double xs, ef, mu;
-      const int st = ncgb_dev::evalNeutron<true,true>( m, rng, e, xs, ef, mu );
-      if ( out_xs ) out_xs[i] = fromD<OutT>( xs );
-      if ( out_ef ) out_ef[i] = fromD<OutT>( ef );
-      if ( out_mu ) out_mu[i] = fromD<OutT>( mu );
-      if ( out_status ) out_status[i] = st;
-      if ( st != NCGB_ST_OK ) atomicAdd( nfail, 1ull );
+    return b.in_f32 ? (double)__ldg( static_cast<const float*>( b.ekin ) + i )
+                    : __ldg( static_cast<const double*>( b.ekin ) + i );
+  }
+
+  __device__ __forceinline__ void store( void* p, int f32, uint64_t o, double v )
+  {
+    if ( !p ) return;
+    if ( f32 ) static_cast<float*>( p )[o] = (float)v;
+    else static_cast<double*>( p )[o] = v;
+  }
+
+  // Write one neutron's scatter result (mode 0: E', mu; mode 1: acos(mu), E'-E).
+  __device__ __forceinline__ void writeScatter( const ncgb::Batch& b, uint64_t o, double e, int st,
+                                                double ef, double mu )
+  {
+    if ( b.status ) b.status[o] = st;
+    if ( st != NCGB_ST_OK ) {
+      atomicAdd( &b.work->nfail, 1ull );
+      if ( b.mode == 1 )
+        return; // genscatter: failed neutrons keep their outputs
+      ef = -1.0;
+      mu = -999.0;
+    }
+    if ( b.mode == 0 ) {
+      store( b.out_a, b.out_f32, o, ef );
+      store( b.out_b, b.out_f32, o, mu );
+    } else {
+      store( b.out_a, b.out_f32, o, acos( mu ) );
+      store( b.out_b, b.out_f32, o, ef - e );
     }
   }
 
-  // Cross-sections only: results[r*n_ekin+i] = xs(ekin[i]) for r < repeat
-  // (ncrystal.cc:1107-1141 writes the same value for every repeat).
-  template<class InT, class OutT>
+  // ---- phase 1: cross-section, pick, short samplers, SAB queue ----------------
   __global__ void __launch_bounds__(256)
-  k_xs( const __grid_constant__ ncgb_material_view m,
-        const InT* __restrict__ ekin, uint64_t n_ekin, uint64_t repeat,
-        OutT* __restrict__ out )
+  k_pick( const __grid_constant__ ncgb_material_view m, const ncgb::Batch b )
   {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for ( uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_ekin; i += stride ) {
-      ncgb_rng dummy;
-      double xs, ef, mu;
-      ncgb_dev::evalNeutron<true,false>( m, dummy, toD( ekin[i] ), xs, ef, mu );
-      for ( uint64_t r = 0; r < repeat; ++r )
-        out[r * n_ekin + i] = fromD<OutT>( xs );
-    }
-  }
-
-  // Scatters for the _many calls: output index o = irepeat*n_ekin + i, energy
-  // ekin[i], stream neutron index o.  mode 0: (E', mu); mode 1: (acos(mu),
-  // E'-E) as ncrystal_genscatter_nonoriented_many.
-  __global__ void __launch_bounds__(256)
-  k_scatter_many( const __grid_constant__ ncgb_material_view m,
-                  const double* __restrict__ ekin, uint64_t n_ekin, uint64_t n_out,
-                  uint64_t seed, uint32_t callseq, uint32_t stream, int mode,
-                  double* __restrict__ out_a, double* __restrict__ out_b,
-                  unsigned long long* __restrict__ nfail )
-  {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for ( uint64_t o = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n_out; o += stride ) {
-      const uint64_t i = o % n_ekin;
-      const double e = ekin[i];
+    for ( uint64_t o = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; o < b.n_out; o += stride ) {
+      const uint64_t i = ( b.n_out == b.n_ekin ) ? o : o % b.n_ekin;
+      const double e = loadE( b, i );
       ncgb_rng rng;
-      ncgb_rng_init( &rng, seed, (uint32_t)o, callseq, stream );
-      double xs, ef, mu;
-      const int st = ncgb_dev::evalNeutron<false,true>( m, rng, e, xs, ef, mu );
-      if ( st != NCGB_ST_OK ) {
-        atomicAdd( nfail, 1ull );
-        if ( mode == 1 )
-          continue; // genscatter: outputs for failed neutrons are left untouched
-      }
-      if ( mode == 0 ) {
-        out_a[o] = ef;
-        out_b[o] = mu;
+      ncgb_rng_init( &rng, b.seed, (uint32_t)o + b.index_offset, b.callseq, b.stream );
+      bool queue = false;
+      int qcomp = 0;
+      if ( !contains( m.dom_elow, m.dom_ehigh, e ) ) {
+        // ProcComposition outside its domain: xs 0, neutron unchanged (NCProcImpl.cc:353-389)
+        store( b.out_xs, b.out_f32, o, 0.0 );
+        writeScatter( b, o, e, NCGB_ST_OK, e, 1.0 );
       } else {
-        out_a[o] = acos( mu );
-        out_b[o] = ef - e;
+        const XSPick p = xsAndPick<true>( m, e, rng );
+        store( b.out_xs, b.out_f32, o, p.xs );
+        const ncgb_comp_view& c = m.comp[p.comp];
+        int st = NCGB_ST_OK;
+        double ef = e, mu = 1.0;
+        switch ( c.type ) {
+          case NCGB_COMP_BRAGG: {
+            // PowderBragg::sampleScatterIsotropic, NCPowderBragg.cc:202-216
+            int64_t idx;
+            braggXS( c.bragg, e, idx );
+            if ( c.bragg.n && e >= c.bragg.threshold && finited(e) )
+              mu = braggMu( c.bragg, rng, e, idx );
+            break;
+          }
+          case NCGB_COMP_ELINC:
+            mu = elincMu( c.elinc, rng, e, st );
+            break;
+          case NCGB_COMP_SAB:
+            if ( e >= ldg( c.sab.egrid + c.sab.ne - 1 ) )
+              st = NCGB_ST_UNSUPPORTED; // E >= Emax: free-gas extender (NCSABSampler.cc:59-156)
+            else
+              queue = true, qcomp = p.comp;
+            break;
+          case NCGB_COMP_FREEGAS:
+            st = NCGB_ST_UNSUPPORTED;
+            break;
+          default:
+            break;
+        }
+        if ( !queue )
+          writeScatter( b, o, e, st, ef, mu );
+      }
+      // warp-aggregated append to the SAB queue
+      const unsigned active = __activemask();
+      const unsigned want = __ballot_sync( active, queue );
+      if ( want ) {
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs( want ) - 1;
+        unsigned base = 0;
+        if ( lane == leader )
+          base = atomicAdd( &b.work->qcount, (unsigned)__popc( want ) );
+        base = __shfl_sync( active, base, leader );
+        if ( queue ) {
+          const unsigned pos = base + __popc( want & ( ( 1u << lane ) - 1u ) );
+          ncgb::QEntry q;
+          q.ekin = e;
+          q.idx = (uint32_t)o;
+          q.comp = (uint16_t)qcomp;
+          q.ndraws = (uint16_t)( 2 * rng.block - rng.have );
+          b.queue[pos] = q;
+        }
       }
     }
+  }
+
+  // ---- phase 2: persistent S(alpha,beta) sampling ---------------------------
+  __global__ void __launch_bounds__(256)
+  k_sab( const __grid_constant__ ncgb_material_view m, const ncgb::Batch b )
+  {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned qcount = *(volatile unsigned*)&b.work->qcount;
+    bool has = false, done = false;
+    ncgb::QEntry q;
+    q.ekin = 0.0; q.idx = 0; q.comp = 0; q.ndraws = 0;
+    SABLane L;
+    ncgb_rng rng;
+    ncgb_rng_init( &rng, 0, 0, 0, 0 );
+    // Bounded: every claimed neutron finishes within 100 x 100 Alg.1 attempts,
+    // and claims stop at qcount.
+    for (;;) {
+      const unsigned need = __ballot_sync( FULL, !has && !done );
+      if ( need ) {
+        const int leader = __ffs( need ) - 1;
+        unsigned base = 0;
+        if ( lane == leader )
+          base = atomicAdd( &b.work->qnext, (unsigned)__popc( need ) );
+        base = __shfl_sync( FULL, base, leader );
+        if ( !has && !done ) {
+          const unsigned slot = base + __popc( need & ( ( 1u << lane ) - 1u ) );
+          if ( slot < qcount ) {
+            q = b.queue[slot];
+            ncgb_rng_init( &rng, b.seed, q.idx + b.index_offset, b.callseq, b.stream );
+            for ( int k = 0; k < q.ndraws; ++k )
+              rand01( rng );
+            const int st = sabBegin( m.comp[q.comp].sab, q.ekin, L );
+            if ( st != NCGB_ST_OK )
+              writeScatter( b, q.idx, q.ekin, st, q.ekin, 1.0 );
+            else
+              has = true;
+          } else {
+            done = true;
+          }
+        }
+      }
+      if ( __all_sync( FULL, done && !has ) )
+        break;
+      if ( has ) {
+        double ef = 0.0, mu = 0.0;
+        const int st = sabStep( m.comp[q.comp].sab, L, rng, ef, mu );
+        if ( st >= 0 ) {
+          writeScatter( b, q.idx, q.ekin, st, ef, mu );
+          has = false;
+        }
+      }
+    }
+  }
+
+  // ---- cross-sections only ------------------------------------------------------
+  // results[r*n_ekin+i] = xs(ekin[i]) for r < repeat (ncrystal.cc:1107-1141
+  // writes the same value for every repeat).
+  __global__ void __launch_bounds__(256)
+  k_xs( const __grid_constant__ ncgb_material_view m, const ncgb::Batch b, uint64_t repeat )
+  {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for ( uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < b.n_ekin; i += stride ) {
+      const double e = loadE( b, i );
+      double xs = 0.0;
+      if ( contains( m.dom_elow, m.dom_ehigh, e ) ) {
+        ncgb_rng dummy;
+        ncgb_rng_init( &dummy, 0, 0, 0, 0 );
+        xs = xsAndPick<false>( m, e, dummy ).xs;
+      }
+      for ( uint64_t r = 0; r < repeat; ++r )
+        store( b.out_xs, b.out_f32, r * b.n_ekin + i, xs );
+    }
+  }
+
+  struct LaunchShape { int nsm = 0; int sab_blocks_per_sm = 0; };
+
+  const LaunchShape& shape()
+  {
+    static LaunchShape s;
+    if ( !s.nsm ) {
+      int dev = 0;
+      cudaGetDevice( &dev );
+      cudaDeviceGetAttribute( &s.nsm, cudaDevAttrMultiProcessorCount, dev );
+      if ( s.nsm <= 0 ) s.nsm = 1;
+      int bps = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_sab, 256, 0 );
+      s.sab_blocks_per_sm = bps > 0 ? bps : 1;
+    }
+    return s;
   }
 
   int gridFor( uint64_t n, int block )
   {
-    static int nsm = 0;
-    if ( !nsm ) {
-      int dev = 0;
-      cudaGetDevice( &dev );
-      cudaDeviceGetAttribute( &nsm, cudaDevAttrMultiProcessorCount, dev );
-      if ( nsm <= 0 ) nsm = 1;
-    }
     uint64_t want = ( n + block - 1 ) / block;
-    uint64_t cap = (uint64_t)nsm * 16; // grid-stride beyond 16 resident blocks per SM
+    uint64_t cap = (uint64_t)shape().nsm * 32; // grid-stride beyond this
     if ( want > cap ) want = cap;
     if ( want < 1 ) want = 1;
     return (int)want;
@@ -110,51 +234,29 @@ namespace {
 
 namespace ncgb {
 
-  cudaError_t launchXSScatter( const ncgb_material_view& m, const double* ekin, uint64_t n,
-                               uint64_t seed, uint32_t callseq, uint32_t stream, uint32_t index_offset,
-                               double* xs, double* ef, double* mu, int32_t* status,
-                               unsigned long long* nfail, cudaStream_t s )
+  cudaError_t launchScatter( const ncgb_material_view& m, const Batch& b, cudaStream_t s )
   {
-    if ( n == 0 ) return cudaSuccess;
-    k_xs_scatter<double,double><<<gridFor(n,256),256,0,s>>>( m, ekin, n, seed, callseq, stream, index_offset,
-                                                             xs, ef, mu, status, nfail );
+    if ( b.n_out == 0 )
+      return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync( &b.work->qcount, 0, 2 * sizeof(unsigned int), s );
+    if ( e != cudaSuccess )
+      return e;
+    k_pick<<<gridFor( b.n_out, 256 ), 256, 0, s>>>( m, b );
+    e = cudaGetLastError();
+    if ( e != cudaSuccess )
+      return e;
+    const LaunchShape& ls = shape();
+    k_sab<<<ls.nsm * ls.sab_blocks_per_sm, 256, 0, s>>>( m, b );
     return cudaGetLastError();
   }
 
-  cudaError_t launchXSScatterF32( const ncgb_material_view& m, const float* ekin, uint64_t n,
-                                  uint64_t seed, uint32_t callseq, uint32_t stream, uint32_t index_offset,
-                                  float* xs, float* ef, float* mu, int32_t* status,
-                                  unsigned long long* nfail, cudaStream_t s )
+  cudaError_t launchXS( const ncgb_material_view& m, const Batch& b, uint64_t repeat, cudaStream_t s )
   {
-    if ( n == 0 ) return cudaSuccess;
-    k_xs_scatter<float,float><<<gridFor(n,256),256,0,s>>>( m, ekin, n, seed, callseq, stream, index_offset,
-                                                           xs, ef, mu, status, nfail );
+    if ( b.n_ekin == 0 || repeat == 0 )
+      return cudaSuccess;
+    k_xs<<<gridFor( b.n_ekin, 256 ), 256, 0, s>>>( m, b, repeat );
     return cudaGetLastError();
   }
 
-  cudaError_t launchXS( const ncgb_material_view& m, const double* ekin, uint64_t n_ekin, uint64_t repeat,
-                        double* out, cudaStream_t s )
-  {
-    if ( n_ekin == 0 || repeat == 0 ) return cudaSuccess;
-    k_xs<double,double><<<gridFor(n_ekin,256),256,0,s>>>( m, ekin, n_ekin, repeat, out );
-    return cudaGetLastError();
-  }
-
-  cudaError_t launchXSF32( const ncgb_material_view& m, const float* ekin, uint64_t n_ekin,
-                           float* out, cudaStream_t s )
-  {
-    if ( n_ekin == 0 ) return cudaSuccess;
-    k_xs<float,float><<<gridFor(n_ekin,256),256,0,s>>>( m, ekin, n_ekin, 1, out );
-    return cudaGetLastError();
-  }
-
-  cudaError_t launchScatterMany( const ncgb_material_view& m, const double* ekin, uint64_t n_ekin, uint64_t n_out,
-                                 uint64_t seed, uint32_t callseq, uint32_t stream, int mode,
-                                 double* out_a, double* out_b, unsigned long long* nfail, cudaStream_t s )
-  {
-    if ( n_out == 0 ) return cudaSuccess;
-    k_scatter_many<<<gridFor(n_out,256),256,0,s>>>( m, ekin, n_ekin, n_out, seed, callseq, stream, mode,
-                                                    out_a, out_b, nfail );
-    return cudaGetLastError();
-  }
+  int scatterLaunchesPerBatch() { return 2; }
 }

@@ -8,23 +8,43 @@
 
 namespace ncgb {
 
-  // Fused cross-section + scatter; neutron i uses stream index i+index_offset.
-  cudaError_t launchXSScatter( const ncgb_material_view& m, const double* ekin, uint64_t n,
-                               uint64_t seed, uint32_t callseq, uint32_t stream, uint32_t index_offset,
-                               double* xs, double* ef, double* mu, int32_t* status,
-                               unsigned long long* nfail, cudaStream_t s );
-  cudaError_t launchXSScatterF32( const ncgb_material_view& m, const float* ekin, uint64_t n,
-                                  uint64_t seed, uint32_t callseq, uint32_t stream, uint32_t index_offset,
-                                  float* xs, float* ef, float* mu, int32_t* status,
-                                  unsigned long long* nfail, cudaStream_t s );
-  cudaError_t launchXS( const ncgb_material_view& m, const double* ekin, uint64_t n_ekin, uint64_t repeat,
-                        double* out, cudaStream_t s );
-  cudaError_t launchXSF32( const ncgb_material_view& m, const float* ekin, uint64_t n_ekin,
-                           float* out, cudaStream_t s );
-  // mode 0: (E', mu); mode 1: (acos(mu), E'-E).
-  cudaError_t launchScatterMany( const ncgb_material_view& m, const double* ekin, uint64_t n_ekin, uint64_t n_out,
-                                 uint64_t seed, uint32_t callseq, uint32_t stream, int mode,
-                                 double* out_a, double* out_b, unsigned long long* nfail, cudaStream_t s );
+  // Device-side counters.  launchScatter zeroes the queue counters at the
+  // start of every batch; the caller zeroes nfail when it wants a new count.
+  struct Work {
+    unsigned long long nfail;  // neutrons with a non-OK status
+    unsigned int qcount;       // SAB queue length
+    unsigned int qnext;        // next queue entry to claim
+  };
+
+  // A neutron queued for S(alpha,beta) sampling: 16 bytes.
+  struct QEntry {
+    double ekin;
+    uint32_t idx;     // output index o (stream neutron index o + index_offset)
+    uint16_t comp;    // SAB component
+    uint16_t ndraws;  // random numbers already drawn (the component pick)
+  };
+
+  // One batch: neutron o (< n_out) has energy ekin[o % n_ekin] and draws
+  // from stream (seed, o + index_offset, callseq, stream).
+  struct Batch {
+    const void* ekin;
+    int in_f32;
+    int out_f32;
+    uint64_t n_ekin, n_out;
+    uint64_t seed;
+    uint32_t callseq, stream, index_offset;
+    int mode;          // 0: out_a = E', out_b = mu;  1: out_a = acos(mu), out_b = E'-E
+    void* out_xs;      // may be null
+    void* out_a;       // may be null
+    void* out_b;       // may be null
+    int32_t* status;   // may be null
+    Work* work;        // scratch, sizeof(Work)
+    QEntry* queue;     // scratch, n_out entries
+  };
+
+  cudaError_t launchScatter( const ncgb_material_view& m, const Batch& b, cudaStream_t s );
+  cudaError_t launchXS( const ncgb_material_view& m, const Batch& b, uint64_t repeat, cudaStream_t s );
+  int scatterLaunchesPerBatch();
 }
 
 #endif
