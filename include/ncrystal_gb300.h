@@ -134,6 +134,21 @@ int ncgb_scatter_device( ncrystal_scatter_t, const double* d_ekin, unsigned long
                          double* d_xs, double* d_ekin_final, double* d_mu,
                          int32_t* d_status, void* stream );
 
+/* No counterpart in the reference.  Same as ncgb_scatter_device (FP64
+ * arrays), but allocates nothing: its working memory is a fixed array inside
+ * the library (16 B per neutron, at most NCGB_NOALLOC_MAX_NEUTRONS neutrons per
+ * call; larger batches are refused with a BadInput error).  For callers that
+ * must not allocate device memory while they run, e.g. a transport code living
+ * in a framework that owns all device memory through its own pool, or one that
+ * cannot take cudaMalloc's device-wide synchronisation inside its loop.  All
+ * calls share that array: calls that overlap on the GPU race.  The first call
+ * on a device looks up the array's address (do it before any stream capture);
+ * the device holding the material must be current. */
+#define NCGB_NOALLOC_MAX_NEUTRONS 1048576u
+int ncgb_scatter_device_noalloc( ncrystal_scatter_t, const double* d_ekin, unsigned long n,
+                                 double* d_xs, double* d_ekin_final, double* d_mu,
+                                 int32_t* d_status, void* stream );
+
 /* Same with FP32 energies in and FP32 results out; all arithmetic in the
  * kernel stays FP64. */
 int ncgb_scatter_device_f32( ncrystal_scatter_t, const float* d_ekin, unsigned long n,

@@ -76,7 +76,7 @@ def build_library(force=False, verbose=False):
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(BUILD, exist_ok=True)
-    cu = ["ncgb_kernels.cu"]
+    cu = ["ncgb_kernels.cu", "ncgb_noalloc.cu"]
     cc = ["ncgb_capi.cc", "ncgb_tables.cc", "ncgb_bundle.cc", "ncgb_hostapi.cc"]
     hdrs = _headers()
     jobs = []

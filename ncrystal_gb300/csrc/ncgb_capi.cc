@@ -845,3 +845,26 @@ unsigned long ncgb_device_bytes( ncrystal_scatter_t sc )
 }
 
 }
+
+// ---- internal hooks for ncgb_noalloc.cu (C++ linkage) ---------------------------------
+namespace ncgb {
+
+  // Validates a handle and returns what a batch launch needs; the call
+  // sequence number is consumed as by any scatter call.  Throws on a bad handle.
+  void handleBatchInfo( ncrystal_scatter_t sc, const char* fct, ncgb_material_view* view, int* device,
+                        uint64_t* seed, uint32_t* streamidx, uint32_t* callseq )
+  {
+    ScatterObj& o = extract( sc.internal, fct );
+    *view = o.mat->view;
+    *device = o.mat->device;
+    *seed = o.seed;
+    *streamidx = o.streamidx;
+    *callseq = nextCall( o );
+  }
+
+  // Routes an exception into the C interface's error state.
+  void reportError( const std::exception& e ) { handleError( e ); }
+
+  // Raises a typed error through the C interface's error state.
+  void reportError( const char* type, const std::string& msg ) { handleError( TypedError( type, msg ) ); }
+}
