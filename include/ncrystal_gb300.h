@@ -188,6 +188,14 @@ void ncgb_tables_free( void* tables );
 int ncgb_tables_array( void* tables, int comp, const char* name, const void** ptr, unsigned long* count );
 int ncgb_tables_scalar( void* tables, int comp, const char* name, double* out );
 
+/* Phase timing for benchmarks: while enabled, every scatter batch records
+ * CUDA events on its stream before and after its two kernels (the pick /
+ * cross-section pass and the S(alpha,beta) pass).  ncgb_phase_times waits for
+ * them, returns the summed milliseconds, the number of batches and the SAB
+ * queue length of this thread's last batch, and forgets them. */
+void ncgb_phase_timing( int enable );
+int ncgb_phase_times( double* ms_pick, double* ms_sab, unsigned long* nbatches, unsigned long* last_nsab );
+
 /* Bytes of device memory holding a handle's material tables. */
 unsigned long ncgb_device_bytes( ncrystal_scatter_t );
 

@@ -97,6 +97,8 @@ def lib():
         "ncgb_xs_scatter_many_f32": (None, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p,
                                             _C.c_void_p]),
         "ncgb_last_nfailed": (_C.c_ulong, []),
+        "ncgb_phase_timing": (None, [_C.c_int]),
+        "ncgb_phase_times": (_C.c_int, [_dblp, _dblp, _C.POINTER(_C.c_ulong), _C.POINTER(_C.c_ulong)]),
         "ncgb_device_bytes": (_C.c_ulong, [H]),
         "ncgb_tables_load": (_C.c_void_p, [_C.c_char_p]),
         "ncgb_tables_lasterror": (_C.c_char_p, []),
@@ -301,6 +303,21 @@ class Scatter(Process):
                                                    mu.ctypes.data)
         _check()
         return ef, mu
+
+
+def phase_timing(enable):
+    """Switch CUDA-event timing of the two scatter kernels on or off."""
+    lib().ncgb_phase_timing(1 if enable else 0)
+
+
+def phase_times():
+    """(ms in the pick pass, ms in the S(alpha,beta) pass, batches, SAB queue
+    length of the last batch) since the last call; waits for the events."""
+    a, b = _C.c_double(), _C.c_double()
+    n, q = _C.c_ulong(), _C.c_ulong()
+    if lib().ncgb_phase_times(_C.byref(a), _C.byref(b), _C.byref(n), _C.byref(q)):
+        _check()
+    return a.value, b.value, n.value, q.value
 
 
 def createScatter(cfgstr, seed=None):

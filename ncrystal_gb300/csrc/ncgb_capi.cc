@@ -836,6 +836,25 @@ void ncgb_xs_scatter_many_f32( ncrystal_scatter_t sc, const float* ekin, unsigne
 
 unsigned long ncgb_last_nfailed( void ) { return t_scratch.last_nfailed; }
 
+void ncgb_phase_timing( int enable ) { ncgb::setPhaseTiming( enable != 0 ); }
+
+int ncgb_phase_times( double* ms_pick, double* ms_sab, unsigned long* nbatches, unsigned long* last_nsab )
+{
+  try {
+    if ( ncgb::takePhaseTimes( ms_pick, ms_sab, nbatches ) )
+      throw TypedError( "CalcError", "could not read the phase timing events" );
+    *last_nsab = 0;
+    Scratch& s = t_scratch;
+    if ( s.d_work ) {
+      ncgb::Work w;
+      checkCuda( cudaMemcpy( &w, s.d_work, sizeof(w), cudaMemcpyDeviceToHost ), "D2H" );
+      *last_nsab = w.qcount;
+    }
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
 unsigned long ncgb_device_bytes( ncrystal_scatter_t sc )
 {
   try {

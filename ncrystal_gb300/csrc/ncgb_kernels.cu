@@ -18,6 +18,8 @@
 // contiguous arrays, read and written once.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <mutex>
+#include <vector>
 
 #include "ncgb_device.cuh"
 #include "ncgb_launch.hh"
@@ -232,6 +234,15 @@ namespace {
   }
 }
 
+namespace {
+  // Optional CUDA-event timing of the two phases, on the launching stream
+  // (enabled by ncgb_phase_timing; used by the benchmark's roofline).
+  struct PhaseEvents { cudaEvent_t a, b, c; };
+  bool g_timing = false;
+  std::vector<PhaseEvents> g_events;
+  std::mutex g_evmtx;
+}
+
 namespace ncgb {
 
   cudaError_t launchScatter( const ncgb_material_view& m, const Batch& b, cudaStream_t s )
@@ -241,13 +252,58 @@ namespace ncgb {
     cudaError_t e = cudaMemsetAsync( &b.work->qcount, 0, 2 * sizeof(unsigned int), s );
     if ( e != cudaSuccess )
       return e;
+    PhaseEvents ev{ nullptr, nullptr, nullptr };
+    if ( g_timing ) {
+      cudaEventCreate( &ev.a );
+      cudaEventCreate( &ev.b );
+      cudaEventCreate( &ev.c );
+      cudaEventRecord( ev.a, s );
+    }
     k_pick<<<gridFor( b.n_out, 256 ), 256, 0, s>>>( m, b );
     e = cudaGetLastError();
     if ( e != cudaSuccess )
       return e;
+    if ( g_timing )
+      cudaEventRecord( ev.b, s );
     const LaunchShape& ls = shape();
     k_sab<<<ls.nsm * ls.sab_blocks_per_sm, 256, 0, s>>>( m, b );
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    if ( g_timing ) {
+      cudaEventRecord( ev.c, s );
+      std::lock_guard<std::mutex> lock( g_evmtx );
+      g_events.push_back( ev );
+    }
+    return e;
+  }
+
+  void setPhaseTiming( bool on )
+  {
+    std::lock_guard<std::mutex> lock( g_evmtx );
+    g_timing = on;
+  }
+
+  // Sums the recorded phase times (waits for them) and forgets them.
+  int takePhaseTimes( double* ms_pick, double* ms_sab, unsigned long* nbatches )
+  {
+    std::lock_guard<std::mutex> lock( g_evmtx );
+    double tp = 0.0, ts = 0.0;
+    for ( auto& ev : g_events ) {
+      float a = 0.f, c = 0.f;
+      if ( cudaEventSynchronize( ev.c ) != cudaSuccess )
+        return 1;
+      cudaEventElapsedTime( &a, ev.a, ev.b );
+      cudaEventElapsedTime( &c, ev.b, ev.c );
+      tp += a;
+      ts += c;
+      cudaEventDestroy( ev.a );
+      cudaEventDestroy( ev.b );
+      cudaEventDestroy( ev.c );
+    }
+    *ms_pick = tp;
+    *ms_sab = ts;
+    *nbatches = static_cast<unsigned long>( g_events.size() );
+    g_events.clear();
+    return 0;
   }
 
   cudaError_t launchXS( const ncgb_material_view& m, const Batch& b, uint64_t repeat, cudaStream_t s )

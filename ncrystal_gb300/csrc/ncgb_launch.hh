@@ -45,6 +45,8 @@ namespace ncgb {
   cudaError_t launchScatter( const ncgb_material_view& m, const Batch& b, cudaStream_t s );
   cudaError_t launchXS( const ncgb_material_view& m, const Batch& b, uint64_t repeat, cudaStream_t s );
   int scatterLaunchesPerBatch();
+  void setPhaseTiming( bool on );
+  int takePhaseTimes( double* ms_pick, double* ms_sab, unsigned long* nbatches );
 }
 
 #endif
