@@ -37,14 +37,37 @@ enum ncgb_comp_type {
 };
 
 /* One beta row's alpha sampler at one energy-grid point
- * (SABSamplerAtE_Alg1::AlphaSampleInfo, NCSABSamplerModels.hh:46-56). */
+ * (SABSamplerAtE_Alg1::AlphaSampleInfo, NCSABSamplerModels.hh:46-56), plus
+ * three reciprocals the GPU uses instead of divisions. */
 typedef struct {
   double front_alpha, front_sval, front_logsval;
   double back_alpha, back_sval, back_logsval;
   double prob_front;   /* 1.0: narrow range, 2.0: zero xs (sample linearly) */
   double prob_notback; /* prob_front + prob_middle */
   uint32_t front_idx, back_idx;
+  double inv_front;    /* 1/prob_front */
+  double inv_middle;   /* 1/(prob_notback-prob_front) */
+  double inv_back;     /* 1/(1-prob_notback) */
 } ncgb_alpha_info;
+
+/* One bin [x0,x1] of a beta sampler's piecewise-linear density, with the
+ * constants of PointwiseDist::percentileWithIndex's in-bin inversion
+ * (NCPointwiseDist.cc:84-109) precomputed: a = y0, d = y1-y0, dx = x1-x0,
+ * k_e = d/(dx*a*a) (a != 0) or 2*dx/d (a == 0, d > 0) or -1, k_z = dx*a/d,
+ * inv_a = 1/a. */
+typedef struct {
+  double x0, x1, cdf0, a;
+  double k_e, k_z, inv_a, pad;
+} ncgb_beta_bin;
+
+/* One alpha cell [alpha_i, alpha_i+1] of a beta row: the constants of the
+ * log-linear in-cell inversion (NCSABUtils.hh:282-304) for the middle part of
+ * the alpha sampler: inv_bin = 1/(cumul_i+1 - cumul_i), ratio = S_i+1/S_i - 1,
+ * slope = (alpha_i+1 - alpha_i)/(logS_i+1 - logS_i); slope is NaN where the
+ * reference takes one of its degenerate branches. */
+typedef struct {
+  double inv_bin, ratio, slope, pad;
+} ncgb_alpha_cell;
 
 typedef struct {
   int64_t n;                 /* number of merged d-spacings */
@@ -88,6 +111,12 @@ typedef struct {
   const double* by;               /* normalised pdf values */
   const double* bcdf;             /* normalised cdf values */
   const ncgb_alpha_info* info;    /* [offset + j], j < nbeta-1 */
+  /* precomputed for the GPU (derived from the arrays above) */
+  double inv_kT;
+  const double* inv_dE;           /* [ne] 1/(egrid[i+1]-egrid[i]) */
+  const double* inv_dbeta;        /* [nb] 1/(beta[i+1]-beta[i]) */
+  const ncgb_beta_bin* bbin;      /* [offset + j]: bin j of a sampler, j < nbeta-1 */
+  const ncgb_alpha_cell* acell;   /* [nb*na] */
 } ncgb_sab_view;
 
 typedef struct {

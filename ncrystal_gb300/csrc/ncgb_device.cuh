@@ -199,9 +199,9 @@ namespace ncgb_dev {
     } else if ( iu == 0 ) {
       xs = ekin > 0.0 ? sqrt( ldg(s.egrid) / ekin ) * ldg(s.xs) : infd();
     } else {
-      const double el = ldg( s.egrid + iu - 1 ), eu = ldg( s.egrid + iu );
+      const double el = ldg( s.egrid + iu - 1 );
       const double xl = ldg( s.xs + iu - 1 ), xu = ldg( s.xs + iu );
-      xs = xl + ( xu - xl ) * ( ekin - el ) / ( eu - el );
+      xs = xl + ( xu - xl ) * ( ( ekin - el ) * ldg( s.inv_dE + iu - 1 ) );
     }
     return xs * s.internal_scale;
   }
@@ -319,28 +319,30 @@ namespace ncgb_dev {
 
   // ---- S(alpha,beta) sampling (Alg.1) -----------------------------------------------
 
-  // PointwiseDist::percentileWithIndex, NCPointwiseDist.cc:76-110
-  __device__ __forceinline__ double percentile( const double* x, const double* y, const double* cdf, int64_t n,
-                                                double p, int64_t& bin )
+  // PointwiseDist::percentileWithIndex, NCPointwiseDist.cc:76-110, with the
+  // in-bin constants read from the sampler's ncgb_beta_bin table instead of
+  // divided out (same formulas, a few ulps apart).
+  __device__ __forceinline__ double percentile( const double* x, const double* cdf, const ncgb_beta_bin* bins,
+                                                int64_t n, double p, int64_t& bin )
   {
     if ( p == 1.0 ) { bin = n - 2; return ldg( x + n - 1 ); }
     int64_t i = lower_bound_nn( cdf, n, p );
     if ( i > n - 1 ) i = n - 1;
     if ( i < 1 ) i = 1;
-    const double x0 = ldg( x + i - 1 ), x1 = ldg( x + i );
-    const double dx = x1 - x0;
-    const double c = ( p - ldg( cdf + i - 1 ) );
-    const double a = ldg( y + i - 1 );
-    const double d = ldg( y + i ) - a;
+    const ncgb_beta_bin* bb = bins + ( i - 1 );
+    const double x0 = ldg( &bb->x0 ), x1 = ldg( &bb->x1 );
+    const double c = p - ldg( &bb->cdf0 );
+    const double a = ldg( &bb->a );
+    const double k_e = ldg( &bb->k_e );
     double zdx;
     if ( !a ) {
-      zdx = d > 0.0 ? sqrt( ( 2.0 * c * dx ) / d ) : 0.5 * dx;
+      zdx = k_e > 0.0 ? sqrt( c * k_e ) : 0.5 * ( x1 - x0 );
     } else {
-      const double e = d * c / ( dx * a * a );
+      const double e = c * k_e;
       if ( fabs(e) > 1e-7 )
-        zdx = ( sqrt( 1.0 + 2.0 * e ) - 1.0 ) * dx * a / d;
+        zdx = ( sqrt( 1.0 + 2.0 * e ) - 1.0 ) * ldg( &bb->k_z );
       else
-        zdx = ( 1 + 0.5 * e * ( e - 1.0 ) ) * c / a;
+        zdx = ( 1 + 0.5 * e * ( e - 1.0 ) ) * c * ldg( &bb->inv_a );
     }
     bin = i - 1;
     return clampd( x0 + zdx, x0, x1 );
@@ -367,7 +369,10 @@ namespace ncgb_dev {
 
   __device__ __forceinline__ double clampRand( double r ) { return clampd( r, 2.2250738585072014e-308, 1.0 ); }
 
-  // SABSamplerAtE_Alg1::sampleAlpha, NCSABSamplerModels.cc:157-234
+  // SABSamplerAtE_Alg1::sampleAlpha, NCSABSamplerModels.cc:157-234.  The
+  // divisions by the section probabilities and bin areas are multiplications
+  // by tabulated reciprocals, and the middle part's log-linear in-cell
+  // inversion uses the cell's tabulated ratio and slope.
   __device__ __forceinline__ double sampleAlpha( const ncgb_sab_view& s, const ncgb_alpha_info* infos,
                                                  int64_t ioff, int64_t ibeta, double rp )
   {
@@ -387,14 +392,14 @@ namespace ncgb_dev {
                        rp, ldg( &info->front_logsval ), ldg( &info->back_logsval ) );
       } else {
         const uint32_t fi = __ldg( &info->front_idx );
-        const double p2 = clampRand( rp / prob_front );
+        const double p2 = clampRand( rp * ldg( &info->inv_front ) );
         return logLin( fa, ldg( &info->front_sval ), ldg( s.alpha + fi ), ldg( sab + fi ),
                        p2, ldg( &info->front_logsval ), ldg( logsab + fi ) );
       }
     }
     const double prob_notback = ldg( &info->prob_notback );
     if ( rp <= prob_notback ) {
-      const double p2 = clampd( ( rp - prob_front ) / ( prob_notback - prob_front ), 0.0, 1.0 );
+      const double p2 = clampd( ( rp - prob_front ) * ldg( &info->inv_middle ), 0.0, 1.0 );
       const int64_t il = __ldg( &info->front_idx ), iu = __ldg( &info->back_idx );
       const double cl = ldg( cumul + il ), cu = ldg( cumul + iu );
       const double sel = cl + p2 * ( cu - cl );
@@ -403,15 +408,17 @@ namespace ncgb_dev {
         return ldg( s.alpha + iu );
       if ( e <= il )
         return ldg( s.alpha + il );
-      const int64_t a0 = e - 1, a1 = e;
-      const double c0 = ldg( cumul + a0 );
-      const double binArea = ldg( cumul + a1 ) - c0;
-      const double rr = clampRand( ( sel - c0 ) / binArea );
-      return logLin( ldg( s.alpha + a0 ), ldg( sab + a0 ), ldg( s.alpha + a1 ), ldg( sab + a1 ),
-                     rr, ldg( logsab + a0 ), ldg( logsab + a1 ) );
+      const int64_t a0 = e - 1;
+      const ncgb_alpha_cell* cell = s.acell + ibeta * na + a0;
+      const double rr = clampRand( ( sel - ldg( cumul + a0 ) ) * ldg( &cell->inv_bin ) );
+      const double slope = ldg( &cell->slope );
+      if ( slope == slope )
+        return ldg( s.alpha + a0 ) + slope * log1p( rr * ldg( &cell->ratio ) );
+      return logLin( ldg( s.alpha + a0 ), ldg( sab + a0 ), ldg( s.alpha + a0 + 1 ), ldg( sab + a0 + 1 ),
+                     rr, ldg( logsab + a0 ), ldg( logsab + a0 + 1 ) );
     }
     const uint32_t bi = __ldg( &info->back_idx );
-    const double p2 = clampRand( ( rp - prob_notback ) / ( 1.0 - prob_notback ) );
+    const double p2 = clampRand( ( rp - prob_notback ) * ldg( &info->inv_back ) );
     return logLin( ldg( s.alpha + bi ), ldg( sab + bi ), ldg( &info->back_alpha ), ldg( &info->back_sval ),
                    p2, ldg( logsab + bi ), ldg( &info->back_logsval ) );
   }
@@ -465,7 +472,7 @@ namespace ncgb_dev {
     const ncgb_alpha_info* infos = s.info + off;
     const int64_t ioff = __ldg( s.smp_ibetaoffset + ie );
     int64_t ibs;
-    const double beta = percentile( bx, s.by + off, s.bcdf + off, nbs, rand01( rng ), ibs );
+    const double beta = percentile( bx, s.bcdf + off, s.bbin + off, nbs, rand01( rng ), ibs );
     const double fbkep = ldg( s.smp_fbkep + ie );
     if ( ibs == 0 && fbkep <= 0.0 )
       return alg1FirstBin( s, infos, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
@@ -477,9 +484,8 @@ namespace ncgb_dev {
       return 0; // cannot happen (beta above the beta grid front); keeps indices in bounds
     const double bl = ldg( s.beta + ibeta - 1 );
     const double alphal = sampleAlpha( s, infos, ioff, ibeta - 1, rp );
-    const double bh = ldg( s.beta + ibeta );
     const double alphah = sampleAlpha( s, infos, ioff, ibeta, rp );
-    const double alpha = alphal + ( alphah - alphal ) * ( beta - bl ) / ( bh - bl );
+    const double alpha = alphal + ( alphah - alphal ) * ( ( beta - bl ) * ldg( s.inv_dbeta + ibeta - 1 ) );
     const ALim al = alphaLimits( x, beta );
     if ( inInterval( al.lo, al.hi, alpha ) ) {
       alpha_out = alpha;
@@ -525,8 +531,8 @@ namespace ncgb_dev {
       }
       L.ie = iu;
     }
-    L.x = ekin / s.kT;
-    L.xsamp = L.ultra_small ? ldg( s.egrid ) / s.kT : L.x;
+    L.x = ekin * s.inv_kT;
+    L.xsamp = L.ultra_small ? ldg( s.egrid ) * s.inv_kT : L.x;
     return NCGB_ST_OK;
   }
 

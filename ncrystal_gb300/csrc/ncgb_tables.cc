@@ -550,7 +550,72 @@ namespace ncgb {
         s.bx = encodeOff<double>( mt->put(d.bx) );
         s.by = encodeOff<double>( mt->put(d.by) );
         s.bcdf = encodeOff<double>( mt->put(d.bcdf) );
+        // Precomputed constants for the GPU (reciprocals instead of divisions):
+        for ( auto& inf : d.info ) {
+          inf.inv_front = inf.prob_front != 0.0 ? 1.0 / inf.prob_front : 0.0;
+          const double mid = inf.prob_notback - inf.prob_front;
+          inf.inv_middle = mid != 0.0 ? 1.0 / mid : 0.0;
+          const double back = 1.0 - inf.prob_notback;
+          inf.inv_back = back != 0.0 ? 1.0 / back : 0.0;
+        }
         s.info = encodeOff<ncgb_alpha_info>( mt->put( d.info.data(), d.info.size() ) );
+        s.inv_kT = 1.0 / s.kT;
+        std::vector<double> inv_dE( in.egrid.size(), 0.0 ), inv_dbeta( in.beta.size(), 0.0 );
+        for ( std::size_t i = 0; i + 1 < in.egrid.size(); ++i )
+          inv_dE[i] = 1.0 / ( in.egrid[i+1] - in.egrid[i] );
+        for ( std::size_t i = 0; i + 1 < in.beta.size(); ++i )
+          inv_dbeta[i] = 1.0 / ( in.beta[i+1] - in.beta[i] );
+        s.inv_dE = encodeOff<double>( mt->put( inv_dE ) );
+        s.inv_dbeta = encodeOff<double>( mt->put( inv_dbeta ) );
+        std::vector<ncgb_beta_bin> bbin( d.bx.size() );
+        std::memset( bbin.data(), 0, bbin.size() * sizeof(ncgb_beta_bin) );
+        for ( std::size_t ie = 0; ie < d.kind.size(); ++ie ) {
+          if ( d.kind[ie] != 1 )
+            continue;
+          const int64_t off = d.offset[ie];
+          for ( int64_t j = 0; j + 1 < d.nbeta[ie]; ++j ) {
+            ncgb_beta_bin& bb = bbin[off + j];
+            bb.x0 = d.bx[off + j];
+            bb.x1 = d.bx[off + j + 1];
+            bb.cdf0 = d.bcdf[off + j];
+            bb.a = d.by[off + j];
+            const double dd = d.by[off + j + 1] - bb.a;
+            const double dx = bb.x1 - bb.x0;
+            if ( bb.a != 0.0 ) {
+              bb.k_e = dd / ( dx * bb.a * bb.a );
+              bb.inv_a = 1.0 / bb.a;
+            } else {
+              bb.k_e = dd > 0.0 ? 2.0 * dx / dd : -1.0;
+              bb.inv_a = 0.0;
+            }
+            bb.k_z = dd != 0.0 ? dx * bb.a / dd : 0.0;
+          }
+        }
+        s.bbin = encodeOff<ncgb_beta_bin>( mt->put( bbin.data(), bbin.size() ) );
+        const std::size_t na = in.alpha.size(), nb = in.beta.size();
+        std::vector<ncgb_alpha_cell> acell( na * nb );
+        std::memset( acell.data(), 0, acell.size() * sizeof(ncgb_alpha_cell) );
+        const double qnan = std::numeric_limits<double>::quiet_NaN();
+        for ( std::size_t ib = 0; ib < nb; ++ib ) {
+          for ( std::size_t ai = 0; ai + 1 < na; ++ai ) {
+            const std::size_t g = ib * na + ai;
+            ncgb_alpha_cell& c = acell[g];
+            const double dc = d.cumul[g+1] - d.cumul[g];
+            c.inv_bin = dc > 0.0 ? 1.0 / dc : 0.0;
+            c.slope = qnan;
+            const double fa = in.sab[g], fb = in.sab[g+1];
+            const double df = fb - fa;
+            if ( fa * fb * df != 0.0 ) {
+              const double L = d.logsab[g+1] - d.logsab[g];
+              const double a = in.alpha[ai], b = in.alpha[ai+1];
+              if ( ( a - b ) * L != 0.0 ) {
+                c.ratio = df / fa;
+                c.slope = ( b - a ) / L;
+              }
+            }
+          }
+        }
+        s.acell = encodeOff<ncgb_alpha_cell>( mt->put( acell.data(), acell.size() ) );
       } else if ( type == "FreeGas" ) {
         c.type = NCGB_COMP_FREEGAS;
         c.fg.kT = b.f64s(p+"kT");
@@ -567,6 +632,8 @@ namespace ncgb {
   }
 
   template int64_t MaterialTables::put<ncgb_alpha_info>( const ncgb_alpha_info*, std::size_t );
+  template int64_t MaterialTables::put<ncgb_beta_bin>( const ncgb_beta_bin*, std::size_t );
+  template int64_t MaterialTables::put<ncgb_alpha_cell>( const ncgb_alpha_cell*, std::size_t );
 
   ncgb_material_view MaterialTables::relocate( const void* basev ) const
   {
@@ -593,6 +660,10 @@ namespace ncgb {
       s.by = reloc( s.by, base );
       s.bcdf = reloc( s.bcdf, base );
       s.info = reloc( s.info, base );
+      s.inv_dE = reloc( s.inv_dE, base );
+      s.inv_dbeta = reloc( s.inv_dbeta, base );
+      s.bbin = reloc( s.bbin, base );
+      s.acell = reloc( s.acell, base );
     }
     return v;
   }

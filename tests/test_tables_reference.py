@@ -14,7 +14,7 @@ from oracle import pyoracle
 pytestmark = pytest.mark.skipif(not B.reference_available() or pyoracle.refpin_lib() is None,
                                 reason="needs the NCrystal sources (reference build)")
 
-INFO = np.dtype([("d", "<f8", (8,)), ("u", "<u4", (2,))])
+INFO = np.dtype([("d", "<f8", (8,)), ("u", "<u4", (2,)), ("inv", "<f8", (3,))])
 CFGS = [W.AL, W.AL2O3, W.PE293, W.WATER]
 
 
