@@ -5,17 +5,21 @@ One step = one pass of the hot path over one batch: for every neutron its
 total cross-section and one sampled isotropic scatter (E', mu).
 
 Default workload ("al2o3_large"): Al2O3_sg167_Corundum.ncmat;temp=293K;
-dcutoff=0.2 (several thousand Bragg planes, ElInc, two S(alpha,beta)
+dcutoff=0.2 (2,886 merged Bragg d-spacings, ElInc, two S(alpha,beta)
 kernels), 2^24 neutrons with energies log-uniform in [1e-4, 1] eV (seeded),
-FP32 energies in and FP32 results out, FP64 arithmetic.
+FP32 energies in and FP32 results out, FP64 arithmetic.  Other workloads:
+al_small (Al at 293 K, 2^20 neutrons, wavelengths uniform in [0.5, 5] Aa, FP64
+I/O), pe (Polyethylene at 293 K, 2^24, FP64 I/O) and crystal_batch (64
+(material, T) instances of 16 crystals at 77/150/293/400 K, ragged neutron
+counts log-uniform in [1e3, 1e6], one batch launch replayed as a CUDA graph).
 
   value  -- device-resident batch (two kernels: k_pick, k_sab), inputs
             already in HBM
   e2e    -- the same through the C ABI with host (pinned) arrays, copies
-            inside the timed region (ncgb_xs_scatter_many_f32)
+            inside the timed region
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-       [--workload al2o3_large|al_small|pe]
+       [--workload al2o3_large|al_small|pe|crystal_batch]
 Under torchrun (N>1) each rank runs an independent replica on its own GPU
 (the path has no cross-neutron exchange: replicas only) and rank 0 prints the
 JSON line with the whole-job throughput.
@@ -36,19 +40,31 @@ sys.path.insert(0, ROOT)
 
 METRIC = "neutron scatters/s on 1 GB300, learned-proposal vs plain GPU sampler (KS p>0.01)"
 UNIT = "scatters/s"
+L2_BYTES = 129 * 1024 * 1024
 
-WORKLOADS = {
-    # name: (cfg, n, energy generator, io dtype, algorithmic bytes/neutron)
-    "al2o3_large": ("Al2O3_sg167_Corundum.ncmat;temp=293K;dcutoff=0.2", 1 << 24,
-                    lambda n, k: __import__("ncrystal_gb300.workloads", fromlist=["x"]).loguniform_energies(
-                        n, 1e-4, 1.0, 0x5EED0002 + k), "f32", 16),
-    "al_small": ("Al_sg225.ncmat;temp=293K", 1 << 20,
-                 lambda n, k: __import__("ncrystal_gb300.workloads", fromlist=["x"]).al_wavelength_energies(
-                     n, 0x5EED0001 + k), "f64", 32),
-    "pe": ("Polyethylene_CH2.ncmat;temp=293K", 1 << 24,
-           lambda n, k: __import__("ncrystal_gb300.workloads", fromlist=["x"]).loguniform_energies(
-               n, 1e-4, 1.0, 0x5EED0004 + k), "f64", 32),
-}
+
+def workload(name, rank):
+    """-> dict(cfgs, counts, energies (list per material), io)."""
+    import ncrystal_gb300.workloads as W
+    if name == "al2o3_large":
+        n = 1 << 24
+        return dict(cfgs=[W.AL2O3], counts=[n], io="f32",
+                    energies=[W.loguniform_energies(n, 1e-4, 1.0, 0x5EED0002 + rank)])
+    if name == "al_small":
+        n = 1 << 20
+        return dict(cfgs=[W.AL], counts=[n], io="f64",
+                    energies=[W.al_wavelength_energies(n, 0x5EED0001 + rank)])
+    if name == "pe":
+        n = 1 << 24
+        return dict(cfgs=[W.PE293], counts=[n], io="f64",
+                    energies=[W.loguniform_energies(n, 1e-4, 1.0, 0x5EED0004 + rank)])
+    if name == "crystal_batch":
+        cfg = W.config("crystal_batch")
+        counts = [int(c) for c in cfg["counts"]]
+        return dict(cfgs=cfg["cfgs"], counts=counts, io="f64",
+                    energies=[W.loguniform_energies(c, 1e-4, 1.0, 0x5EED0003 + 1000 * rank + k)
+                              for k, c in enumerate(counts)])
+    raise KeyError(name)
 
 
 def parse():
@@ -57,7 +73,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="al2o3_large", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="al2o3_large",
+                    choices=["al2o3_large", "al_small", "pe", "crystal_batch"])
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="wall-clock budget of the CPU baseline sample")
     return ap.parse_args()
@@ -72,10 +89,10 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel, workload):
+def profiled_traffic(kernel, workload_name):
     """DRAM bytes per launch from the committed ncu summary, if any
     (profiles/<kernel>_<workload>.md, line 'dram_bytes_per_launch: X')."""
-    p = os.path.join(ROOT, "profiles", "%s_%s.md" % (kernel, workload))
+    p = os.path.join(ROOT, "profiles", "%s_%s.md" % (kernel, workload_name))
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -143,38 +160,51 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(cfg, energies, seconds, threads=None):
+def cpu_baseline(wl, seconds, threads=None):
     """The CPU oracle (a plain-C restatement of NCrystal's per-neutron
-    evaluation) timed on this host's cores on a bounded sample of the same
-    workload: cross-section + one scatter per neutron."""
+    evaluation, pinned to the reference neutron by neutron) timed on this
+    host's cores on a bounded sample of the same workload: cross-section and
+    one scatter per neutron.  For a multi-material workload the sample takes
+    the same fraction of every material's neutrons."""
     from concurrent.futures import ThreadPoolExecutor
 
     import ncrystal_gb300._build as B
     from oracle.pyoracle import HostMaterial
     threads = threads or os.cpu_count() or 1
-    m = HostMaterial(os.path.join(B.BUNDLES, B.bundle_file_name(cfg)))
-    e = np.ascontiguousarray(energies, dtype=np.float64)
+    mats = [HostMaterial(os.path.join(B.BUNDLES, B.bundle_file_name(c))) for c in wl["cfgs"]]
+    total = sum(wl["counts"])
 
-    def work(chunk, off):
+    def work(item):
+        m, chunk, off = item
         m.xs(chunk)
         m.scatter(chunk, 12345, index_offset=off)
 
-    # calibrate on a small slice, then size the sample to the time budget
+    def items(frac, parts):
+        out = []
+        for m, e in zip(mats, wl["energies"]):
+            e = np.ascontiguousarray(e[:max(1, int(len(e) * frac))], dtype=np.float64)
+            for ch in np.array_split(e, max(1, min(parts, len(e)))):
+                if len(ch):
+                    out.append((m, ch, 0))
+        return out
+
+    # calibrate on a small sample, then size the sample to the time budget
     t0 = time.perf_counter()
-    cal = e[:20000]
-    work(cal, 0)
-    rate1 = len(cal) / max(time.perf_counter() - t0, 1e-6)
-    nsample = int(min(len(e), max(threads * 20000, rate1 * threads * seconds)))
-    sample = e[:nsample]
-    chunks = np.array_split(sample, threads * 4)
-    offs = np.cumsum([0] + [len(c) for c in chunks[:-1]])
+    cal = items(min(1.0, 20000.0 / total), 1)
+    for it in cal:
+        work(it)
+    ncal = sum(len(it[1]) for it in cal)
+    rate1 = ncal / max(time.perf_counter() - t0, 1e-6)
+    frac = min(1.0, rate1 * threads * seconds / total)
+    sample = items(frac, threads)
+    nsample = sum(len(it[1]) for it in sample)
     t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as ex:
-        list(ex.map(work, chunks, offs))
+        list(ex.map(work, sample))
     dt = time.perf_counter() - t0
     return {"value": nsample / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "first %d neutrons of the workload (xs + one scatter each), %d threads, %.1f s"
-                      % (nsample, threads, dt)}
+            "sample": "%d neutrons (%.3g of each material's, xs + one scatter each), %d threads, %.1f s"
+                      % (nsample, frac, threads, dt)}
 
 
 def dist_env():
@@ -184,21 +214,27 @@ def dist_env():
     return world, rank, local
 
 
+def config_of(args, wl, world):
+    cfgs = wl["cfgs"]
+    return {"workload": args.workload, "cfg": cfgs[0] if len(cfgs) == 1 else "%d instances" % len(cfgs),
+            "neutrons_per_gpu": int(sum(wl["counts"])), "io": wl["io"], "sampler": "plain (Alg.1 tables)",
+            "parallelism": "replicas%d" % world}
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
-    cfg, n, gen, io, bpn = WORKLOADS[args.workload]
     import __graft_entry__
     __graft_entry__.build()
-    energies = gen(n, 0)
-    if io == "f32":
-        energies = energies.astype(np.float32).astype(np.float64)
+    wl = workload(args.workload, 0)
+    if wl["io"] == "f32":
+        wl["energies"] = [e.astype(np.float32).astype(np.float64) for e in wl["energies"]]
     vals = []
     base = None
     per_step = max(1.0, 60.0 / max(1, args.steps + args.warmup))
     for i in range(args.warmup + args.steps):
-        b = cpu_baseline(cfg, energies, min(per_step, args.cpu_seconds))
+        b = cpu_baseline(wl, min(per_step, args.cpu_seconds))
         if i >= args.warmup:
             vals.append(b["value"])
             base = b
@@ -206,12 +242,99 @@ def run_reference(args):
     base["value"] = v
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "cfg": cfg, "neutrons": n, "io": io},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_of(args, wl, 1),
             "impl": "reference", "cpu_baseline": base,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+class SingleRunner:
+    """One material, device arrays (ncgb_scatter_device) and host arrays
+    (ncgb_xs_scatter_many[_f32])."""
+
+    def __init__(self, NC, torch, wl, dev, seed):
+        self.torch = torch
+        self.f32 = wl["io"] == "f32"
+        self.dt = torch.float32 if self.f32 else torch.float64
+        e = wl["energies"][0].astype(np.float32 if self.f32 else np.float64)
+        self.n = len(e)
+        self.sc = NC.createScatter(wl["cfgs"][0], seed=seed)
+        self.d_e = torch.from_numpy(e).to(dev)
+        self.d_xs, self.d_ef, self.d_mu = (torch.empty_like(self.d_e) for _ in range(3))
+        self.h_e = torch.from_numpy(e).pin_memory()
+        self.h_xs, self.h_ef, self.h_mu = (torch.empty(self.n, dtype=self.dt).pin_memory() for _ in range(3))
+
+    def gate(self, stream):
+        st = self.torch.zeros(self.n, dtype=self.torch.int32, device=self.d_e.device)
+        self.sc.scatter_device(self.d_e, self.d_xs, self.d_ef, self.d_mu, st, stream=stream)
+        self.torch.cuda.synchronize()
+        return int((st != 0).sum().item())
+
+    def step(self, stream):
+        self.sc.scatter_device(self.d_e, self.d_xs, self.d_ef, self.d_mu, None, stream=stream)
+
+    timed_step = step
+
+    def e2e_step(self):
+        self.sc.xs_scatter_host_ptr(self.h_e.data_ptr(), self.n, self.h_xs.data_ptr(), self.h_ef.data_ptr(),
+                                    self.h_mu.data_ptr(), self.f32)
+
+    def e2e_info(self):
+        esz = 4 if self.f32 else 8
+        chunk = 1 << 22
+        return {"h2d_bytes_per_step": self.n * esz, "d2h_bytes_per_step": 3 * self.n * esz,
+                "gpu_launches_per_step": 2 * ((self.n + chunk - 1) // chunk),
+                "api": "ncgb_xs_scatter_many%s (C ABI, pinned host arrays)" % ("_f32" if self.f32 else "")}
+
+    def launches_per_step(self):
+        return 2
+
+
+class BatchRunner:
+    """Ragged multi-material batch: autotuned shape, CUDA-graph replay on
+    device arrays; host arrays through ncgb_batch_xs_scatter_many."""
+
+    def __init__(self, NC, torch, wl, dev, seed):
+        self.torch = torch
+        self.f32 = False
+        e = np.concatenate(wl["energies"]).astype(np.float64)
+        self.n = len(e)
+        offs = np.concatenate([[0], np.cumsum(wl["counts"])]).astype(np.int64)
+        self.batch = NC.Batch([NC.createScatter(c, seed=seed + k) for k, c in enumerate(wl["cfgs"])])
+        self.d_e = torch.from_numpy(e).to(dev)
+        self.d_off = torch.from_numpy(offs).to(dev)
+        self.d_xs, self.d_ef, self.d_mu = (torch.empty_like(self.d_e) for _ in range(3))
+        self.h_e = torch.from_numpy(e).pin_memory()
+        self.h_off = torch.from_numpy(offs).pin_memory()
+        self.h_xs, self.h_ef, self.h_mu = (torch.empty(self.n, dtype=torch.float64).pin_memory() for _ in range(3))
+        self.shape = None
+
+    def gate(self, stream):
+        self.shape = self.batch.autotune(self.d_e, self.d_off, self.d_xs, self.d_ef, self.d_mu, stream=stream)
+        st = self.torch.zeros(self.n, dtype=self.torch.int32, device=self.d_e.device)
+        self.batch.scatter_device(self.d_e, self.d_off, self.d_xs, self.d_ef, self.d_mu, st, stream=stream)
+        self.torch.cuda.synchronize()
+        return int((st != 0).sum().item())
+
+    def step(self, stream):
+        # plain launch (used for the per-kernel timing pass)
+        self.batch.scatter_device(self.d_e, self.d_off, self.d_xs, self.d_ef, self.d_mu, None, stream=stream)
+
+    def timed_step(self, stream):
+        self.batch.graph_launch(self.d_e, self.d_off, self.d_xs, self.d_ef, self.d_mu, None, stream=stream)
+
+    def e2e_step(self):
+        self.batch.xs_scatter_host_ptr(self.h_e.data_ptr(), self.h_off.data_ptr(), self.n, self.h_xs.data_ptr(),
+                                       self.h_ef.data_ptr(), self.h_mu.data_ptr())
+
+    def e2e_info(self):
+        return {"h2d_bytes_per_step": self.n * 8 + self.h_off.numel() * 8, "d2h_bytes_per_step": 3 * self.n * 8,
+                "gpu_launches_per_step": 2, "api": "ncgb_batch_xs_scatter_many (C ABI, pinned host arrays)",
+                "autotuned_shape": {"pick_block": self.shape[0], "sab_blocks_per_sm": self.shape[1]}}
+
+    def launches_per_step(self):
+        return 2
 
 
 def run_gb300(args):
@@ -230,23 +353,15 @@ def run_gb300(args):
         __graft_entry__.build()  # no-op when up to date; loads the package
     import ncrystal_gb300 as NC
 
-    cfg, n, gen, io, bpn = WORKLOADS[args.workload]
-    dt_t = torch.float32 if io == "f32" else torch.float64
-    np_t = np.float32 if io == "f32" else np.float64
-    energies = gen(n, rank).astype(np_t)
-    sc = NC.createScatter(cfg, seed=0xB0057 + rank)
+    wl = workload(args.workload, rank)
     dev = torch.device("cuda", local)
-    d_e = torch.from_numpy(energies).to(dev)
-    d_xs = torch.empty_like(d_e)
-    d_ef = torch.empty_like(d_e)
-    d_mu = torch.empty_like(d_e)
     stream = torch.cuda.current_stream(dev)
+    R = (BatchRunner if len(wl["cfgs"]) > 1 else SingleRunner)(NC, torch, wl, dev, 0xB0057 + 977 * rank)
+    n = R.n
+    esz = 4 if R.f32 else 8
+    io_bytes = 4 * esz * n  # energies in, xs / E' / mu out
 
-    # correctness gate before timing: no neutron may fail
-    d_st = torch.zeros(n, dtype=torch.int32, device=dev)
-    sc.scatter_device(d_e, d_xs, d_ef, d_mu, d_st, stream=stream)
-    torch.cuda.synchronize()
-    nbad = int((d_st != 0).sum().item())
+    nbad = R.gate(stream)   # correctness gate before timing: no neutron may fail
     if nbad:
         raise SystemExit("bench: %d neutrons failed to sample" % nbad)
 
@@ -255,22 +370,38 @@ def run_gb300(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    # Between timed steps the L2 must not hold the previous step's arrays:
+    # workloads whose I/O is smaller than twice the L2 flush it with a write
+    # of a 2xL2 buffer, outside the timed events.
+    flush = None
+    if io_bytes < 2 * L2_BYTES:
+        flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+
     for _ in range(args.warmup):
-        sc.scatter_device(d_e, d_xs, d_ef, d_mu, None, stream=stream)
+        R.timed_step(stream)
     barrier()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    NC.phase_times()          # drop anything recorded before
-    NC.phase_timing(True)     # CUDA events around each kernel, on `stream`
-    with ClockSampler(local) as clk:
-        ev0.record(stream)
-        for _ in range(args.steps):
-            sc.scatter_device(d_e, d_xs, d_ef, d_mu, None, stream=stream)
-        ev1.record(stream)
-        barrier()
+
+    # per-kernel durations (CUDA events on the launching stream, recorded by the library)
+    NC.phase_times()
+    NC.phase_timing(True)
+    for _ in range(max(2, args.steps // 4)):
+        if flush is not None:
+            flush.fill_(1.0)
+        R.step(stream)
     NC.phase_timing(False)
     ms_pick, ms_sab, nbatches, n_sab = NC.phase_times()
-    ms = ev0.elapsed_time(ev1)
+    barrier()
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        for a, b in evs:
+            if flush is not None:
+                flush.fill_(1.0)
+            a.record(stream)
+            R.timed_step(stream)
+            b.record(stream)
+        barrier()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
     if dist:
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -281,7 +412,6 @@ def run_gb300(args):
     # Algorithmic bytes per launch (inputs read + results written, nothing
     # else): k_pick reads every energy, writes every xs and the (E', mu) of the
     # neutrons it finishes; k_sab writes (E', mu) of the n_sab queued ones.
-    esz = 4 if io == "f32" else 8
     bytes_pick = n * (esz + esz) + (n - n_sab) * 2 * esz
     bytes_sab = n_sab * 2 * esz
     t_pick = ms_pick / max(1, nbatches) / 1e3
@@ -298,61 +428,47 @@ def run_gb300(args):
     achieved = kernels[dom]["achieved_gbs"]
 
     # ---- e2e: host (pinned) arrays through the C ABI, copies timed ----------
-    h_e = torch.from_numpy(energies).pin_memory()
-    h_xs = torch.empty(n, dtype=dt_t).pin_memory()
-    h_ef = torch.empty(n, dtype=dt_t).pin_memory()
-    h_mu = torch.empty(n, dtype=dt_t).pin_memory()
-    f32 = io == "f32"
-
-    def e2e_step():
-        sc.xs_scatter_host_ptr(h_e.data_ptr(), n, h_xs.data_ptr(), h_ef.data_ptr(), h_mu.data_ptr(), f32)
-
     for _ in range(max(1, args.warmup // 2)):
-        e2e_step()
+        R.e2e_step()
     barrier()
     e2e_steps = max(3, args.steps // 2)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        e2e_step()
+        R.e2e_step()
     barrier()
     e2e_s = time.perf_counter() - t0
     if dist:
         t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    esize = 4 if f32 else 8
-    chunk = 1 << 22
-    e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": n * esize, "d2h_bytes_per_step": 3 * n * esize,
-           "steps": e2e_steps, "gpu_launches_per_step": (n + chunk - 1) // chunk,
-           "api": "ncgb_xs_scatter_many%s (C ABI, pinned host arrays)" % ("_f32" if f32 else "")}
+    e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT, "steps": e2e_steps}
+    e2e.update(R.e2e_info())
 
-    # results sanity: outputs of the last step
-    mu_h = d_mu.float().cpu().numpy()
-    if not np.all(np.abs(mu_h) <= 1.0):
+    if not float(R.d_mu.abs().max().item()) <= 1.0:
         raise SystemExit("bench: mu outside [-1,1]")
 
     if rank == 0:
-        base = cpu_baseline(cfg, energies.astype(np.float64), args.cpu_seconds)
-        clocks = clk.summary()
-        traffic = profiled_traffic(dom, args.workload)
+        base = cpu_baseline(wl, args.cpu_seconds)
+        cfgd = config_of(args, wl, world)
+        cfgd["l2"] = ("flushed between timed steps (2xL2 write)" if flush is not None
+                      else "per-step I/O %d MB > 2xL2; material tables stay L2-resident" % (io_bytes >> 20))
+        cfgd["inputs"] = "device-resident, not re-read from host"
+        if len(wl["cfgs"]) > 1:
+            cfgd["timed_launch"] = "CUDA graph replay of the autotuned batch launch"
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "cfg": cfg, "neutrons_per_gpu": n, "io": io,
-                       "sampler": "plain (Alg.1 tables)", "parallelism": "replicas%d" % world,
-                       "l2": "per-step I/O %d MB > L2 (129 MB); material tables stay L2-resident" % (bpn * n >> 20),
-                       "inputs": "device-resident, not re-read from host"},
+            "config": cfgd,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": traffic, "kernel": dom, "kernels": kernels,
-                         "step_bytes_per_neutron": bpn,
+                         "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
+                         "traffic": profiled_traffic(dom, args.workload), "kernel": dom, "kernels": kernels,
+                         "step_bytes_per_neutron": 4 * esz,
                          "note": "FP64-pipe bound, not HBM bound: see profiles/"},
             "cpu_baseline": base,
             "e2e": e2e,
-            "clocks": clocks,
-            "gpu_launches": args.steps * 2,
+            "clocks": clk.summary(),
+            "gpu_launches": args.steps * R.launches_per_step(),
         }
         print(json.dumps(line), flush=True)
     if dist:

@@ -188,6 +188,34 @@ void ncgb_tables_free( void* tables );
 int ncgb_tables_array( void* tables, int comp, const char* name, const void** ptr, unsigned long* count );
 int ncgb_tables_scalar( void* tables, int comp, const char* name, double* out );
 
+/* Ragged multi-material batches (no reference counterpart): one launch pair
+ * for neutrons of many materials.  d_offsets[nmat+1] (int64, device memory,
+ * ascending, d_offsets[0] = 0, d_offsets[nmat] = n) gives each material's
+ * neutrons [d_offsets[k], d_offsets[k+1]); neutron o of material k draws from
+ * stream (seed_k, o - d_offsets[k], batch call sequence, clone index_k), so
+ * a batch reproduces the single-material calls of fresh handles.  The
+ * handles must live on one device and outlive nothing: the batch keeps their
+ * tables alive itself. */
+typedef struct { void * internal; } ncgb_batch_t;
+ncgb_batch_t ncgb_batch_create( const ncrystal_scatter_t* scatters, unsigned long nmat );
+void ncgb_batch_destroy( ncgb_batch_t* );
+int ncgb_batch_scatter_device( ncgb_batch_t, const double* d_ekin, const int64_t* d_offsets, unsigned long n,
+                               double* d_xs, double* d_ekin_final, double* d_mu, int32_t* d_status,
+                               void* stream );
+/* Times the launch shapes (pick block 128/256/512 x S(alpha,beta) blocks per
+ * SM) on this batch's arrays and keeps the fastest for the batch. */
+int ncgb_batch_autotune( ncgb_batch_t, const double* d_ekin, const int64_t* d_offsets, unsigned long n,
+                         double* d_xs, double* d_ekin_final, double* d_mu, void* stream );
+int ncgb_batch_config( ncgb_batch_t, int* pick_block, int* sab_blocks_per_sm );
+/* Same as ncgb_batch_scatter_device, replayed as a CUDA graph (captured on
+ * first use, updated in place afterwards). */
+int ncgb_batch_graph_launch( ncgb_batch_t, const double* d_ekin, const int64_t* d_offsets, unsigned long n,
+                             double* d_xs, double* d_ekin_final, double* d_mu, int32_t* d_status,
+                             void* stream );
+/* Host arrays: copies in, runs and copies out (synchronous). */
+void ncgb_batch_xs_scatter_many( ncgb_batch_t, const double* ekin, const int64_t* offsets, unsigned long n,
+                                 double* xs, double* ekin_final, double* mu );
+
 /* Phase timing for benchmarks: while enabled, every scatter batch records
  * CUDA events on its stream before and after its two kernels (the pick /
  * cross-section pass and the S(alpha,beta) pass).  ncgb_phase_times waits for

@@ -97,6 +97,17 @@ def lib():
         "ncgb_xs_scatter_many_f32": (None, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p,
                                             _C.c_void_p]),
         "ncgb_last_nfailed": (_C.c_ulong, []),
+        "ncgb_batch_create": (_Handle, [_C.POINTER(_Handle), _C.c_ulong]),
+        "ncgb_batch_destroy": (None, [_C.c_void_p]),
+        "ncgb_batch_scatter_device": (_C.c_int, [_Handle, _C.c_void_p, _C.c_void_p, _C.c_ulong, _C.c_void_p,
+                                                 _C.c_void_p, _C.c_void_p, _C.c_void_p, _C.c_void_p]),
+        "ncgb_batch_graph_launch": (_C.c_int, [_Handle, _C.c_void_p, _C.c_void_p, _C.c_ulong, _C.c_void_p,
+                                               _C.c_void_p, _C.c_void_p, _C.c_void_p, _C.c_void_p]),
+        "ncgb_batch_autotune": (_C.c_int, [_Handle, _C.c_void_p, _C.c_void_p, _C.c_ulong, _C.c_void_p,
+                                           _C.c_void_p, _C.c_void_p, _C.c_void_p]),
+        "ncgb_batch_config": (_C.c_int, [_Handle, _C.POINTER(_C.c_int), _C.POINTER(_C.c_int)]),
+        "ncgb_batch_xs_scatter_many": (None, [_Handle, _C.c_void_p, _C.c_void_p, _C.c_ulong, _C.c_void_p,
+                                              _C.c_void_p, _C.c_void_p]),
         "ncgb_phase_timing": (None, [_C.c_int]),
         "ncgb_phase_times": (_C.c_int, [_dblp, _dblp, _C.POINTER(_C.c_ulong), _C.POINTER(_C.c_ulong)]),
         "ncgb_device_bytes": (_C.c_ulong, [H]),
@@ -303,6 +314,70 @@ class Scatter(Process):
                                                    mu.ctypes.data)
         _check()
         return ef, mu
+
+
+class Batch:
+    """A ragged multi-material batch (ncgb_batch_*): neutrons [offsets[k],
+    offsets[k+1]) belong to scatters[k].  Device entry points take torch CUDA
+    tensors (ekin float64, offsets int64)."""
+
+    def __init__(self, scatters):
+        L = lib()
+        self._scatters = list(scatters)   # keep the handles alive
+        arr = (_Handle * len(self._scatters))(*[sc._h for sc in self._scatters])
+        self._h = L.ncgb_batch_create(arr, len(self._scatters))
+        _check()
+        if not self._h.internal:
+            raise NCException("could not create the batch")
+
+    def __del__(self):
+        try:
+            if self._h is not None and self._h.internal:
+                lib().ncgb_batch_destroy(_C.byref(self._h))
+        except Exception:
+            pass
+
+    @property
+    def nmat(self):
+        return len(self._scatters)
+
+    def _args(self, ekin, offsets, xs, ef, mu, status, stream):
+        import torch
+        p = (lambda t: 0 if t is None else t.data_ptr())
+        if stream is None:
+            stream = torch.cuda.current_stream(ekin.device)
+        return (self._h, ekin.data_ptr(), offsets.data_ptr(), ekin.numel(), p(xs), p(ef), p(mu), p(status),
+                stream.cuda_stream)
+
+    def scatter_device(self, ekin, offsets, xs=None, ekin_final=None, mu=None, status=None, stream=None):
+        if lib().ncgb_batch_scatter_device(*self._args(ekin, offsets, xs, ekin_final, mu, status, stream)):
+            _check()
+
+    def graph_launch(self, ekin, offsets, xs=None, ekin_final=None, mu=None, status=None, stream=None):
+        if lib().ncgb_batch_graph_launch(*self._args(ekin, offsets, xs, ekin_final, mu, status, stream)):
+            _check()
+
+    def autotune(self, ekin, offsets, xs, ekin_final, mu, stream=None):
+        a = self._args(ekin, offsets, xs, ekin_final, mu, None, stream)
+        if lib().ncgb_batch_autotune(*(a[:7] + a[8:])):
+            _check()
+        pb, sb = _C.c_int(), _C.c_int()
+        lib().ncgb_batch_config(self._h, _C.byref(pb), _C.byref(sb))
+        return pb.value, sb.value
+
+    def xs_scatter_host(self, ekin, offsets):
+        e = _np.ascontiguousarray(ekin, dtype=_np.float64)
+        off = _np.ascontiguousarray(offsets, dtype=_np.int64)
+        n = len(e)
+        xs, ef, mu = (_np.empty(n) for _ in range(3))
+        lib().ncgb_batch_xs_scatter_many(self._h, e.ctypes.data, off.ctypes.data, n, xs.ctypes.data,
+                                         ef.ctypes.data, mu.ctypes.data)
+        _check()
+        return xs, ef, mu
+
+    def xs_scatter_host_ptr(self, ekin_ptr, offsets_ptr, n, xs_ptr, ef_ptr, mu_ptr):
+        lib().ncgb_batch_xs_scatter_many(self._h, ekin_ptr, offsets_ptr, n, xs_ptr, ef_ptr, mu_ptr)
+        _check()
 
 
 def phase_timing(enable):

@@ -887,3 +887,266 @@ namespace ncgb {
   // Raises a typed error through the C interface's error state.
   void reportError( const char* type, const std::string& msg ) { handleError( TypedError( type, msg ) ); }
 }
+
+// ---- ragged multi-material batches ---------------------------------------------------
+namespace {
+
+  constexpr uint32_t kBatchTypeID = 0x6e636262; // "ncbb"
+
+  struct BatchObj {
+    uint32_t typeid_ = kBatchTypeID;
+    int device = -1;
+    std::vector<std::shared_ptr<DeviceMaterial>> mats;   // keeps the tables alive
+    ncgb::MatSlot* d_slots = nullptr;
+    int nmat = 0;
+    ncgb::LaunchCfg cfg;
+    bool tuned = false;
+    std::atomic<uint32_t> callseq{0};
+    // CUDA graph of (counter reset, k_pick, k_sab) for one set of arrays
+    cudaGraphExec_t exec = nullptr;
+    const void* g_key[6] = {};
+    unsigned long g_n = 0;
+    ~BatchObj()
+    {
+      if ( exec ) cudaGraphExecDestroy( exec );
+      if ( d_slots ) cudaFree( d_slots );
+    }
+  };
+
+  BatchObj& extractBatch( void* internal, const char* fct )
+  {
+    auto b = static_cast<BatchObj*>( internal );
+    if ( !b || b->typeid_ != kBatchTypeID )
+      throw TypedError( "LogicError", std::string("Invalid batch handle passed to ") + fct );
+    return *b;
+  }
+
+  ncgb::Batch multiBatch( BatchObj& bo, Scratch& s, const double* d_ekin, unsigned long n,
+                          double* d_xs, double* d_ef, double* d_mu, int32_t* d_status )
+  {
+    ncgb::Batch b;
+    std::memset( &b, 0, sizeof(b) );
+    b.ekin = d_ekin;
+    b.n_ekin = b.n_out = n;
+    b.callseq = bo.callseq.fetch_add( 1, std::memory_order_relaxed );
+    b.out_xs = d_xs;
+    b.out_a = d_ef;
+    b.out_b = d_mu;
+    b.status = d_status;
+    b.work = s.d_work;
+    ensure( s.d_queue, s.cap_queue, n * sizeof(ncgb::QEntry) );
+    b.queue = static_cast<ncgb::QEntry*>( s.d_queue );
+    return b;
+  }
+}
+
+extern "C" {
+
+ncgb_batch_t ncgb_batch_create( const ncrystal_scatter_t* scatters, unsigned long nmat )
+{
+  try {
+    if ( !scatters || nmat == 0 || nmat > 65535 )
+      throw TypedError( "BadInput", "ncgb_batch_create: need between 1 and 65535 materials" );
+    std::unique_ptr<BatchObj> bo( new BatchObj );
+    std::vector<ncgb::MatSlot> slots( nmat );
+    for ( unsigned long k = 0; k < nmat; ++k ) {
+      ScatterObj& o = extract( scatters[k].internal, "ncgb_batch_create" );
+      if ( k == 0 )
+        bo->device = o.mat->device;
+      else if ( o.mat->device != bo->device )
+        throw TypedError( "BadInput", "ncgb_batch_create: materials live on different devices" );
+      bo->mats.push_back( o.mat );
+      std::memset( &slots[k], 0, sizeof(ncgb::MatSlot) );
+      slots[k].view = o.mat->view;
+      slots[k].seed = o.seed;
+      slots[k].stream = o.streamidx;
+    }
+    Scratch& s = scratchFor( *bo->mats.front() );
+    (void)s;
+    void* p = nullptr;
+    checkCuda( cudaMalloc( &p, nmat * sizeof(ncgb::MatSlot) ), "cudaMalloc (batch materials)" );
+    bo->d_slots = static_cast<ncgb::MatSlot*>( p );
+    checkCuda( cudaMemcpy( p, slots.data(), nmat * sizeof(ncgb::MatSlot), cudaMemcpyHostToDevice ),
+               "cudaMemcpy (batch materials)" );
+    bo->nmat = static_cast<int>( nmat );
+    return ncgb_batch_t{ bo.release() };
+  } NCGB_CATCH;
+  return ncgb_batch_t{ nullptr };
+}
+
+void ncgb_batch_destroy( ncgb_batch_t* b )
+{
+  try {
+    if ( !b || !b->internal )
+      return;
+    BatchObj& bo = extractBatch( b->internal, "ncgb_batch_destroy" );
+    cudaDeviceSynchronize();
+    delete &bo;
+    b->internal = nullptr;
+  } NCGB_CATCH;
+}
+
+int ncgb_batch_scatter_device( ncgb_batch_t bt, const double* d_ekin, const int64_t* d_offsets,
+                               unsigned long n, double* d_xs, double* d_ef, double* d_mu,
+                               int32_t* d_status, void* stream )
+{
+  try {
+    BatchObj& bo = extractBatch( bt.internal, "ncgb_batch_scatter_device" );
+    checkSize( n, 1 );
+    if ( n == 0 )
+      return 0;
+    Scratch& s = scratchFor( *bo.mats.front() );
+    cudaStream_t st = static_cast<cudaStream_t>( stream );
+    ncgb::Batch b = multiBatch( bo, s, d_ekin, n, d_xs, d_ef, d_mu, d_status );
+    checkCuda( cudaStreamWaitEvent( st, s.done, 0 ), "cudaStreamWaitEvent" );
+    checkCuda( ncgb::launchScatterMulti( bo.d_slots, d_offsets, bo.nmat, b, bo.cfg, st ), "batch kernels" );
+    checkCuda( cudaEventRecord( s.done, st ), "cudaEventRecord" );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_batch_autotune( ncgb_batch_t bt, const double* d_ekin, const int64_t* d_offsets, unsigned long n,
+                         double* d_xs, double* d_ef, double* d_mu, void* stream )
+{
+  try {
+    BatchObj& bo = extractBatch( bt.internal, "ncgb_batch_autotune" );
+    checkSize( n, 1 );
+    if ( n == 0 )
+      return 0;
+    Scratch& s = scratchFor( *bo.mats.front() );
+    cudaStream_t st = static_cast<cudaStream_t>( stream );
+    checkCuda( cudaStreamWaitEvent( st, s.done, 0 ), "cudaStreamWaitEvent" );
+    const int maxb = ncgb::maxSabBlocksPerSM();
+    std::vector<ncgb::LaunchCfg> cands;
+    for ( int pb : { 128, 256, 512 } )
+      for ( int sb : { maxb, std::max( 1, maxb / 2 ) } ) {
+        ncgb::LaunchCfg c;
+        c.pick_block = pb;
+        c.sab_blocks_per_sm = sb;
+        cands.push_back( c );
+      }
+    cudaEvent_t e0, e1;
+    checkCuda( cudaEventCreate( &e0 ), "event" );
+    checkCuda( cudaEventCreate( &e1 ), "event" );
+    float best = -1.f;
+    ncgb::LaunchCfg bestc;
+    for ( auto& c : cands ) {
+      for ( int rep = 0; rep < 2; ++rep ) { // first run warms up, second is timed
+        ncgb::Batch b = multiBatch( bo, s, d_ekin, n, d_xs, d_ef, d_mu, nullptr );
+        checkCuda( cudaEventRecord( e0, st ), "event" );
+        checkCuda( ncgb::launchScatterMulti( bo.d_slots, d_offsets, bo.nmat, b, c, st ), "batch kernels" );
+        checkCuda( cudaEventRecord( e1, st ), "event" );
+      }
+      checkCuda( cudaEventSynchronize( e1 ), "autotune" );
+      float ms = 0.f;
+      cudaEventElapsedTime( &ms, e0, e1 );
+      if ( best < 0.f || ms < best ) { best = ms; bestc = c; }
+    }
+    cudaEventDestroy( e0 );
+    cudaEventDestroy( e1 );
+    checkCuda( cudaEventRecord( s.done, st ), "cudaEventRecord" );
+    bo.cfg = bestc;
+    bo.tuned = true;
+    if ( bo.exec ) { cudaGraphExecDestroy( bo.exec ); bo.exec = nullptr; }
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_batch_config( ncgb_batch_t bt, int* pick_block, int* sab_blocks_per_sm )
+{
+  try {
+    BatchObj& bo = extractBatch( bt.internal, "ncgb_batch_config" );
+    *pick_block = bo.cfg.pick_block;
+    *sab_blocks_per_sm = bo.cfg.sab_blocks_per_sm > 0 ? bo.cfg.sab_blocks_per_sm : ncgb::maxSabBlocksPerSM();
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_batch_graph_launch( ncgb_batch_t bt, const double* d_ekin, const int64_t* d_offsets, unsigned long n,
+                             double* d_xs, double* d_ef, double* d_mu, int32_t* d_status, void* stream )
+{
+  try {
+    BatchObj& bo = extractBatch( bt.internal, "ncgb_batch_graph_launch" );
+    checkSize( n, 1 );
+    if ( n == 0 )
+      return 0;
+    Scratch& s = scratchFor( *bo.mats.front() );
+    cudaStream_t st = static_cast<cudaStream_t>( stream );
+    // Capture this launch's nodes on a private stream; instantiate once, and
+    // update the instantiated graph in place on later calls (the call
+    // sequence number, a kernel parameter, changes every call).
+    ncgb::Batch b = multiBatch( bo, s, d_ekin, n, d_xs, d_ef, d_mu, d_status );
+    static thread_local cudaStream_t cap = nullptr;
+    if ( !cap )
+      checkCuda( cudaStreamCreateWithFlags( &cap, cudaStreamNonBlocking ), "cudaStreamCreate" );
+    cudaGraph_t g = nullptr;
+    checkCuda( cudaStreamBeginCapture( cap, cudaStreamCaptureModeThreadLocal ), "cudaStreamBeginCapture" );
+    cudaError_t le = ncgb::launchScatterMulti( bo.d_slots, d_offsets, bo.nmat, b, bo.cfg, cap );
+    cudaError_t ce = cudaStreamEndCapture( cap, &g );
+    checkCuda( le, "batch kernels (capture)" );
+    checkCuda( ce, "cudaStreamEndCapture" );
+    bool fresh = true;
+    if ( bo.exec ) {
+      cudaGraphExecUpdateResultInfo info;
+      if ( cudaGraphExecUpdate( bo.exec, g, &info ) == cudaSuccess )
+        fresh = false;
+      else {
+        cudaGetLastError();
+        cudaGraphExecDestroy( bo.exec );
+        bo.exec = nullptr;
+      }
+    }
+    if ( fresh )
+      checkCuda( cudaGraphInstantiate( &bo.exec, g, 0 ), "cudaGraphInstantiate" );
+    cudaGraphDestroy( g );
+    checkCuda( cudaStreamWaitEvent( st, s.done, 0 ), "cudaStreamWaitEvent" );
+    checkCuda( cudaGraphLaunch( bo.exec, st ), "cudaGraphLaunch" );
+    checkCuda( cudaEventRecord( s.done, st ), "cudaEventRecord" );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+void ncgb_batch_xs_scatter_many( ncgb_batch_t bt, const double* ekin, const int64_t* offsets, unsigned long n,
+                                 double* xs, double* ef, double* mu )
+{
+  try {
+    BatchObj& bo = extractBatch( bt.internal, "ncgb_batch_xs_scatter_many" );
+    checkSize( n, 1 );
+    if ( n == 0 )
+      return;
+    Scratch& s = scratchFor( *bo.mats.front() );
+    ensure( s.d_in, s.cap_in, n * sizeof(double) );
+    ensure( s.d_a, s.cap_a, n * sizeof(double) );
+    ensure( s.d_b, s.cap_b, n * sizeof(double) );
+    ensure( s.d_c, s.cap_c, std::max<std::size_t>( n * sizeof(double), ( bo.nmat + 1 ) * sizeof(int64_t) ) );
+    void* d_off = nullptr;
+    std::size_t offbytes = ( bo.nmat + 1 ) * sizeof(int64_t);
+    // offsets live at the end of the 'c' buffer (after the mu outputs)
+    ensure( s.d_c, s.cap_c, n * sizeof(double) + offbytes + 256 );
+    d_off = static_cast<char*>( s.d_c ) + ( ( n * sizeof(double) + 255 ) & ~std::size_t(255) );
+    resetNFail( s, s.stream );
+    checkCuda( cudaMemcpyAsync( s.d_in, ekin, n * sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
+    checkCuda( cudaMemcpyAsync( d_off, offsets, offbytes, cudaMemcpyHostToDevice, s.stream ), "H2D" );
+    ncgb::Batch b = multiBatch( bo, s, static_cast<const double*>( s.d_in ), n,
+                                xs ? static_cast<double*>( s.d_a ) : nullptr,
+                                ef ? static_cast<double*>( s.d_b ) : nullptr,
+                                mu ? static_cast<double*>( s.d_c ) : nullptr, nullptr );
+    checkCuda( ncgb::launchScatterMulti( bo.d_slots, static_cast<const int64_t*>( d_off ), bo.nmat, b, bo.cfg,
+                                         s.stream ), "batch kernels" );
+    if ( xs ) checkCuda( cudaMemcpyAsync( xs, s.d_a, n * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    if ( ef ) checkCuda( cudaMemcpyAsync( ef, s.d_b, n * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    if ( mu ) checkCuda( cudaMemcpyAsync( mu, s.d_c, n * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    checkCuda( cudaEventRecord( s.done, s.stream ), "cudaEventRecord" );
+    const unsigned long bad = readNFail( s, s.stream );
+    if ( bad )
+      throwSamplingFailure( bad );
+    return;
+  } NCGB_CATCH;
+  fillSentinels<double>( n, xs, ef, mu );
+}
+
+}

@@ -12,10 +12,16 @@
 //            so warps stay full while neutrons need different numbers of
 //            attempts.
 //
-// The material's flat table view (~5 KB) is a __grid_constant__ kernel
-// parameter: its scalars sit in the constant bank and warps read them with
-// broadcast loads; the tables stay in HBM / L2.  Inputs and outputs are
-// contiguous arrays, read and written once.
+// Both are templated on where the material comes from:
+//   SingleSrc  one material; its flat table view (~5 KB) is a
+//              __grid_constant__ parameter, so its scalars sit in the constant
+//              bank and warps read them with broadcast loads.
+//   MultiSrc   a ragged batch of materials: a device array of views (with each
+//              material's seed and stream index) and the offsets of each
+//              material's neutrons; a neutron finds its material by a binary
+//              search over the offsets.
+// The tables themselves stay in HBM / L2.  Inputs and outputs are contiguous
+// arrays, read and written once.
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <mutex>
@@ -27,6 +33,40 @@
 namespace {
 
   using namespace ncgb_dev;
+
+  struct SingleSrc {
+    ncgb_material_view m;
+    uint64_t seed;
+    uint32_t stream, index_offset;
+    __device__ __forceinline__ int find( uint64_t ) const { return 0; }
+    __device__ __forceinline__ const ncgb_material_view& mat( int ) const { return m; }
+    __device__ __forceinline__ void rngFor( ncgb_rng& r, int, uint64_t o, uint32_t callseq ) const
+    {
+      ncgb_rng_init( &r, seed, (uint32_t)o + index_offset, callseq, stream );
+    }
+  };
+
+  struct MultiSrc {
+    const ncgb::MatSlot* slots;
+    const int64_t* offsets;   // [nmat+1]
+    int nmat;
+    __device__ __forceinline__ int find( uint64_t o ) const
+    {
+      // last k with offsets[k] <= o
+      int lo = 0, hi = nmat - 1;
+      while ( lo < hi ) {
+        const int mid = ( lo + hi + 1 ) >> 1;
+        if ( __ldg( offsets + mid ) <= (int64_t)o ) lo = mid; else hi = mid - 1;
+      }
+      return lo;
+    }
+    __device__ __forceinline__ const ncgb_material_view& mat( int k ) const { return slots[k].view; }
+    __device__ __forceinline__ void rngFor( ncgb_rng& r, int k, uint64_t o, uint32_t callseq ) const
+    {
+      const uint64_t local = o - (uint64_t)__ldg( offsets + k );
+      ncgb_rng_init( &r, slots[k].seed, (uint32_t)local, callseq, slots[k].stream );
+    }
+  };
 
   __device__ __forceinline__ double loadE( const ncgb::Batch& b, uint64_t i )
   {
@@ -63,15 +103,18 @@ namespace {
   }
 
   // ---- phase 1: cross-section, pick, short samplers, SAB queue ----------------
-  __global__ void __launch_bounds__(256)
-  k_pick( const __grid_constant__ ncgb_material_view m, const ncgb::Batch b )
+  template<class Src>
+  __global__ void __launch_bounds__(512)
+  k_pick( const __grid_constant__ Src src, const ncgb::Batch b )
   {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for ( uint64_t o = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; o < b.n_out; o += stride ) {
       const uint64_t i = ( b.n_out == b.n_ekin ) ? o : o % b.n_ekin;
       const double e = loadE( b, i );
+      const int k = src.find( o );
+      const ncgb_material_view& m = src.mat( k );
       ncgb_rng rng;
-      ncgb_rng_init( &rng, b.seed, (uint32_t)o + b.index_offset, b.callseq, b.stream );
+      src.rngFor( rng, k, o, b.callseq );
       bool queue = false;
       int qcomp = 0;
       if ( !contains( m.dom_elow, m.dom_ehigh, e ) ) {
@@ -126,8 +169,9 @@ namespace {
           ncgb::QEntry q;
           q.ekin = e;
           q.idx = (uint32_t)o;
-          q.comp = (uint16_t)qcomp;
-          q.ndraws = (uint16_t)( 2 * rng.block - rng.have );
+          q.mat = (uint16_t)k;
+          q.comp = (uint8_t)qcomp;
+          q.ndraws = (uint8_t)( 2 * rng.block - rng.have );
           b.queue[pos] = q;
         }
       }
@@ -135,15 +179,16 @@ namespace {
   }
 
   // ---- phase 2: persistent S(alpha,beta) sampling ---------------------------
+  template<class Src>
   __global__ void __launch_bounds__(256)
-  k_sab( const __grid_constant__ ncgb_material_view m, const ncgb::Batch b )
+  k_sab( const __grid_constant__ Src src, const ncgb::Batch b )
   {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned qcount = *(volatile unsigned*)&b.work->qcount;
     bool has = false, done = false;
     ncgb::QEntry q;
-    q.ekin = 0.0; q.idx = 0; q.comp = 0; q.ndraws = 0;
+    q.ekin = 0.0; q.idx = 0; q.mat = 0; q.comp = 0; q.ndraws = 0;
     SABLane L;
     ncgb_rng rng;
     ncgb_rng_init( &rng, 0, 0, 0, 0 );
@@ -161,10 +206,10 @@ namespace {
           const unsigned slot = base + __popc( need & ( ( 1u << lane ) - 1u ) );
           if ( slot < qcount ) {
             q = b.queue[slot];
-            ncgb_rng_init( &rng, b.seed, q.idx + b.index_offset, b.callseq, b.stream );
+            src.rngFor( rng, q.mat, q.idx, b.callseq );
             for ( int k = 0; k < q.ndraws; ++k )
               rand01( rng );
-            const int st = sabBegin( m.comp[q.comp].sab, q.ekin, L );
+            const int st = sabBegin( src.mat( q.mat ).comp[q.comp].sab, q.ekin, L );
             if ( st != NCGB_ST_OK )
               writeScatter( b, q.idx, q.ekin, st, q.ekin, 1.0 );
             else
@@ -178,7 +223,7 @@ namespace {
         break;
       if ( has ) {
         double ef = 0.0, mu = 0.0;
-        const int st = sabStep( m.comp[q.comp].sab, L, rng, ef, mu );
+        const int st = sabStep( src.mat( q.mat ).comp[q.comp].sab, L, rng, ef, mu );
         if ( st >= 0 ) {
           writeScatter( b, q.idx, q.ekin, st, ef, mu );
           has = false;
@@ -207,45 +252,47 @@ namespace {
     }
   }
 
-  struct LaunchShape { int nsm = 0; int sab_blocks_per_sm = 0; };
-
-  const LaunchShape& shape()
+  int numSMs()
   {
-    static LaunchShape s;
-    if ( !s.nsm ) {
+    static int nsm = 0;
+    if ( !nsm ) {
       int dev = 0;
       cudaGetDevice( &dev );
-      cudaDeviceGetAttribute( &s.nsm, cudaDevAttrMultiProcessorCount, dev );
-      if ( s.nsm <= 0 ) s.nsm = 1;
-      int bps = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_sab, 256, 0 );
-      s.sab_blocks_per_sm = bps > 0 ? bps : 1;
+      cudaDeviceGetAttribute( &nsm, cudaDevAttrMultiProcessorCount, dev );
+      if ( nsm <= 0 ) nsm = 1;
     }
-    return s;
+    return nsm;
+  }
+
+  template<class Src>
+  int sabBlocksPerSM()
+  {
+    static int bps = 0;
+    if ( !bps ) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_sab<Src>, 256, 0 );
+      if ( bps <= 0 ) bps = 1;
+    }
+    return bps;
   }
 
   int gridFor( uint64_t n, int block )
   {
     uint64_t want = ( n + block - 1 ) / block;
-    uint64_t cap = (uint64_t)shape().nsm * 32; // grid-stride beyond this
+    uint64_t cap = (uint64_t)numSMs() * ( 8192 / block ); // grid-stride beyond this
     if ( want > cap ) want = cap;
     if ( want < 1 ) want = 1;
     return (int)want;
   }
-}
 
-namespace {
   // Optional CUDA-event timing of the two phases, on the launching stream
   // (enabled by ncgb_phase_timing; used by the benchmark's roofline).
   struct PhaseEvents { cudaEvent_t a, b, c; };
   bool g_timing = false;
   std::vector<PhaseEvents> g_events;
   std::mutex g_evmtx;
-}
 
-namespace ncgb {
-
-  cudaError_t launchScatter( const ncgb_material_view& m, const Batch& b, cudaStream_t s )
+  template<class Src>
+  cudaError_t launchBoth( const Src& src, const ncgb::Batch& b, const ncgb::LaunchCfg& cfg, cudaStream_t s )
   {
     if ( b.n_out == 0 )
       return cudaSuccess;
@@ -253,28 +300,66 @@ namespace ncgb {
     if ( e != cudaSuccess )
       return e;
     PhaseEvents ev{ nullptr, nullptr, nullptr };
-    if ( g_timing ) {
+    const bool timing = g_timing;
+    if ( timing ) {
       cudaEventCreate( &ev.a );
       cudaEventCreate( &ev.b );
       cudaEventCreate( &ev.c );
       cudaEventRecord( ev.a, s );
     }
-    k_pick<<<gridFor( b.n_out, 256 ), 256, 0, s>>>( m, b );
+    const int pb = ( cfg.pick_block == 128 || cfg.pick_block == 512 ) ? cfg.pick_block : 256;
+    k_pick<Src><<<gridFor( b.n_out, pb ), pb, 0, s>>>( src, b );
     e = cudaGetLastError();
     if ( e != cudaSuccess )
       return e;
-    if ( g_timing )
+    if ( timing )
       cudaEventRecord( ev.b, s );
-    const LaunchShape& ls = shape();
-    k_sab<<<ls.nsm * ls.sab_blocks_per_sm, 256, 0, s>>>( m, b );
+    const int maxb = sabBlocksPerSM<Src>();
+    const int mult = ( cfg.sab_blocks_per_sm > 0 && cfg.sab_blocks_per_sm < maxb ) ? cfg.sab_blocks_per_sm : maxb;
+    k_sab<Src><<<numSMs() * mult, 256, 0, s>>>( src, b );
     e = cudaGetLastError();
-    if ( g_timing ) {
+    if ( timing ) {
       cudaEventRecord( ev.c, s );
       std::lock_guard<std::mutex> lock( g_evmtx );
       g_events.push_back( ev );
     }
     return e;
   }
+}
+
+namespace ncgb {
+
+  cudaError_t launchScatter( const ncgb_material_view& m, const Batch& b, cudaStream_t s )
+  {
+    SingleSrc src;
+    src.m = m;
+    src.seed = b.seed;
+    src.stream = b.stream;
+    src.index_offset = b.index_offset;
+    return launchBoth( src, b, LaunchCfg(), s );
+  }
+
+  cudaError_t launchScatterMulti( const MatSlot* d_slots, const int64_t* d_offsets, int nmat,
+                                  const Batch& b, const LaunchCfg& cfg, cudaStream_t s )
+  {
+    MultiSrc src;
+    src.slots = d_slots;
+    src.offsets = d_offsets;
+    src.nmat = nmat;
+    return launchBoth( src, b, cfg, s );
+  }
+
+  int maxSabBlocksPerSM() { return sabBlocksPerSM<MultiSrc>(); }
+
+  cudaError_t launchXS( const ncgb_material_view& m, const Batch& b, uint64_t repeat, cudaStream_t s )
+  {
+    if ( b.n_ekin == 0 || repeat == 0 )
+      return cudaSuccess;
+    k_xs<<<gridFor( b.n_ekin, 256 ), 256, 0, s>>>( m, b, repeat );
+    return cudaGetLastError();
+  }
+
+  int scatterLaunchesPerBatch() { return 2; }
 
   void setPhaseTiming( bool on )
   {
@@ -305,14 +390,4 @@ namespace ncgb {
     g_events.clear();
     return 0;
   }
-
-  cudaError_t launchXS( const ncgb_material_view& m, const Batch& b, uint64_t repeat, cudaStream_t s )
-  {
-    if ( b.n_ekin == 0 || repeat == 0 )
-      return cudaSuccess;
-    k_xs<<<gridFor( b.n_ekin, 256 ), 256, 0, s>>>( m, b, repeat );
-    return cudaGetLastError();
-  }
-
-  int scatterLaunchesPerBatch() { return 2; }
 }

@@ -19,9 +19,26 @@ namespace ncgb {
   // A neutron queued for S(alpha,beta) sampling: 16 bytes.
   struct QEntry {
     double ekin;
-    uint32_t idx;     // output index o (stream neutron index o + index_offset)
-    uint16_t comp;    // SAB component
-    uint16_t ndraws;  // random numbers already drawn (the component pick)
+    uint32_t idx;     // output index o
+    uint16_t mat;     // material of a multi-material batch (0 otherwise)
+    uint8_t comp;     // SAB component
+    uint8_t ndraws;   // random numbers already drawn (the component pick)
+  };
+
+  // One material of a multi-material batch, in device memory.
+  struct MatSlot {
+    ncgb_material_view view;
+    uint64_t seed;
+    uint32_t stream;
+    uint32_t pad;
+  };
+
+  // Launch shape (autotuned for multi-material batches): threads per block of
+  // the pick pass (128/256/512), resident blocks per SM of the persistent
+  // S(alpha,beta) pass (0 = as many as fit).
+  struct LaunchCfg {
+    int pick_block = 256;
+    int sab_blocks_per_sm = 0;
   };
 
   // One batch: neutron o (< n_out) has energy ekin[o % n_ekin] and draws
@@ -43,6 +60,11 @@ namespace ncgb {
   };
 
   cudaError_t launchScatter( const ncgb_material_view& m, const Batch& b, cudaStream_t s );
+  // Ragged multi-material batch: neutrons [d_offsets[k], d_offsets[k+1]) use
+  // material k, drawing from stream (seed_k, o - d_offsets[k], callseq, stream_k).
+  cudaError_t launchScatterMulti( const MatSlot* d_slots, const int64_t* d_offsets, int nmat,
+                                  const Batch& b, const LaunchCfg& cfg, cudaStream_t s );
+  int maxSabBlocksPerSM();
   cudaError_t launchXS( const ncgb_material_view& m, const Batch& b, uint64_t repeat, cudaStream_t s );
   int scatterLaunchesPerBatch();
   void setPhaseTiming( bool on );

@@ -174,3 +174,43 @@ def test_energies_above_emax_report_unsupported():
     sc = NC.createScatter(W.AL, seed=1)
     with pytest.raises(NC.NCCalcError):
         sc.sampleScatterIsotropic(np.array([10.0]))
+
+
+def test_ragged_batch_matches_single_material_calls():
+    """A multi-material batch reproduces, material by material, the first
+    scatter call of fresh single-material handles (same seed, stream index,
+    call sequence 0, neutron index local to the material)."""
+    import torch
+    cfgs = [W.AL, W.AL2O3, W.PE293, "Cu_sg225.ncmat;temp=77K", "ZnO_sg186_ZincOxide.ncmat;temp=400K"]
+    for c in cfgs:
+        bundle_path(c)
+    counts = [1000, 70000, 3, 25000, 40000]
+    seeds = [11, 12, 13, 14, 15]
+    energies = [W.loguniform_energies(n, 1e-4, 1.0, 50 + k) for k, n in enumerate(counts)]
+    e_all = torch.as_tensor(np.concatenate(energies), device="cuda")
+    off = torch.as_tensor(np.concatenate([[0], np.cumsum(counts)]), dtype=torch.int64, device="cuda")
+    n = e_all.numel()
+    batch = NC.Batch([NC.createScatter(c, seed=s) for c, s in zip(cfgs, seeds)])
+    xs, ef, mu = (torch.empty_like(e_all) for _ in range(3))
+    st = torch.zeros(n, dtype=torch.int32, device="cuda")
+    batch.scatter_device(e_all, off, xs, ef, mu, st)
+    torch.cuda.synchronize()
+    assert int((st != 0).sum()) == 0
+    o = np.concatenate([[0], np.cumsum(counts)])
+    for k, (c, s) in enumerate(zip(cfgs, seeds)):
+        single = NC.createScatter(c, seed=s)
+        sxs, sef, smu = single.xs_scatter(energies[k])
+        np.testing.assert_array_equal(xs[o[k]:o[k + 1]].cpu().numpy(), sxs)
+        np.testing.assert_array_equal(ef[o[k]:o[k + 1]].cpu().numpy(), sef)
+        np.testing.assert_array_equal(mu[o[k]:o[k + 1]].cpu().numpy(), smu)
+    # graph replay and autotuned shape give the same statistics and no failures
+    pb, sb = batch.autotune(e_all, off, xs, ef, mu)
+    assert pb in (128, 256, 512) and sb >= 1
+    for _ in range(2):
+        batch.graph_launch(e_all, off, xs, ef, mu, st)
+    torch.cuda.synchronize()
+    assert int((st != 0).sum()) == 0
+    assert float(mu.abs().max()) <= 1.0
+    # host-array entry point
+    hxs, hef, hmu = batch.xs_scatter_host(e_all.cpu().numpy(), off.cpu().numpy())
+    np.testing.assert_array_equal(hxs, xs.cpu().numpy())
