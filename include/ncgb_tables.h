@@ -138,6 +138,9 @@ typedef struct {
   int32_t pad0;
   double dom_elow, dom_ehigh; /* union of the component domains */
   ncgb_comp_view comp[NCGB_MAX_COMP];
+  /* erfc at the 1101 bin edges of [-2,9] plus +-infinity, for the free-gas
+   * sampler's cheap bounds (NCFreeGasUtils.cc:95-147); 1103 values */
+  const double* fg_erfc_table;
 } ncgb_material_view;
 
 #ifdef __cplusplus

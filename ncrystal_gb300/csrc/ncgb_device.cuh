@@ -495,32 +495,52 @@ namespace ncgb_dev {
     return 0;
   }
 
+}
+
+#include "ncgb_freegas.cuh"
+
+namespace ncgb_dev {
+
   // Per-neutron state of SABSampler::sampleAlphaBeta (NCSABSampler.cc:158-227)
   // with its two nested rejection loops flattened: 'outer' counts Alg.1 calls
-  // (<=100), 'inner' the attempts of the current call (<=100).
+  // (<=100), 'inner' the attempts of the current call (<=100).  'x' is E/kT of
+  // the energy the table is sampled at (Emax above the grid), 'xtrue' the
+  // neutron's own; 'preset' marks an (alpha, beta) already drawn from the
+  // free-gas extender.
   struct SABLane {
-    double ekin, x, xsamp;
+    double ekin, x, xsamp, xtrue;
+    double pre_alpha, pre_beta;
     int64_t ie;
     int inner, outer;
-    bool ultra_small;
+    bool ultra_small, preset;
   };
 
-  // Set-up of a SAB scatter at energy ekin (NCSABSampler.cc:163-197).
-  // Returns NCGB_ST_UNSUPPORTED for E >= Emax (free-gas extender).
-  __device__ __forceinline__ int sabBegin( const ncgb_sab_view& s, double ekin, SABLane& L )
+  // Set-up of a SAB scatter at energy ekin (NCSABSampler.cc:163-197),
+  // including the high-E extrapolation (NCSABSampler.cc:170-178).
+  __device__ __forceinline__ int sabBegin( const ncgb_sab_view& s, const double* fgtab, double ekin,
+                                           ncgb_rng& rng, SABLane& L )
   {
     const int64_t ne = s.ne;
     int64_t iu = upper_bound_nn( s.egrid, ne, ekin );
     L.ekin = ekin;
     L.ultra_small = false;
+    L.preset = false;
     L.inner = 0;
     L.outer = 0;
     L.ie = 0;
-    L.x = 0.0;
-    L.xsamp = 0.0;
-    if ( iu == ne )
-      return NCGB_ST_UNSUPPORTED;
-    if ( iu == 0 ) {
+    L.pre_alpha = L.pre_beta = 0.0;
+    L.xtrue = ekin * s.inv_kT;
+    double etab = ekin;
+    if ( iu == ne ) {
+      const int h = sabHighE( s, fgtab, ekin, rng, L.pre_alpha, L.pre_beta );
+      if ( h == -1 )
+        return NCGB_ST_CALCERROR;
+      if ( h < 0 )
+        return NCGB_ST_LOOPCAP;
+      L.preset = ( h == 1 );
+      etab = ldg( s.egrid + ne - 1 );
+      L.ie = ne - 1;
+    } else if ( iu == 0 ) {
       L.ie = 0;
       L.ultra_small = ( ekin < ldg( s.egrid ) );
     } else {
@@ -531,7 +551,7 @@ namespace ncgb_dev {
       }
       L.ie = iu;
     }
-    L.x = ekin * s.inv_kT;
+    L.x = etab * s.inv_kT;
     L.xsamp = L.ultra_small ? ldg( s.egrid ) * s.inv_kT : L.x;
     return NCGB_ST_OK;
   }
@@ -541,34 +561,40 @@ namespace ncgb_dev {
   __device__ __forceinline__ int sabStep( const ncgb_sab_view& s, SABLane& L, ncgb_rng& rng, double& ef, double& mu )
   {
     double alpha = 0.0, beta = 0.0;
-    if ( __ldg( s.smp_kind + L.ie ) != 0 ) {
-      if ( !alg1Attempt( s, L.ie, L.xsamp, rng, alpha, beta ) ) {
-        if ( ++L.inner >= 100 )
+    if ( L.preset ) {
+      alpha = L.pre_alpha;
+      beta = L.pre_beta;
+    } else {
+      if ( __ldg( s.smp_kind + L.ie ) != 0 ) {
+        if ( !alg1Attempt( s, L.ie, L.xsamp, rng, alpha, beta ) ) {
+          if ( ++L.inner >= 100 )
+            return NCGB_ST_LOOPCAP;
+          return -1;
+        }
+      } // else SABSamplerAtE_NoScatter: (alpha, beta) = (0, 0), no draws
+      // an Alg.1 call completed: the outer loop's tests
+      L.inner = 0;
+      const double x = L.x;
+      bool accept = false;
+      if ( !( beta < -x ) ) {
+        const ALim al = alphaLimits( x, beta );
+        if ( inInterval( al.lo, al.hi, alpha ) ) {
+          accept = true;
+        } else if ( L.ultra_small ) {
+          alpha = al.lo + rand01( rng ) * ( al.hi - al.lo );
+          accept = true;
+        }
+      }
+      if ( !accept ) {
+        if ( ++L.outer >= 100 )
           return NCGB_ST_LOOPCAP;
         return -1;
       }
-    } // else SABSamplerAtE_NoScatter: (alpha, beta) = (0, 0), no draws
-    // an Alg.1 call completed: the outer loop's tests
-    L.inner = 0;
-    const double x = L.x;
-    bool accept = false;
-    if ( !( beta < -x ) ) {
-      const ALim al = alphaLimits( x, beta );
-      if ( inInterval( al.lo, al.hi, alpha ) ) {
-        accept = true;
-      } else if ( L.ultra_small ) {
-        alpha = al.lo + rand01( rng ) * ( al.hi - al.lo );
-        accept = true;
-      }
     }
-    if ( !accept ) {
-      if ( ++L.outer >= 100 )
-        return NCGB_ST_LOOPCAP;
-      return -1;
-    }
-    // SABSampler::sampleDeltaEMu (NCSABSampler.cc:229-236), SABScatter (NCSABScatter.cc:92-101)
+    // SABSampler::sampleDeltaEMu (NCSABSampler.cc:229-236), SABScatter
+    // (NCSABScatter.cc:92-101), with the neutron's own energy
     double deltaE, muv;
-    if ( beta <= x * ( -1.0 + 1e-14 ) ) { // muIsotropicAtBeta, NCKinUtils.hh:64-70
+    if ( beta <= L.xtrue * ( -1.0 + 1e-14 ) ) { // muIsotropicAtBeta, NCKinUtils.hh:64-70
       deltaE = beta * s.kT;
       muv = rand01( rng ) * 2.0 - 1.0;
     } else {

@@ -140,13 +140,10 @@ namespace {
             mu = elincMu( c.elinc, rng, e, st );
             break;
           case NCGB_COMP_SAB:
-            if ( e >= ldg( c.sab.egrid + c.sab.ne - 1 ) )
-              st = NCGB_ST_UNSUPPORTED; // E >= Emax: free-gas extender (NCSABSampler.cc:59-156)
-            else
-              queue = true, qcomp = p.comp;
-            break;
           case NCGB_COMP_FREEGAS:
-            st = NCGB_ST_UNSUPPORTED;
+            // sampled by k_sab's refilled lanes
+            queue = true;
+            qcomp = p.comp;
             break;
           default:
             break;
@@ -180,7 +177,7 @@ namespace {
 
   // ---- phase 2: persistent S(alpha,beta) sampling ---------------------------
   template<class Src>
-  __global__ void __launch_bounds__(256)
+  __global__ void __launch_bounds__(256, 4)
   k_sab( const __grid_constant__ Src src, const ncgb::Batch b )
   {
     const unsigned FULL = 0xffffffffu;
@@ -209,11 +206,20 @@ namespace {
             src.rngFor( rng, q.mat, q.idx, b.callseq );
             for ( int k = 0; k < q.ndraws; ++k )
               rand01( rng );
-            const int st = sabBegin( src.mat( q.mat ).comp[q.comp].sab, q.ekin, L );
-            if ( st != NCGB_ST_OK )
-              writeScatter( b, q.idx, q.ekin, st, q.ekin, 1.0 );
-            else
-              has = true;
+            const ncgb_material_view& m = src.mat( q.mat );
+            const ncgb_comp_view& c = m.comp[q.comp];
+            if ( c.type == NCGB_COMP_FREEGAS ) {
+              // FreeGas component: sampled to completion here
+              double ef = q.ekin, mu = 1.0;
+              const int st = freeGasScatter( c.fg, m.fg_erfc_table, rng, q.ekin, ef, mu );
+              writeScatter( b, q.idx, q.ekin, st, ef, mu );
+            } else {
+              const int st = sabBegin( c.sab, m.fg_erfc_table, q.ekin, rng, L );
+              if ( st != NCGB_ST_OK )
+                writeScatter( b, q.idx, q.ekin, st, q.ekin, 1.0 );
+              else
+                has = true;
+            }
           } else {
             done = true;
           }

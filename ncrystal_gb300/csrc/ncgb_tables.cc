@@ -626,6 +626,21 @@ namespace ncgb {
         throw Error("unsupported component type in material bundle: " + type);
       }
     }
+    // erfc table of the free-gas sampler's bounds (NCFreeGasUtils.cc:95-122,
+    // linspace as NCMath.cc:68-81), with the host's erfc like the reference.
+    {
+      const int len = 1103;
+      std::vector<double> t( len );
+      const double lo = -2.0, hi = 9.0;
+      const unsigned num = len - 2, nm1 = num - 1;
+      const double interval = ( hi - lo ) / nm1;
+      t[0] = 2.0;
+      for ( unsigned i = 0; i < nm1; ++i )
+        t[1 + i] = std::erfc( lo + i * interval );
+      t[num] = std::erfc( hi );
+      t[len - 1] = 0.0;
+      v.fg_erfc_table = encodeOff<double>( mt->put( t ) );
+    }
     // Pad the arena so that it can be uploaded in 256-byte units.
     mt->m_arena.resize( ( mt->m_arena.size() + 255 ) & ~std::size_t(255) );
     return mt;
@@ -639,6 +654,7 @@ namespace ncgb {
   {
     const char* base = static_cast<const char*>( basev );
     ncgb_material_view v = m_rel;
+    v.fg_erfc_table = reloc( v.fg_erfc_table, base );
     for ( int ic = 0; ic < v.ncomp; ++ic ) {
       ncgb_comp_view& c = v.comp[ic];
       c.bragg.two_dE = reloc( c.bragg.two_dE, base );

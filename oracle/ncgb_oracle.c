@@ -17,8 +17,9 @@
  *
  * Status codes (per neutron): 0 ok; 1 a rejection loop hit its cap (the
  * reference throws CalcError, NCSABSampler.cc:226, NCSABSamplerModels.cc:150);
- * 2 free-gas sampling requested (not restated yet); 3 the reference throws
- * CalcError in convertAlphaBetaToDeltaEMu (E*E' == 0, NCKinUtils.cc:40-45).
+ * 3 the reference throws CalcError in convertAlphaBetaToDeltaEMu (E*E' == 0,
+ * NCKinUtils.cc:40-45) or BadInput in SABSampler::sampleHighE
+ * (NCSABSampler.cc:121-122).
  *
  * Built with -ffp-contract=off -O2 (no fast-math).
  */
@@ -438,6 +439,550 @@ static int ora_alg1( const ncgb_sab_view* s, int64_t ie, double ekin_div_kT, ncg
   return ORA_LOOPCAP;
 }
 
+/* ---- free gas (NCFreeGasUtils.cc) ------------------------------------------ */
+
+#define FG_TABLE_LEN 1103
+static double fg_erfc_table[FG_TABLE_LEN];
+
+/* erfc at the edges of 1100 bins on [-2,9] plus +-infinity
+ * (NCFreeGasUtils.cc:95-122; linspace as NCMath.cc:68-81). */
+__attribute__((constructor)) static void fg_init_table( void )
+{
+  const double lo = -2.0, hi = 9.0;
+  const unsigned num = FG_TABLE_LEN - 2, nm1 = num - 1;
+  const double interval = ( hi - lo ) / nm1;
+  fg_erfc_table[0] = 2.0;
+  for ( unsigned i = 0; i < nm1; ++i )
+    fg_erfc_table[1 + i] = erfc( lo + i * interval );
+  fg_erfc_table[num] = erfc( hi );
+  fg_erfc_table[FG_TABLE_LEN - 1] = 0.0;
+}
+
+/* erfcQuickBounds, NCFreeGasUtils.cc:124-147: lb <= erfc(x) <= ub. */
+static void fg_erfc_bounds( double x, double* lb, double* ub )
+{
+  const double binw = ( 9.0 - ( -2.0 ) ) / ( FG_TABLE_LEN - 3 );
+  const double invbinw = ( FG_TABLE_LEN - 3 ) / ( 9.0 - ( -2.0 ) );
+  const double verylow = -2.0 - 0.5 * binw;
+  const double veryhigh = 9.0 + 0.5 * binw;
+  const double xs = ora_clamp( x, verylow, veryhigh );
+  const double rel = xs - ( -2.0 );
+  int bin = (int)( 1.0 + rel * invbinw );
+  if ( bin > FG_TABLE_LEN - 1 ) bin = FG_TABLE_LEN - 1;
+  if ( bin < 0 ) bin = 0;
+  *lb = fg_erfc_table[bin + 1] * 0.99999999;
+  *ub = fg_erfc_table[bin] * 1.00000001;
+}
+
+/* erfcdiff, NCMath.cc:338-390 */
+static double fg_erfcdiff_nt( double a, double b )
+{
+  if ( b < 0 ) { double t = -b; b = -a; a = t; }
+  const double erfca = a > 27.3 ? 0.0 : erfc( a );
+  if ( b > a + 4.0 && ( a >= 4 || ( a < 0.0 && b > 6.0 ) ) )
+    return erfca;
+  const double erfcb = b > 27.3 ? 0.0 : erfc( b );
+  return erfca - erfcb;
+}
+
+static double fg_erfcdiff( double a, double b )
+{
+  const double kisp = 0.564189583547756286948079451560772585844050629;
+  if ( ora_max( fabs(a), fabs(b) ) < 0.32 ) {
+    const double c1 = -2.0 * kisp, c3 = 2.0 * kisp / 3.0, c5 = -0.2 * kisp, c7 = kisp / 21.0;
+    const double c9 = -kisp / 108.0, c11 = kisp / 660.0, c13 = -kisp / 4680.0, c15 = kisp / 37800.0;
+    const double a2 = a*a, b2 = b*b;
+    const double a3 = a * a2 * ( c3 + a2 * ( c5 + a2 * ( c7 + ( a2 * ( c9 + a2 * ( c11 + a2 * ( c13 + a2 * c15 ) ) ) ) ) ) );
+    const double b3 = b * b2 * ( c3 + b2 * ( c5 + b2 * ( c7 + ( b2 * ( c9 + b2 * ( c11 + b2 * ( c13 + b2 * c15 ) ) ) ) ) ) );
+    return c1*(a-b) + ( a3 - b3 );
+  }
+  return a > b ? -fg_erfcdiff_nt( b, a ) : fg_erfcdiff_nt( a, b );
+}
+
+/* erfc_rescaled, NCMath.cc:393-417: exp(b)*erfc(x) */
+static double fg_erfc_rescaled( double x, double b )
+{
+  if ( b < -745.1 )
+    return 0.0;
+  if ( ( x < 23.0 && fabs(b) < 700 ) || x < 5 )
+    return exp( b ) * erfc( x );
+  const double bxx = b - x*x;
+  if ( bxx < -745.1 )
+    return 0.0;
+  const double y = 1/x, y2 = y*y;
+  return 0.564189583547756286948079451560772585844050629 * exp( bxx )
+         * ( y+y2*(-0.5+y2*(0.75+y2*(-1.875+y2*(6.5625+y2*-29.53125)))) );
+}
+
+/* RandExpIntervalSampler, NCRandUtils.hh:162-199 */
+typedef struct { double a, c1, c2; } fg_expint;
+static void fg_expint_set( fg_expint* s, double a, double b, double c )
+{
+  s->a = a; s->c1 = -1.0 / c; s->c2 = expm1( -c * ( b - a ) );
+}
+static double fg_expint_sample( const fg_expint* s, ncgb_rng* rng )
+{
+  return s->a + s->c1 * log( 1.0 + ncgb_rng_generate( rng ) * s->c2 );
+}
+
+/* randExpDivSqrt, NCRandUtils.cc:224-330: exp(-c*x)/sqrt(x) on [a,b] */
+static double fg_rand_exp_div_sqrt( ncgb_rng* rng, double c, double a, double b )
+{
+  const double A = c*a;
+  if ( A > 0.1 ) {
+    const double U = c*(b-a);
+    const double invA = 1.0/A;
+    fg_expint es;
+    fg_expint_set( &es, 0, U, 1.0 );
+    for (;;) {
+      const double ugen = fg_expint_sample( &es, rng );
+      const double R = ncgb_rng_generate( rng );
+      if ( (1.0+ugen*invA)*R*R < 1.0 )
+        return ora_clamp( (ugen+A)/c, a, b );
+    }
+  }
+  const double Ulim = 16.1180956509583;
+  const double U = c*(b-a) < Ulim ? c*(b-a) : Ulim;
+  const double B = U+A;
+  if ( !( B > A ) )
+    return a;
+  const double sqrtA = sqrt(A), sqrtB = sqrt(B);
+  const double sBmA = sqrtB - sqrtA, twosqrtA = 2*sqrtA;
+  double ugen;
+  for (;;) {
+    const double T = ncgb_rng_generate( rng ) * sBmA;
+    ugen = T*(T+twosqrtA);
+    const double Ra = ncgb_rng_generate( rng );
+    if ( ugen < 2.0 ) {
+      const double t6 = 1.0+ugen*(-1.0+ugen*(1.0/2.0+ugen*(-1.0/6.0+ugen*(1.0/24.0+ugen*(-1.0/120.0+ugen*(1.0/720.0))))));
+      if ( Ra > t6 ) continue;
+      if ( Ra + 0.020221 < t6 ) break;
+    } else {
+      if ( Ra > 0.135335283236614 ) continue;
+      if ( ugen > 4.0 && Ra > 0.0183156388887343 ) continue;
+    }
+    if ( Ra < exp( -ugen ) )
+      break;
+  }
+  return ora_clamp( (ugen+A)/c, a, b );
+}
+
+/* randExpMInvXMCXDivSqrtX, NCFreeGasUtils.cc:223-488: exp(-1/x-c*x)/sqrt(x) on [xm,xp] */
+static double fg_f_eval( double x, double xmax, double c )
+{
+  const double exparg = (x-xmax)/(x*xmax)-c*(x-xmax);
+  if ( exparg >= 706.0 )
+    return 1.0;
+  return exparg < -745.1 ? 0.0 : exp( exparg ) * sqrt( xmax/x );
+}
+
+static double fg_rand_emix( ncgb_rng* rng, double c, double xm, double xp )
+{
+  if ( xp == xm )
+    return xm;
+  const double sqrtc = sqrt(c);
+  const double invsqrtc = 1/sqrtc;
+  const double xpeak = ( c > 1e-5
+                         ? ( c > 1e200 ? invsqrtc : (sqrt(16.0*c+1.0)-1.0)/(4.0*c) )
+                         : ( 2.0-c*(8.0-c*(64.0-c*(640.0-c*7168.0))) ) );
+  if ( xpeak == 0.0 )
+    return xm > 0.0 ? xm : ( DBL_MIN < xp ? DBL_MIN : xp );
+  const double xmax = ( xm > xpeak ? xm : ( xp < xpeak ? xp : xpeak ) );
+  if ( !( xmax > 0.0 ) )
+    return xm;
+  double xlarge = ora_max( 5.0/sqrt(c), 2*xpeak );
+  double xsmall = ( 0.2/sqrt(c) < 0.5*xpeak ) ? 0.2/sqrt(c) : 0.5*xpeak;
+  if ( xp > xlarge ) {
+    const double t = ora_max( xm, xlarge ) + 15.0/c;
+    xp = xp < t ? xp : t;
+  }
+  if ( xm < xsmall ) {
+    const double xsm = xp < xsmall ? xp : xsmall;
+    xm = ora_max( xm, xsm / ( 1 + 30.0*xsm ) );
+  }
+  const double fpmin = DBL_MIN;
+  if ( ( xm = ora_max( fpmin, ora_max( fpmin/xp, xm ) ) ) >= xp )
+    return xp;
+  const double fcutoff_limit = 1e-9;
+  if ( xp < xpeak ) {
+    for (;;) {
+      const double xm_new = xp - 0.01*(xp-xm);
+      const double fval = fg_f_eval( xm_new, xmax, c );
+      if ( fval >= fcutoff_limit )
+        break;
+      xm = xm_new;
+    }
+  }
+  double probability_flat = -1.0, xswitch = -1.0, area_right = -1.0;
+  if ( xm >= xlarge ) {
+    probability_flat = 0.0;
+    xswitch = xm;
+  } else if ( c > 25 || xp <= xlarge ) {
+    probability_flat = 1.0;
+    xswitch = xp;
+  } else {
+    xswitch = xlarge;
+    const double area_left = (xswitch-xm);
+    const double B = c*xmax+1/xmax-1/xp;
+    area_right = ( fg_erfc_rescaled( sqrtc*sqrt(xswitch), B ) - fg_erfc_rescaled( sqrtc*sqrt(xp), B ) )
+                 * sqrt( 3.1415926535897932384626433832795028841971694*(xmax/c) );
+    probability_flat = area_left/(area_left+area_right);
+  }
+  int single_side, always_left;
+#define FG_EVALP(pl) do { always_left = ( (pl) > 1.0-fcutoff_limit ); \
+    int always_right = ( (pl) < fcutoff_limit ); single_side = ( always_left || always_right ); } while(0)
+  FG_EVALP( probability_flat );
+  if ( !single_side && fg_f_eval( xswitch, xmax, c ) < fcutoff_limit*1.1 ) {
+    probability_flat = 1.0;
+    area_right = 0.0;
+    xp = xswitch;
+    always_left = 1;
+    single_side = 0;
+  }
+  for (;;) {
+    const int do_flat = single_side ? always_left : ( ncgb_rng_generate( rng ) < probability_flat );
+    if ( do_flat ) {
+      double dx = xswitch-xm;
+      const double xthr_up = xswitch, xthr_low = xm;
+      const double fthreshold = 0.05;
+      const double xgen = xm + ncgb_rng_generate( rng )*dx;
+      const double Raccept = ncgb_rng_generate( rng );
+      if ( !ora_in_interval( xthr_low, xthr_up, xgen ) && Raccept > fthreshold )
+        continue;
+      const double fval = fg_f_eval( xgen, xmax, c );
+      if ( fval < fthreshold ) {
+        if ( fval < fcutoff_limit ) {
+          if ( xgen < xmax )
+            xm = xgen;
+          else
+            xswitch = xgen;
+          dx = xswitch-xm;
+          if ( !single_side ) {
+            const double area_left = dx;
+            probability_flat = area_left/(area_left+area_right);
+            FG_EVALP( probability_flat );
+          }
+          continue;
+        }
+      }
+      if ( Raccept <= fval )
+        return xgen;
+    } else {
+      const double xgen = fg_rand_exp_div_sqrt( rng, c, xswitch, xp );
+      if ( ncgb_rng_generate( rng ) < exp( (xgen-xp)/(xgen*xp) ) )
+        return xgen;
+    }
+  }
+#undef FG_EVALP
+}
+
+/* FreeGasSampler state, NCFreeGasUtils.cc:492-515 */
+typedef struct {
+  double c, kT, sqrtAc, invA, Adiv4, normfact, c_real;
+} fg_sampler;
+
+static void fg_sampler_init( fg_sampler* s, double ekin, double kT, double mass_amu )
+{
+  const double cr = ekin / kT;
+  s->c = cr > 1e-10 ? cr : 1e-10;
+  if ( s->c > 1e14 ) s->c = 1e14;
+  s->kT = kT;
+  s->sqrtAc = sqrt( mass_amu * s->c / 1.00866491588 );
+  const double Arel = ( 1.0 / 1.00866491588 ) * mass_amu;
+  s->invA = 1.0 / Arel;
+  s->Adiv4 = 0.25 * Arel;
+  s->normfact = 0.5 / erf( sqrt( s->c * s->invA ) );
+  s->c_real = cr;
+}
+
+/* FGEvalBetaDistHelper, NCFreeGasUtils.cc:153-222 */
+typedef struct { double beta, normfact, expmbeta, k11, k12, k21, k22; } fg_betaeval;
+
+static void fg_betaeval_init( fg_betaeval* h, const fg_sampler* s, double beta )
+{
+  h->beta = beta;
+  h->normfact = s->normfact;
+  h->expmbeta = -1.0;
+  const double eps = beta / s->c;
+  const double sqrt1pluseps = sqrt( 1 + eps );
+  const double S = ( beta < 0.0 ? -1.0 : 1.0 );
+  const double sqrtepsprime = ( eps >= 0.0 ? 1.0 : sqrt1pluseps );
+  const double sqrtgammaplus = sqrt( 2.0+eps+2.0*sqrt1pluseps );
+  const double SP = 0.5*(S+s->invA);
+  const double SM = 0.5*(S-s->invA);
+  const double invA_sqrtepsprime = s->invA*sqrtepsprime;
+  const double mS_sqrtepsprime = -S*sqrtepsprime;
+  const double SPsgp = sqrtgammaplus*SP;
+  const double SMsgp = sqrtgammaplus*SM;
+  h->k11 = s->sqrtAc*( -invA_sqrtepsprime + SPsgp );
+  h->k12 = s->sqrtAc*( mS_sqrtepsprime + SPsgp );
+  h->k21 = s->sqrtAc*( mS_sqrtepsprime + SMsgp );
+  h->k22 = s->sqrtAc*( invA_sqrtepsprime + SMsgp );
+}
+
+static void fg_betaeval_expm( fg_betaeval* h )
+{
+  if ( h->expmbeta < 0 )
+    h->expmbeta = h->beta < -700.0 ? 0.0 : exp( -h->beta );
+}
+
+static double fg_betaeval_exact( fg_betaeval* h )
+{
+  const double t1 = fg_erfcdiff( h->k11, h->k12 );
+  fg_betaeval_expm( h );
+  if ( !h->expmbeta )
+    return h->normfact*t1;
+  const double t2 = fg_erfcdiff( h->k21, h->k22 );
+  return h->normfact*(t1+t2*h->expmbeta);
+}
+
+static void fg_betaeval_bounds( fg_betaeval* h, double* lb, double* ub )
+{
+  double l11, u11, l12, u12, l21, u21, l22, u22;
+  fg_erfc_bounds( h->k11, &l11, &u11 );
+  fg_erfc_bounds( h->k12, &l12, &u12 );
+  const double t1l = l11 - u12, t1u = u11 - l12;
+  fg_erfc_bounds( h->k21, &l21, &u21 );
+  fg_erfc_bounds( h->k22, &l22, &u22 );
+  const double t2l = l21 - u22, t2u = u21 - l22;
+  if ( t2u > 0.0 ) {
+    fg_betaeval_expm( h );
+    *lb = h->normfact*(t1l+t2l*h->expmbeta);
+    *ub = h->normfact*(t1u+t2u*h->expmbeta);
+    return;
+  }
+  *lb = h->normfact*t1l;
+  *ub = h->normfact*t1u;
+}
+
+/* FreeGasSampler::sampleBeta, NCFreeGasUtils.cc:530-849 */
+static double fg_sample_beta( const fg_sampler* s, ncgb_rng* rng )
+{
+  if ( s->c_real > 1e4 ) {
+    const double A = 1.0 / s->invA;
+    const double A2 = A*A;
+    const double thr = 1e4 * ( 1000.0*A < A2*A2*A2 ? 1000.0*A : A2*A2*A2 );
+    if ( s->c_real > thr ) {
+      const double am1_div_ap1 = (1.0-s->invA)/(1.0+s->invA);
+      const double elossmax = s->c_real * (1.0-am1_div_ap1*am1_div_ap1);
+      return -elossmax*ncgb_rng_generate( rng );
+    }
+  }
+  const double Tlim = 2.0;
+  const double Tlim_k1 = 0.135335283236612691893999494972484403407;
+  const double Tlim_k2 = 274./315.;
+  const double fcutoff_limit = 1e-6;
+  double aa = ora_max( -s->c_real, -s->c ), bb = 13.815510557964274;
+  if ( s->invA <= 1.0/10.0 ) {
+    if ( s->c > 10.1 ) {
+      for (;;) {
+        const double aa_new = aa*0.2;
+        if ( aa_new > -1e-99 )
+          break;
+        fg_betaeval h;
+        fg_betaeval_init( &h, s, aa_new );
+        if ( fg_betaeval_exact( &h ) > fcutoff_limit )
+          break;
+        aa = aa_new;
+      }
+    }
+    for (;;) {
+      const double bb_new = bb*0.25;
+      if ( bb_new < 1e-99 )
+        break;
+      fg_betaeval h;
+      double lb, ub;
+      fg_betaeval_init( &h, s, bb_new );
+      fg_betaeval_bounds( &h, &lb, &ub );
+      if ( ub > fcutoff_limit )
+        break;
+      bb = bb_new;
+    }
+  }
+  if ( !( bb > aa ) )
+    return aa;
+  double a = 0, b = 0, prob_downscat = 0, prob_notclosetail = 0;
+  fg_expint es;
+  int es_valid = 0;
+#define FG_SETAB(aaa,bbb) do { \
+    a = (aaa); b = (bbb); \
+    double area_downscat = -a, area_fartail, area_closetail; \
+    if ( b <= Tlim ) { \
+      area_fartail = 0.0; \
+      area_closetail = b * (1.0+b*(-1./2.+b*(1./6.+b*(-1./24.+b*(1./120.+b*(-1./720.+b*(1./5040.))))))); \
+    } else { \
+      area_fartail = Tlim_k1 - exp( -b ); \
+      area_closetail = Tlim_k2; \
+    } \
+    const double invareatot = 1.0 / ( area_downscat + area_closetail + area_fartail ); \
+    prob_downscat = area_downscat * invareatot; \
+    prob_notclosetail = ( area_fartail + area_downscat ) * invareatot; \
+    es_valid = 0; } while (0)
+  FG_SETAB( aa, bb );
+  const double fthreshold = 0.1;
+  double afthreshold = a, bfthreshold = b;
+  for (;;) {
+    double beta, foverlay;
+    const double Rsel = ncgb_rng_generate( rng );
+    if ( Rsel < prob_downscat ) {
+      beta = ncgb_rng_generate( rng )*a;
+      foverlay = 1.0;
+    } else if ( Rsel < prob_notclosetail ) {
+      if ( !es_valid ) { fg_expint_set( &es, Tlim, b, 1.0 ); es_valid = 1; }
+      beta = fg_expint_sample( &es, rng );
+      foverlay = exp( -beta );
+    } else {
+      const double bmax = b < Tlim ? b : Tlim;
+      for (;;) {
+        beta = ncgb_rng_generate( rng )*bmax;
+        const double R0 = ncgb_rng_generate( rng );
+        const double kcheap = 19./45.;
+        if ( R0 > 1.0 - kcheap*beta )
+          continue;
+        foverlay = 1.0+beta*(-1.+beta*(1./2.+beta*(-1./6.+beta*(1./24.+beta*(-1./120.+beta*(1./720.))))));
+        if ( R0 < foverlay )
+          break;
+      }
+    }
+    const double faccept = ncgb_rng_generate( rng )*foverlay;
+    if ( faccept > fthreshold && !ora_in_interval( afthreshold, bfthreshold, beta ) )
+      continue;
+    fg_betaeval h;
+    fg_betaeval_init( &h, s, beta );
+    int need_exact = 1;
+    double fval = 0.0;
+    if ( beta > 0 ) {
+      double lb, ub;
+      fg_betaeval_bounds( &h, &lb, &ub );
+      if ( faccept <= lb )
+        return beta;
+      fval = ub;
+      if ( faccept > ub )
+        need_exact = 0;
+    }
+    if ( need_exact ) {
+      fval = fg_betaeval_exact( &h );
+      if ( faccept < fval )
+        return beta;
+    }
+    if ( fval < fcutoff_limit ) {
+      if ( beta < 0 ) { FG_SETAB( beta, b ); } else { FG_SETAB( a, beta ); }
+      continue;
+    }
+    if ( fval < fthreshold ) {
+      if ( beta < 0 )
+        afthreshold = ora_max( afthreshold, beta );
+      else
+        bfthreshold = bfthreshold < beta ? bfthreshold : beta;
+    }
+  }
+#undef FG_SETAB
+}
+
+/* FreeGasSampler::sampleAlpha, NCFreeGasUtils.cc:851-932 */
+static double fg_sample_alpha( const fg_sampler* s, double beta, ncgb_rng* rng )
+{
+  if ( s->c_real < s->c || ora_mu_isotropic_at_beta( beta, s->c ) ) {
+    ora_alim al = ora_alpha_limits( s->c_real, beta );
+    const double alpha = al.lo + ncgb_rng_generate( rng )*(al.hi-al.lo);
+    return ora_clamp( alpha, al.lo, al.hi );
+  }
+  beta = ora_max( -s->c, beta );
+  ora_alim al = ora_alpha_limits( s->c, beta );
+  const double am = al.lo, ap = al.hi;
+  if ( am == ap )
+    return am;
+  const double betasq = beta*beta;
+  const double t = betasq * s->Adiv4;
+  const double c = 0.0625 * betasq;
+  if ( ( t < c ? t : c ) < 1e-5 ) {
+    const double fourA = s->Adiv4*16.0;
+    const double inv4A = 1.0/fourA;
+    const double xxm = am*inv4A, xxp = ap*inv4A;
+    for (;;) {
+      const double xx = fg_rand_exp_div_sqrt( rng, 1.0, xxm, xxp );
+      const double alpha = xx * fourA;
+      if ( alpha < am || alpha > ap )
+        continue;
+      if ( alpha*ap*( -log( ncgb_rng_generate( rng ) ) ) >= t*(ap-alpha) )
+        return alpha;
+    }
+  }
+  const double invt = 1.0/t;
+  const double x = fg_rand_emix( rng, c, am*invt, ap*invt );
+  return ora_clamp( x*t, am, ap );
+}
+
+/* FreeGasSampler::sampleAlphaBeta (NCFreeGasUtils.hh:132-144) */
+static void fg_sample_alphabeta( const fg_sampler* s, ncgb_rng* rng, double* alpha, double* beta )
+{
+  const double b = fg_sample_beta( s, rng );
+  if ( b < -s->c || ora_mu_isotropic_at_beta( b, s->c ) ) {
+    ora_alim al = ora_alpha_limits( s->c_real, b );
+    const double a = al.lo+ncgb_rng_generate( rng )*(al.hi-al.lo);
+    *alpha = ora_clamp( a, al.lo, al.hi );
+    *beta = b;
+    return;
+  }
+  *alpha = fg_sample_alpha( s, b, rng );
+  *beta = b;
+}
+
+/* FreeGas::sampleScatterIsotropic (NCFreeGas.cc:70-75) via
+ * FreeGasSampler::sampleDeltaEMu (NCFreeGasUtils.hh:146-161). */
+static int ora_freegas_scatter( const ncgb_freegas_view* v, ncgb_rng* rng, double ekin, double* ef, double* mu )
+{
+  fg_sampler s;
+  fg_sampler_init( &s, ekin, v->kT, v->mass_amu );
+  const double beta = fg_sample_beta( &s, rng );
+  double dE, muv;
+  if ( beta <= -s.c || ora_mu_isotropic_at_beta( beta, s.c ) ) {
+    dE = beta*s.kT;
+    muv = ncgb_rng_generate( rng )*2.0-1.0;
+  } else {
+    const double alpha = fg_sample_alpha( &s, beta, rng );
+    int st = ora_alphabeta_to_demu( alpha, beta, s.c*s.kT, s.kT, &dE, &muv );
+    if ( st != ORA_OK )
+      return st;
+  }
+  *ef = ora_max( 0.0, ekin + dE );
+  *mu = muv;
+  return ORA_OK;
+}
+
+/* SABSampler::sampleHighE, NCSABSampler.cc:59-156.  Returns 1 with (alpha,
+ * beta) from the extender, 0 if the table must be sampled at E = Emax, or -1
+ * where the reference throws BadInput. */
+static int ora_sab_high_e( const ncgb_sab_view* s, double ekin, ncgb_rng* rng, double* alpha, double* beta )
+{
+  const double emax = s->egrid[s->ne - 1];
+  const double extE = ekin * ( s->ext_sigma_free * ora_freegas_shape( s->ext_ca * ekin ) );
+  const double P_inside = s->k1 / ( ( s->k1 - s->k2 ) + extE );
+  const double P_ext_inside = s->k2 / extE;
+  const double P_discard = ( P_ext_inside >= P_inside ? ( 1.0 - P_inside/P_ext_inside ) : 0.0 );
+  if ( P_discard > 0.95 )
+    return -1;
+  if ( P_ext_inside < P_inside ) {
+    const double aa = 1.0 - P_ext_inside;
+    const double P_extra = aa > 1e-10 ? ( P_inside - P_ext_inside ) / aa : 1.0;
+    if ( ncgb_rng_generate( rng ) < P_extra )
+      return 0;
+  }
+  const double emax_div_kt = emax / s->kT;
+  fg_sampler fs;
+  fg_sampler_init( &fs, ekin, s->ext_kT, s->ext_mass_amu );
+  for (;;) {
+    double a, b;
+    fg_sample_alphabeta( &fs, rng, &a, &b );
+    if ( b <= -emax_div_kt ) { *alpha = a; *beta = b; return 1; }
+    ora_alim al = ora_alpha_limits( emax_div_kt, b );
+    if ( !ora_in_interval( al.lo, al.hi, a ) ) { *alpha = a; *beta = b; return 1; }
+    if ( P_discard && ncgb_rng_generate( rng ) < P_discard )
+      continue;
+    return 0;
+  }
+}
+
 /* SABSampler::sampleAlphaBeta + sampleDeltaEMu, NCSABSampler.cc:158-236,
  * and SABScatter::sampleScatterIsotropic, NCSABScatter.cc:92-101. */
 static int ora_sab_scatter( const ncgb_sab_view* s, ncgb_rng* rng, double ekin, double* ef, double* mu )
@@ -446,8 +991,18 @@ static int ora_sab_scatter( const ncgb_sab_view* s, ncgb_rng* rng, double ekin, 
   size_t iu = ora_upper_bound( s->egrid, ne, ekin );
   int ultra_small = 0;
   int64_t ie;
+  double ekin_tab = ekin; /* energy the table is sampled at */
+  double alpha = 0.0, beta = 0.0;
+  int found = 0;
   if ( iu == ne ) {
-    return ORA_UNSUPPORTED; /* E >= Emax: free-gas extender sampling (NCSABSampler.cc:59-156) */
+    /* high-E extrapolation (NCSABSampler.cc:170-178) */
+    const int h = ora_sab_high_e( s, ekin, rng, &alpha, &beta );
+    if ( h < 0 )
+      return ORA_CALCERROR;
+    if ( h == 1 )
+      found = 1;
+    ekin_tab = s->egrid[ne - 1];
+    ie = (int64_t)ne - 1;
   } else if ( iu == 0 ) {
     ie = 0;
     ultra_small = ( ekin < s->egrid[0] );
@@ -458,11 +1013,9 @@ static int ora_sab_scatter( const ncgb_sab_view* s, ncgb_rng* rng, double ekin, 
     }
     ie = (int64_t)iu;
   }
-  const double ekin_div_kT = ekin / s->kT;
+  const double ekin_div_kT = ekin_tab / s->kT;
   const double sampling_ekin_div_kT = ultra_small ? s->egrid[0] / s->kT : ekin_div_kT;
-  double alpha = 0.0, beta = 0.0;
-  int found = 0;
-  for ( int loop = 0; loop < 100; ++loop ) {
+  for ( int loop = 0; !found && loop < 100; ++loop ) {
     if ( s->smp_kind[ie] == 0 ) {
       alpha = 0.0; beta = 0.0;
     } else {
@@ -482,6 +1035,7 @@ static int ora_sab_scatter( const ncgb_sab_view* s, ncgb_rng* rng, double ekin, 
   }
   if ( !found )
     return ORA_LOOPCAP;
+  /* SABSampler::sampleDeltaEMu uses the neutron's own energy from here on */
   double deltaE, muv;
   if ( ora_mu_isotropic_at_beta( beta, ekin / s->kT ) ) {
     deltaE = beta * s->kT;
@@ -530,7 +1084,7 @@ int ncgb_oracle_scatter( const ncgb_material_view* m, ncgb_rng* rng, double ekin
       st = ora_sab_scatter( &c->sab, rng, ekin, ef, mu );
       break;
     case NCGB_COMP_FREEGAS:
-      st = ORA_UNSUPPORTED;
+      st = ora_freegas_scatter( &c->fg, rng, ekin, ef, mu );
       break;
     default:
       *ef = ekin; *mu = 1.0;

@@ -37,6 +37,9 @@ GOLDEN = {
     "cu77": ("Cu_sg225.ncmat;temp=77K", lambda n: W.loguniform_energies(n, 1e-4, 1.0, 106)),
     "zno400": ("ZnO_sg186_ZincOxide.ncmat;temp=400K", lambda n: W.loguniform_energies(n, 1e-4, 1.0, 107)),
     "kat_ni": ("Ni_sg225.ncmat;dcutoff=0.6;vdoslux=2", lambda n: W.loguniform_energies(n, 1e-4, 1.0, 108)),
+    # above the S(alpha,beta) grids' Emax (free-gas extender) and free-gas O in water
+    "al_highe": (W.AL, lambda n: W.loguniform_energies(n, 4.0, 60.0, 109)),
+    "water_highe": (W.WATER, lambda n: W.loguniform_energies(n, 1e-3, 60.0, 110)),
 }
 
 
