@@ -75,6 +75,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="al2o3_large",
                     choices=["al2o3_large", "al_small", "pe", "crystal_batch"])
+    ap.add_argument("--mode", default="exact", choices=["exact", "mixed"],
+                    help="arithmetic mode of the GPU path (mixed: FP32 incoherent-elastic exponentials "
+                         "and alpha inversion, FP64 elsewhere)")
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="wall-clock budget of the CPU baseline sample")
     return ap.parse_args()
@@ -218,7 +221,7 @@ def config_of(args, wl, world):
     cfgs = wl["cfgs"]
     return {"workload": args.workload, "cfg": cfgs[0] if len(cfgs) == 1 else "%d instances" % len(cfgs),
             "neutrons_per_gpu": int(sum(wl["counts"])), "io": wl["io"], "sampler": "plain (Alg.1 tables)",
-            "parallelism": "replicas%d" % world}
+            "mode": getattr(args, "mode", "exact"), "parallelism": "replicas%d" % world}
 
 
 def run_reference(args):
@@ -253,13 +256,13 @@ class SingleRunner:
     """One material, device arrays (ncgb_scatter_device) and host arrays
     (ncgb_xs_scatter_many[_f32])."""
 
-    def __init__(self, NC, torch, wl, dev, seed):
+    def __init__(self, NC, torch, wl, dev, seed, mode):
         self.torch = torch
         self.f32 = wl["io"] == "f32"
         self.dt = torch.float32 if self.f32 else torch.float64
         e = wl["energies"][0].astype(np.float32 if self.f32 else np.float64)
         self.n = len(e)
-        self.sc = NC.createScatter(wl["cfgs"][0], seed=seed)
+        self.sc = NC.createScatter(wl["cfgs"][0], seed=seed).set_mode(mode)
         self.d_e = torch.from_numpy(e).to(dev)
         self.d_xs, self.d_ef, self.d_mu = (torch.empty_like(self.d_e) for _ in range(3))
         self.h_e = torch.from_numpy(e).pin_memory()
@@ -295,13 +298,14 @@ class BatchRunner:
     """Ragged multi-material batch: autotuned shape, CUDA-graph replay on
     device arrays; host arrays through ncgb_batch_xs_scatter_many."""
 
-    def __init__(self, NC, torch, wl, dev, seed):
+    def __init__(self, NC, torch, wl, dev, seed, mode):
         self.torch = torch
         self.f32 = False
         e = np.concatenate(wl["energies"]).astype(np.float64)
         self.n = len(e)
         offs = np.concatenate([[0], np.cumsum(wl["counts"])]).astype(np.int64)
         self.batch = NC.Batch([NC.createScatter(c, seed=seed + k) for k, c in enumerate(wl["cfgs"])])
+        self.batch.set_mode(mode)
         self.d_e = torch.from_numpy(e).to(dev)
         self.d_off = torch.from_numpy(offs).to(dev)
         self.d_xs, self.d_ef, self.d_mu = (torch.empty_like(self.d_e) for _ in range(3))
@@ -356,7 +360,7 @@ def run_gb300(args):
     wl = workload(args.workload, rank)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
-    R = (BatchRunner if len(wl["cfgs"]) > 1 else SingleRunner)(NC, torch, wl, dev, 0xB0057 + 977 * rank)
+    R = (BatchRunner if len(wl["cfgs"]) > 1 else SingleRunner)(NC, torch, wl, dev, 0xB0057 + 977 * rank, args.mode)
     n = R.n
     esz = 4 if R.f32 else 8
     io_bytes = 4 * esz * n  # energies in, xs / E' / mu out
@@ -458,8 +462,8 @@ def run_gb300(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": cfgd,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.mode == "exact" else "f64+f32",
+            "data": "synthetic", "config": cfgd,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
                          "traffic": profiled_traffic(dom, args.workload), "kernel": dom, "kernels": kernels,

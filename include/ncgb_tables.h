@@ -60,6 +60,25 @@ typedef struct {
   double k_e, k_z, inv_a, pad;
 } ncgb_beta_bin;
 
+/* Learned beta proposal of one sampler (egrid point): a partition of the
+ * sampler's regular beta range into NCGB_LP_K intervals with knots placed by
+ * a trained network, a piecewise-constant envelope (the maximum of the
+ * sampler's piecewise-linear beta density on each interval) and an alias
+ * table over the interval masses.  No reference counterpart. */
+#define NCGB_LP_K 63
+typedef struct {
+  double c1;        /* probability of the special first beta bin (0 if none) */
+  float accept;     /* expected acceptance of the envelope */
+  int32_t enabled;  /* 0: the plain percentile inversion is used */
+} ncgb_lp_hdr;
+typedef struct {
+  double q;         /* knot k (interval k is [q_k, q_k+1]) */
+  float env;        /* envelope height on interval k */
+  float aprob;      /* alias table: keep probability of slot k */
+  int32_t bin;      /* beta-bin j of the sampler with bx[j] <= q_k < bx[j+1] */
+  int32_t alias;    /* alias table: other interval of slot k */
+} ncgb_lp_cell;
+
 /* One alpha cell [alpha_i, alpha_i+1] of a beta row: the constants of the
  * log-linear in-cell inversion (NCSABUtils.hh:282-304) for the middle part of
  * the alpha sampler: inv_bin = 1/(cumul_i+1 - cumul_i), ratio = S_i+1/S_i - 1,
@@ -117,6 +136,9 @@ typedef struct {
   const double* inv_dbeta;        /* [nb] 1/(beta[i+1]-beta[i]) */
   const ncgb_beta_bin* bbin;      /* [offset + j]: bin j of a sampler, j < nbeta-1 */
   const ncgb_alpha_cell* acell;   /* [nb*na] */
+  /* learned beta proposal (NULL: none attached): lp_hdr[ne], lp_cell[ne*(NCGB_LP_K+1)] */
+  const ncgb_lp_hdr* lp_hdr;
+  const ncgb_lp_cell* lp_cell;
 } ncgb_sab_view;
 
 typedef struct {

@@ -120,7 +120,7 @@ const char * ncrystal_version_str( void );
 /* Per-neutron status codes written by the kernels. */
 #define NCGB_ST_OK 0
 #define NCGB_ST_LOOPCAP 1      /* rejection loop cap hit (reference: CalcError) */
-#define NCGB_ST_UNSUPPORTED 2  /* free-gas sampling (not yet on the GPU) */
+#define NCGB_ST_UNSUPPORTED 2  /* reserved (no kernel writes it) */
 #define NCGB_ST_CALCERROR 3    /* E*E' == 0 in the (alpha,beta) -> mu conversion
                                   (reference: CalcError, NCKinUtils.cc:40-45) */
 
@@ -161,6 +161,25 @@ void ncgb_crosssection_nonoriented_many_f32( ncrystal_process_t, const float* ek
 void ncgb_samplescatterisotropic_many_f32( ncrystal_scatter_t, const float* ekin,
                                            unsigned long n_ekin, float* results_ekin,
                                            float* results_cos_scat_angle );
+
+/* Arithmetic mode of a handle (or a batch).  NCGB_MODE_EXACT (the default)
+ * computes in FP64 throughout and reproduces the reference's results.
+ * NCGB_MODE_MIXED evaluates the incoherent-elastic exponentials (cross-section
+ * and angle sampling) and the log-linear alpha inversion of the S(alpha,beta)
+ * sampler in FP32; the beta-CDF inversion, Bragg sums, rejection tests and
+ * kinematics stay FP64.  Mixed-mode cross-sections agree with the exact ones
+ * to about 1e-7 relative; sampled alpha values move by about 1e-7 relative,
+ * so a rejection decision or the choice of a table bin near its edge can
+ * differ for a small fraction of neutrons (the sampled distributions are
+ * unchanged).  New handles start in the mode named by the environment
+ * variable NCGB_MODE ("exact" or "mixed"; unset = exact); clones inherit the
+ * mode.  ncgb_scatter_device_noalloc always computes in the exact mode.
+ * ncgb_set_mode returns 0, or non-zero after setting the error state;
+ * ncgb_get_mode returns the mode, or -1 on error. */
+#define NCGB_MODE_EXACT 0
+#define NCGB_MODE_MIXED 1
+int ncgb_set_mode( ncrystal_scatter_t, int mode );
+int ncgb_get_mode( ncrystal_scatter_t );
 
 /* Fused cross-section + scatter with HOST arrays: ekin[n] -> xs[n], E'[n],
  * mu[n] (any output may be NULL), FP64 or FP32.  Copies in, runs and copies
@@ -212,6 +231,8 @@ int ncgb_batch_config( ncgb_batch_t, int* pick_block, int* sab_blocks_per_sm );
 int ncgb_batch_graph_launch( ncgb_batch_t, const double* d_ekin, const int64_t* d_offsets, unsigned long n,
                              double* d_xs, double* d_ekin_final, double* d_mu, int32_t* d_status,
                              void* stream );
+/* Arithmetic mode of the batch (NCGB_MODE_*; starts as NCGB_MODE below). */
+int ncgb_batch_set_mode( ncgb_batch_t, int mode );
 /* Host arrays: copies in, runs and copies out (synchronous). */
 void ncgb_batch_xs_scatter_many( ncgb_batch_t, const double* ekin, const int64_t* offsets, unsigned long n,
                                  double* xs, double* ekin_final, double* mu );

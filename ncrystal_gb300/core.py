@@ -106,6 +106,9 @@ def lib():
         "ncgb_batch_autotune": (_C.c_int, [_Handle, _C.c_void_p, _C.c_void_p, _C.c_ulong, _C.c_void_p,
                                            _C.c_void_p, _C.c_void_p, _C.c_void_p]),
         "ncgb_batch_config": (_C.c_int, [_Handle, _C.POINTER(_C.c_int), _C.POINTER(_C.c_int)]),
+        "ncgb_batch_set_mode": (_C.c_int, [_Handle, _C.c_int]),
+        "ncgb_set_mode": (_C.c_int, [H, _C.c_int]),
+        "ncgb_get_mode": (_C.c_int, [H]),
         "ncgb_batch_xs_scatter_many": (None, [_Handle, _C.c_void_p, _C.c_void_p, _C.c_ulong, _C.c_void_p,
                                               _C.c_void_p, _C.c_void_p]),
         "ncgb_phase_timing": (None, [_C.c_int]),
@@ -214,8 +217,30 @@ class Process:
         return lib().ncgb_device_bytes(self._h)
 
 
+MODES = {"exact": 0, "mixed": 1}
+
+
+def _mode_code(mode):
+    if mode not in MODES:
+        raise NCBadInput("mode must be one of %s" % sorted(MODES))
+    return MODES[mode]
+
+
 class Scatter(Process):
     """A scattering process with its own random streams (NCrystal core.py:1411-1520)."""
+
+    @property
+    def mode(self):
+        """Arithmetic mode, "exact" (FP64 throughout) or "mixed" (FP32 for the
+        incoherent-elastic exponentials and the alpha inversion)."""
+        m = lib().ncgb_get_mode(self._h)
+        _check()
+        return {v: k for k, v in MODES.items()}[m]
+
+    def set_mode(self, mode):
+        if lib().ncgb_set_mode(self._h, _mode_code(mode)):
+            _check()
+        return self
 
     def sampleScatterIsotropic(self, ekin, repeat=None):
         """Returns (ekin_final, mu) -- NCrystal core.py:1492."""
@@ -340,6 +365,12 @@ class Batch:
     @property
     def nmat(self):
         return len(self._scatters)
+
+    def set_mode(self, mode):
+        """Arithmetic mode of the batch: "exact" or "mixed" (see Scatter.mode)."""
+        if lib().ncgb_batch_set_mode(self._h, _mode_code(mode)):
+            _check()
+        return self
 
     def _args(self, ekin, offsets, xs, ef, mu, status, stream):
         import torch

@@ -209,6 +209,32 @@ namespace {
   constexpr uint32_t kScatterTypeID = 0x7d6b0637; // same tag value as NCrystal's Scatter
   constexpr uint64_t kDefaultSeed = 0x4e43727973746c21ull;
 
+  // Mode of new handles and batches: the environment variable NCGB_MODE
+  // ("exact" / "mixed", or 0 / 1); unset means exact.
+  int defaultMode()
+  {
+    static const int m = [] {
+      const char* v = std::getenv( "NCGB_MODE" );
+      if ( !v || !*v )
+        return NCGB_MODE_EXACT;
+      const std::string s( v );
+      if ( s == "mixed" || s == "1" )
+        return NCGB_MODE_MIXED;
+      if ( s == "exact" || s == "0" )
+        return NCGB_MODE_EXACT;
+      std::fprintf( stderr, "NCrystal WARNING: ignoring NCGB_MODE=%s (expected exact or mixed)\n", v );
+      return NCGB_MODE_EXACT;
+    }();
+    return m;
+  }
+
+  int checkMode( int mode, const char* fct )
+  {
+    if ( mode != NCGB_MODE_EXACT && mode != NCGB_MODE_MIXED )
+      throw TypedError( "BadInput", std::string( fct ) + ": mode must be NCGB_MODE_EXACT or NCGB_MODE_MIXED" );
+    return mode;
+  }
+
   struct ScatterObj;
   struct FingerPrint {
     uint32_t typeid_;
@@ -222,6 +248,7 @@ namespace {
     std::string cfg;
     uint64_t seed = kDefaultSeed;
     uint32_t streamidx = 0;
+    int mode = defaultMode();
     std::atomic<uint32_t> callseq{0};
     ScatterObj() { fp.typeid_ = kScatterTypeID; fp.obj = this; }
   };
@@ -317,6 +344,7 @@ namespace {
     b.seed = o.seed;
     b.callseq = call;
     b.stream = o.streamidx;
+    b.fast = ( o.mode == NCGB_MODE_MIXED );
     b.work = s.d_work;
     b.queue = static_cast<ncgb::QEntry*>( s.d_queue );
     return b;
@@ -563,7 +591,25 @@ static ncrystal_scatter_t cloneWithStream( ncrystal_scatter_t sc, uint32_t strea
   o->cfg = src.cfg;
   o->seed = src.seed;
   o->streamidx = streamidx;
+  o->mode = src.mode;
   return makeHandle( o.release() );
+}
+
+int ncgb_set_mode( ncrystal_scatter_t sc, int mode )
+{
+  try {
+    extract( sc.internal, "ncgb_set_mode" ).mode = checkMode( mode, "ncgb_set_mode" );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_get_mode( ncrystal_scatter_t sc )
+{
+  try {
+    return extract( sc.internal, "ncgb_get_mode" ).mode;
+  } NCGB_CATCH;
+  return -1;
 }
 
 ncrystal_scatter_t ncrystal_clone_scatter( ncrystal_scatter_t sc )
@@ -901,6 +947,7 @@ namespace {
     int nmat = 0;
     ncgb::LaunchCfg cfg;
     bool tuned = false;
+    int mode = defaultMode();
     std::atomic<uint32_t> callseq{0};
     // CUDA graph of (counter reset, k_pick, k_sab) for one set of arrays
     cudaGraphExec_t exec = nullptr;
@@ -933,6 +980,7 @@ namespace {
     b.out_a = d_ef;
     b.out_b = d_mu;
     b.status = d_status;
+    b.fast = ( bo.mode == NCGB_MODE_MIXED );
     b.work = s.d_work;
     ensure( s.d_queue, s.cap_queue, n * sizeof(ncgb::QEntry) );
     b.queue = static_cast<ncgb::QEntry*>( s.d_queue );
@@ -1049,6 +1097,16 @@ int ncgb_batch_autotune( ncgb_batch_t bt, const double* d_ekin, const int64_t* d
     bo.cfg = bestc;
     bo.tuned = true;
     if ( bo.exec ) { cudaGraphExecDestroy( bo.exec ); bo.exec = nullptr; }
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_batch_set_mode( ncgb_batch_t bt, int mode )
+{
+  try {
+    BatchObj& bo = extractBatch( bt.internal, "ncgb_batch_set_mode" );
+    bo.mode = checkMode( mode, "ncgb_batch_set_mode" );
     return 0;
   } NCGB_CATCH;
   return 1;

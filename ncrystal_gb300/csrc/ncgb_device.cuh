@@ -135,13 +135,19 @@ namespace ncgb_dev {
 
   // ---- cross-sections ---------------------------------------------------------
 
-  // NCElIncXS.cc:34-54
+  // NCElIncXS.cc:34-54.  Fast (mixed-precision mode): the expm1 branch in
+  // FP32 (relative error ~1e-7).
+  template<bool Fast>
   __device__ __forceinline__ double oneMinusExpMtDivT( double t )
   {
     if ( t < 0.01 )
       return ( 1 + t * ( -0.5 + t * 0.16666666666666666666666666666666666666666667 * ( 1. - 0.25 * t ) ) );
     if ( t > 24.0 )
       return 1.0 / t;
+    if ( Fast ) {
+      const float tf = (float)( -t );
+      return (double)( expm1f( tf ) / tf );
+    }
     t = -t;
     return expm1( t ) / t;
   }
@@ -150,12 +156,13 @@ namespace ncgb_dev {
   constexpr double kElIncMu = 8.0 * 9.86960440108935861883449099987615113531369941 * 12.22430978582345950656;
 
   // ElIncXS::evaluate (NCElIncXS.cc:117-128)
+  template<bool Fast>
   __device__ __forceinline__ double elincXS( const ncgb_elinc_view& v, double ekin )
   {
     const double e = kElIncXS * ekin;
     double xs = 0.0;
     for ( int i = 0; i < v.n && i < NCGB_MAX_ELINC; ++i )
-      xs += v.sigma[i] * oneMinusExpMtDivT( v.msd[i] * e );
+      xs += v.sigma[i] * oneMinusExpMtDivT<Fast>( v.msd[i] * e );
     return xs;
   }
 
@@ -206,13 +213,14 @@ namespace ncgb_dev {
     return xs * s.internal_scale;
   }
 
+  template<bool Fast>
   __device__ __forceinline__ double compXS( const ncgb_comp_view& c, double ekin )
   {
     if ( !contains( c.elow, c.ehigh, ekin ) )
       return 0.0;
     int64_t dummy;
     switch ( c.type ) {
-      case NCGB_COMP_ELINC: return elincXS( c.elinc, ekin );
+      case NCGB_COMP_ELINC: return elincXS<Fast>( c.elinc, ekin );
       case NCGB_COMP_BRAGG: return braggXS( c.bragg, ekin, dummy );
       case NCGB_COMP_SAB: return sabXS( c.sab, ekin );
       case NCGB_COMP_FREEGAS: return c.fg.sigma_free * freeGasShape( c.fg.ca * ekin );
@@ -225,7 +233,7 @@ namespace ncgb_dev {
   // with the cumulative cross-sections in registers (fully unrolled).
   struct XSPick { double xs; int comp; };
 
-  template<bool Pick>
+  template<bool Pick, bool Fast>
   __device__ __forceinline__ XSPick xsAndPick( const ncgb_material_view& m, double ekin, ncgb_rng& rng )
   {
     double commul[NCGB_MAX_COMP];
@@ -233,7 +241,7 @@ namespace ncgb_dev {
 #pragma unroll
     for ( int i = 0; i < NCGB_MAX_COMP; ++i ) {
       if ( i < m.ncomp )
-        tot += m.comp[i].scale * compXS( m.comp[i], ekin );
+        tot += m.comp[i].scale * compXS<Fast>( m.comp[i], ekin );
       commul[i] = tot;
     }
     XSPick r{ tot, 0 };
@@ -280,6 +288,7 @@ namespace ncgb_dev {
   // ElIncXS::sampleMuMonoAtomic, NCElIncXS.cc:81-115.  The reference's
   // rejection loop is unbounded; its acceptance is above 98% here, and the
   // cap only guards the GPU.
+  template<bool Fast>
   __device__ __noinline__ double elincMuMono( ncgb_rng& rng, double ekin, double msd, int& status )
   {
     const double a = ( kElIncMu * ekin ) * msd;
@@ -293,28 +302,37 @@ namespace ncgb_dev {
       status = NCGB_ST_LOOPCAP;
       return 1.0;
     }
+    if ( Fast ) {
+      // FP32; for a > 20, log1p(R*expm1(2a))/a - 1 = 1 + log(R)/a to within
+      // exp(-40), which also avoids FP32 overflow of expm1(2a).
+      const float r = (float)rand01( rng );
+      const float af = (float)a;
+      const float m = a > 20.0 ? 1.0f + logf( r ) / af : log1pf( r * expm1f( 2.0f * af ) ) / af - 1.0f;
+      return clampd( (double)m, -1.0, 1.0 );
+    }
     return clampd( log1p( rand01( rng ) * expm1( 2.0 * a ) ) / a - 1.0, -1.0, 1.0 );
   }
 
   // ElIncXS::EPointAnalysis::sampleMu, NCElIncXS.cc:178-191 (element picked
   // by pickRandIdxByWeight on the cumulative contributions).
+  template<bool Fast>
   __device__ __noinline__ double elincMu( const ncgb_elinc_view& v, ncgb_rng& rng, double ekin, int& status )
   {
     if ( v.n == 1 )
-      return elincMuMono( rng, ekin, v.msd[0], status );
+      return elincMuMono<Fast>( rng, ekin, v.msd[0], status );
     const double e = kElIncXS * ekin;
     double tot = 0.0;
     for ( int i = 0; i < v.n && i < NCGB_MAX_ELINC; ++i )
-      tot += v.sigma[i] * oneMinusExpMtDivT( v.msd[i] * e );
+      tot += v.sigma[i] * oneMinusExpMtDivT<Fast>( v.msd[i] * e );
     const double choice = tot * rand01( rng );
     int pick = v.n - 1;
     double c = 0.0;
     const bool linear = v.n < 5;
     for ( int i = 0; i < v.n && i < NCGB_MAX_ELINC; ++i ) {
-      c += v.sigma[i] * oneMinusExpMtDivT( v.msd[i] * e );
+      c += v.sigma[i] * oneMinusExpMtDivT<Fast>( v.msd[i] * e );
       if ( linear ? ( c > choice ) : ( c >= choice ) ) { pick = i; break; }
     }
-    return elincMuMono( rng, ekin, v.msd[pick], status );
+    return elincMuMono<Fast>( rng, ekin, v.msd[pick], status );
   }
 
   // ---- S(alpha,beta) sampling (Alg.1) -----------------------------------------------
@@ -352,13 +370,23 @@ namespace ncgb_dev {
   // a_sub_b*log(fa*exp(a*L/a_sub_b)/(fa+r*df))/L, with L = logfb-logfa, is
   // evaluated as a + (b-a)*log1p(r*df/fa)/L: the same value algebraically,
   // one transcendental instead of two, and no cancellation at small r.
+  // log1p, in FP32 in the mixed-precision mode (arguments above 1e30 stay FP64).
+  template<bool Fast>
+  __device__ __forceinline__ double log1pMode( double q )
+  {
+    if ( Fast && q < 1e30 )
+      return (double)log1pf( (float)q );
+    return log1p( q );
+  }
+
+  template<bool Fast>
   __device__ __forceinline__ double logLin( double a, double fa, double b, double fb, double rnd, double logfa, double logfb )
   {
     double df = fb - fa;
     if ( fa * fb * df != 0.0 ) {
       const double L = logfb - logfa;
       if ( ( a - b ) * L != 0.0 )
-        return a + ( b - a ) * ( log1p( rnd * df / fa ) / L );
+        return a + ( b - a ) * ( log1pMode<Fast>( rnd * df / fa ) / L );
       df = 0.0;
     }
     if ( !df )
@@ -373,6 +401,7 @@ namespace ncgb_dev {
   // divisions by the section probabilities and bin areas are multiplications
   // by tabulated reciprocals, and the middle part's log-linear in-cell
   // inversion uses the cell's tabulated ratio and slope.
+  template<bool Fast>
   __device__ __forceinline__ double sampleAlpha( const ncgb_sab_view& s, const ncgb_alpha_info* infos,
                                                  int64_t ioff, int64_t ibeta, double rp )
   {
@@ -388,12 +417,12 @@ namespace ncgb_dev {
         const double da = ldg( &info->back_alpha ) - fa;
         return fa + rp * da;
       } else if ( prob_front == 1.0 ) {
-        return logLin( fa, ldg( &info->front_sval ), ldg( &info->back_alpha ), ldg( &info->back_sval ),
+        return logLin<Fast>( fa, ldg( &info->front_sval ), ldg( &info->back_alpha ), ldg( &info->back_sval ),
                        rp, ldg( &info->front_logsval ), ldg( &info->back_logsval ) );
       } else {
         const uint32_t fi = __ldg( &info->front_idx );
         const double p2 = clampRand( rp * ldg( &info->inv_front ) );
-        return logLin( fa, ldg( &info->front_sval ), ldg( s.alpha + fi ), ldg( sab + fi ),
+        return logLin<Fast>( fa, ldg( &info->front_sval ), ldg( s.alpha + fi ), ldg( sab + fi ),
                        p2, ldg( &info->front_logsval ), ldg( logsab + fi ) );
       }
     }
@@ -413,19 +442,20 @@ namespace ncgb_dev {
       const double rr = clampRand( ( sel - ldg( cumul + a0 ) ) * ldg( &cell->inv_bin ) );
       const double slope = ldg( &cell->slope );
       if ( slope == slope )
-        return ldg( s.alpha + a0 ) + slope * log1p( rr * ldg( &cell->ratio ) );
-      return logLin( ldg( s.alpha + a0 ), ldg( sab + a0 ), ldg( s.alpha + a0 + 1 ), ldg( sab + a0 + 1 ),
+        return ldg( s.alpha + a0 ) + slope * log1pMode<Fast>( rr * ldg( &cell->ratio ) );
+      return logLin<Fast>( ldg( s.alpha + a0 ), ldg( sab + a0 ), ldg( s.alpha + a0 + 1 ), ldg( sab + a0 + 1 ),
                      rr, ldg( logsab + a0 ), ldg( logsab + a0 + 1 ) );
     }
     const uint32_t bi = __ldg( &info->back_idx );
     const double p2 = clampRand( ( rp - prob_notback ) * ldg( &info->inv_back ) );
-    return logLin( ldg( s.alpha + bi ), ldg( sab + bi ), ldg( &info->back_alpha ), ldg( &info->back_sval ),
+    return logLin<Fast>( ldg( s.alpha + bi ), ldg( sab + bi ), ldg( &info->back_alpha ), ldg( &info->back_sval ),
                    p2, ldg( logsab + bi ), ldg( &info->back_logsval ) );
   }
 
   // First beta bin with a kinematic endpoint (NCSABSamplerModels.cc:69-116):
   // beta uniform in the bin, alpha from the first row, up to 30 tries.
   // Returns 1 if (alpha, beta) is accepted, 0 if the attempt is rejected.
+  template<bool Fast>
   __device__ __noinline__ int alg1FirstBin( const ncgb_sab_view& s, const ncgb_alpha_info* infos, int64_t ioff,
                                             double fbkep, double b1, double x, ncgb_rng& rng,
                                             double& alpha_out, double& beta_out )
@@ -440,7 +470,7 @@ namespace ncgb_dev {
       beta = maxd( fbkep, b0 + delta_beta * rand01( rng ) );
       if ( beta < -x )
         break;
-      alphaval = sampleAlpha( s, infos, ioff, ioff, rand01( rng ) );
+      alphaval = sampleAlpha<Fast>( s, infos, ioff, ioff, rand01( rng ) );
       const ALim al = alphaLimits( -fbkep, beta );
       if ( inInterval( al.lo, al.hi, alphaval ) )
         break;
@@ -463,6 +493,60 @@ namespace ncgb_dev {
   // One attempt of SABSamplerAtE_Alg1::sampleAlphaBeta's loop
   // (NCSABSamplerModels.cc:59-148) at energy-grid point ie, sampling energy
   // x = E/kT.  Returns 1 with (alpha, beta) on acceptance, 0 on rejection.
+  // Order-preserving integer key of a double (any sign): compares on the
+  // integer pipe.
+  __device__ __forceinline__ long long okey( double v )
+  {
+    const long long b = __double_as_longlong( v );
+    return b ^ ( ( b >> 63 ) & 0x7fffffffffffffffLL );
+  }
+
+  // Learned proposal for the regular beta range of sampler ie (tables built by
+  // ncgb_proposal.cc): an interval from the alias table, beta uniform in it,
+  // accepted with probability y(beta)/env.  Returns 1 with (beta, ibs), or 0
+  // if 1000 proposals were all rejected.
+  __device__ __forceinline__ int lpBeta( const ncgb_sab_view& s, int64_t ie, const double* bx, const double* by,
+                                         ncgb_rng& rng, double& beta, int64_t& ibs )
+  {
+    const ncgb_lp_cell* cells = s.lp_cell + ie * ( NCGB_LP_K + 1 );
+    for ( int tries = 0; tries < 1000; ++tries ) {
+      const double t = rand01( rng ) * (double)NCGB_LP_K;
+      int j = (int)t;
+      if ( j > NCGB_LP_K - 1 )
+        j = NCGB_LP_K - 1;
+      const float fr = (float)( t - (double)j );
+      const int k = ( fr < __ldg( &cells[j].aprob ) ) ? j : __ldg( &cells[j].alias );
+      const double q0 = ldg( &cells[k].q ), q1 = ldg( &cells[k + 1].q );
+      const double b = fma( rand01( rng ), q1 - q0, q0 );
+      // largest bin j in [bin_k, bin_k+1] with bx[j] <= b
+      int64_t lo = __ldg( &cells[k].bin ), hi = __ldg( &cells[k + 1].bin );
+      const long long kb = okey( b );
+      while ( lo < hi ) {
+        const int64_t mid = ( lo + hi + 1 ) >> 1;
+        if ( okey( ldg( bx + mid ) ) <= kb )
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      const double x0 = ldg( bx + lo );
+      const float dx = (float)( ldg( bx + lo + 1 ) - x0 );
+      const float tt = dx > 0.0f ? (float)( b - x0 ) / dx : 0.0f;
+      const float y0 = (float)ldg( by + lo );
+      const float y = fmaf( (float)ldg( by + lo + 1 ) - y0, tt, y0 );
+      if ( (float)rand01( rng ) * __ldg( &cells[k].env ) < y ) {
+        beta = b;
+        ibs = lo;
+        return 1;
+      }
+    }
+    return 0;
+  }
+
+  // One attempt of SABSamplerAtE_Alg1::sampleAlphaBeta.  Returns 1 with
+  // (alpha, beta) accepted, 0 if the attempt is rejected, -1 if the learned
+  // proposal hit its cap.  Learned: the beta percentile inversion of samplers
+  // with an enabled learned proposal is replaced by lpBeta (same distribution).
+  template<bool Fast, bool Learned>
   __device__ __forceinline__ int alg1Attempt( const ncgb_sab_view& s, int64_t ie, double x, ncgb_rng& rng,
                                               double& alpha_out, double& beta_out )
   {
@@ -472,10 +556,20 @@ namespace ncgb_dev {
     const ncgb_alpha_info* infos = s.info + off;
     const int64_t ioff = __ldg( s.smp_ibetaoffset + ie );
     int64_t ibs;
-    const double beta = percentile( bx, s.bcdf + off, s.bbin + off, nbs, rand01( rng ), ibs );
+    double beta;
     const double fbkep = ldg( s.smp_fbkep + ie );
-    if ( ibs == 0 && fbkep <= 0.0 )
-      return alg1FirstBin( s, infos, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+    if ( Learned && s.lp_hdr && __ldg( &s.lp_hdr[ie].enabled ) ) {
+      // the special first bin keeps its probability bcdf[1]; the regular
+      // range is drawn from the learned proposal
+      if ( rand01( rng ) <= ldg( &s.lp_hdr[ie].c1 ) )
+        return alg1FirstBin<Fast>( s, infos, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+      if ( !lpBeta( s, ie, bx, s.by + off, rng, beta, ibs ) )
+        return -1;
+    } else {
+      beta = percentile( bx, s.bcdf + off, s.bbin + off, nbs, rand01( rng ), ibs );
+      if ( ibs == 0 && fbkep <= 0.0 )
+        return alg1FirstBin<Fast>( s, infos, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+    }
     if ( beta <= maxd( -x, ldg( s.beta ) ) )
       return 0;
     const double rp = rand01( rng );
@@ -483,8 +577,8 @@ namespace ncgb_dev {
     if ( ibeta < 1 )
       return 0; // cannot happen (beta above the beta grid front); keeps indices in bounds
     const double bl = ldg( s.beta + ibeta - 1 );
-    const double alphal = sampleAlpha( s, infos, ioff, ibeta - 1, rp );
-    const double alphah = sampleAlpha( s, infos, ioff, ibeta, rp );
+    const double alphal = sampleAlpha<Fast>( s, infos, ioff, ibeta - 1, rp );
+    const double alphah = sampleAlpha<Fast>( s, infos, ioff, ibeta, rp );
     const double alpha = alphal + ( alphah - alphal ) * ( ( beta - bl ) * ldg( s.inv_dbeta + ibeta - 1 ) );
     const ALim al = alphaLimits( x, beta );
     if ( inInterval( al.lo, al.hi, alpha ) ) {
@@ -557,16 +651,22 @@ namespace ncgb_dev {
   }
 
   // One step of the flattened loops.  Returns -1 to continue, NCGB_ST_OK when
-  // (ef, mu) are final, or an error status.
-  __device__ __forceinline__ int sabStep( const ncgb_sab_view& s, SABLane& L, ncgb_rng& rng, double& ef, double& mu )
+  // (alpha, beta) are final, or an error status.
+  template<bool Fast, bool Learned>
+  __device__ __forceinline__ int sabStepAB( const ncgb_sab_view& s, SABLane& L, ncgb_rng& rng, double& alpha,
+                                            double& beta )
   {
-    double alpha = 0.0, beta = 0.0;
+    alpha = 0.0;
+    beta = 0.0;
     if ( L.preset ) {
       alpha = L.pre_alpha;
       beta = L.pre_beta;
     } else {
       if ( __ldg( s.smp_kind + L.ie ) != 0 ) {
-        if ( !alg1Attempt( s, L.ie, L.xsamp, rng, alpha, beta ) ) {
+        const int a = alg1Attempt<Fast, Learned>( s, L.ie, L.xsamp, rng, alpha, beta );
+        if ( a < 0 )
+          return NCGB_ST_LOOPCAP;
+        if ( a == 0 ) {
           if ( ++L.inner >= 100 )
             return NCGB_ST_LOOPCAP;
           return -1;
@@ -591,6 +691,17 @@ namespace ncgb_dev {
         return -1;
       }
     }
+    return NCGB_ST_OK;
+  }
+
+  // sabStepAB, then (alpha, beta) -> (E', mu).
+  template<bool Fast, bool Learned>
+  __device__ __forceinline__ int sabStep( const ncgb_sab_view& s, SABLane& L, ncgb_rng& rng, double& ef, double& mu )
+  {
+    double alpha, beta;
+    const int st = sabStepAB<Fast, Learned>( s, L, rng, alpha, beta );
+    if ( st != NCGB_ST_OK )
+      return st;
     // SABSampler::sampleDeltaEMu (NCSABSampler.cc:229-236), SABScatter
     // (NCSABScatter.cc:92-101), with the neutron's own energy
     double deltaE, muv;

@@ -103,7 +103,7 @@ namespace {
   }
 
   // ---- phase 1: cross-section, pick, short samplers, SAB queue ----------------
-  template<class Src>
+  template<class Src, bool Fast>
   __global__ void __launch_bounds__(512)
   k_pick( const __grid_constant__ Src src, const ncgb::Batch b )
   {
@@ -122,7 +122,7 @@ namespace {
         store( b.out_xs, b.out_f32, o, 0.0 );
         writeScatter( b, o, e, NCGB_ST_OK, e, 1.0 );
       } else {
-        const XSPick p = xsAndPick<true>( m, e, rng );
+        const XSPick p = xsAndPick<true, Fast>( m, e, rng );
         store( b.out_xs, b.out_f32, o, p.xs );
         const ncgb_comp_view& c = m.comp[p.comp];
         int st = NCGB_ST_OK;
@@ -137,7 +137,7 @@ namespace {
             break;
           }
           case NCGB_COMP_ELINC:
-            mu = elincMu( c.elinc, rng, e, st );
+            mu = elincMu<Fast>( c.elinc, rng, e, st );
             break;
           case NCGB_COMP_SAB:
           case NCGB_COMP_FREEGAS:
@@ -176,7 +176,7 @@ namespace {
   }
 
   // ---- phase 2: persistent S(alpha,beta) sampling ---------------------------
-  template<class Src>
+  template<class Src, bool Fast, bool Learned>
   __global__ void __launch_bounds__(256, 4)
   k_sab( const __grid_constant__ Src src, const ncgb::Batch b )
   {
@@ -189,8 +189,8 @@ namespace {
     SABLane L;
     ncgb_rng rng;
     ncgb_rng_init( &rng, 0, 0, 0, 0 );
-    // Bounded: every claimed neutron finishes within 100 x 100 Alg.1 attempts,
-    // and claims stop at qcount.
+    // Bounded: every claimed neutron finishes within 100 x 100 Alg.1 attempts
+    // (each with at most 1000 learned-proposal draws), and claims stop at qcount.
     for (;;) {
       const unsigned need = __ballot_sync( FULL, !has && !done );
       if ( need ) {
@@ -229,7 +229,7 @@ namespace {
         break;
       if ( has ) {
         double ef = 0.0, mu = 0.0;
-        const int st = sabStep( src.mat( q.mat ).comp[q.comp].sab, L, rng, ef, mu );
+        const int st = sabStep<Fast, Learned>( src.mat( q.mat ).comp[q.comp].sab, L, rng, ef, mu );
         if ( st >= 0 ) {
           writeScatter( b, q.idx, q.ekin, st, ef, mu );
           has = false;
@@ -238,9 +238,40 @@ namespace {
     }
   }
 
+  // ---- (alpha, beta) of one S(alpha,beta) component ----------------------------
+  // SABSampler::sampleAlphaBeta (NCSABSampler.cc:158-227) per neutron, for the
+  // proposal's training set and its tests: out_a = alpha, out_b = beta.
+  template<bool Fast, bool Learned>
+  __global__ void __launch_bounds__(256)
+  k_sab_ab( const __grid_constant__ ncgb_material_view m, int comp, const ncgb::Batch b )
+  {
+    const ncgb_comp_view& c = m.comp[comp];
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for ( uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < b.n_ekin; i += stride ) {
+      const double e = loadE( b, i );
+      ncgb_rng rng;
+      ncgb_rng_init( &rng, b.seed, (uint32_t)( b.index_offset + i ), b.callseq, b.stream );
+      double alpha = 0.0, beta = 0.0;
+      SABLane L;
+      int st = sabBegin( c.sab, m.fg_erfc_table, e, rng, L );
+      if ( st == NCGB_ST_OK ) {
+        do {
+          st = sabStepAB<Fast, Learned>( c.sab, L, rng, alpha, beta );
+        } while ( st < 0 );
+      }
+      static_cast<double*>( b.out_a )[i] = alpha;
+      static_cast<double*>( b.out_b )[i] = beta;
+      if ( b.status )
+        b.status[i] = st;
+      if ( st != NCGB_ST_OK )
+        atomicAdd( &b.work->nfail, 1ull );
+    }
+  }
+
   // ---- cross-sections only ------------------------------------------------------
   // results[r*n_ekin+i] = xs(ekin[i]) for r < repeat (ncrystal.cc:1107-1141
   // writes the same value for every repeat).
+  template<bool Fast>
   __global__ void __launch_bounds__(256)
   k_xs( const __grid_constant__ ncgb_material_view m, const ncgb::Batch b, uint64_t repeat )
   {
@@ -251,7 +282,7 @@ namespace {
       if ( contains( m.dom_elow, m.dom_ehigh, e ) ) {
         ncgb_rng dummy;
         ncgb_rng_init( &dummy, 0, 0, 0, 0 );
-        xs = xsAndPick<false>( m, e, dummy ).xs;
+        xs = xsAndPick<false, Fast>( m, e, dummy ).xs;
       }
       for ( uint64_t r = 0; r < repeat; ++r )
         store( b.out_xs, b.out_f32, r * b.n_ekin + i, xs );
@@ -275,7 +306,7 @@ namespace {
   {
     static int bps = 0;
     if ( !bps ) {
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_sab<Src>, 256, 0 );
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_sab<Src, false, false>, 256, 0 );
       if ( bps <= 0 ) bps = 1;
     }
     return bps;
@@ -314,7 +345,10 @@ namespace {
       cudaEventRecord( ev.a, s );
     }
     const int pb = ( cfg.pick_block == 128 || cfg.pick_block == 512 ) ? cfg.pick_block : 256;
-    k_pick<Src><<<gridFor( b.n_out, pb ), pb, 0, s>>>( src, b );
+    if ( b.fast )
+      k_pick<Src, true><<<gridFor( b.n_out, pb ), pb, 0, s>>>( src, b );
+    else
+      k_pick<Src, false><<<gridFor( b.n_out, pb ), pb, 0, s>>>( src, b );
     e = cudaGetLastError();
     if ( e != cudaSuccess )
       return e;
@@ -322,7 +356,18 @@ namespace {
       cudaEventRecord( ev.b, s );
     const int maxb = sabBlocksPerSM<Src>();
     const int mult = ( cfg.sab_blocks_per_sm > 0 && cfg.sab_blocks_per_sm < maxb ) ? cfg.sab_blocks_per_sm : maxb;
-    k_sab<Src><<<numSMs() * mult, 256, 0, s>>>( src, b );
+    const int grid = numSMs() * mult;
+    if ( b.fast ) {
+      if ( b.learned )
+        k_sab<Src, true, true><<<grid, 256, 0, s>>>( src, b );
+      else
+        k_sab<Src, true, false><<<grid, 256, 0, s>>>( src, b );
+    } else {
+      if ( b.learned )
+        k_sab<Src, false, true><<<grid, 256, 0, s>>>( src, b );
+      else
+        k_sab<Src, false, false><<<grid, 256, 0, s>>>( src, b );
+    }
     e = cudaGetLastError();
     if ( timing ) {
       cudaEventRecord( ev.c, s );
@@ -361,7 +406,29 @@ namespace ncgb {
   {
     if ( b.n_ekin == 0 || repeat == 0 )
       return cudaSuccess;
-    k_xs<<<gridFor( b.n_ekin, 256 ), 256, 0, s>>>( m, b, repeat );
+    if ( b.fast )
+      k_xs<true><<<gridFor( b.n_ekin, 256 ), 256, 0, s>>>( m, b, repeat );
+    else
+      k_xs<false><<<gridFor( b.n_ekin, 256 ), 256, 0, s>>>( m, b, repeat );
+    return cudaGetLastError();
+  }
+
+  cudaError_t launchSabAB( const ncgb_material_view& m, int comp, const Batch& b, cudaStream_t s )
+  {
+    if ( b.n_ekin == 0 )
+      return cudaSuccess;
+    const int grid = gridFor( b.n_ekin, 256 );
+    if ( b.fast ) {
+      if ( b.learned )
+        k_sab_ab<true, true><<<grid, 256, 0, s>>>( m, comp, b );
+      else
+        k_sab_ab<true, false><<<grid, 256, 0, s>>>( m, comp, b );
+    } else {
+      if ( b.learned )
+        k_sab_ab<false, true><<<grid, 256, 0, s>>>( m, comp, b );
+      else
+        k_sab_ab<false, false><<<grid, 256, 0, s>>>( m, comp, b );
+    }
     return cudaGetLastError();
   }
 

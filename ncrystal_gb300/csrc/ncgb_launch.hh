@@ -51,6 +51,9 @@ namespace ncgb {
     uint64_t seed;
     uint32_t callseq, stream, index_offset;
     int mode;          // 0: out_a = E', out_b = mu;  1: out_a = acos(mu), out_b = E'-E
+    int fast;          // mixed-precision mode (FP32 transcendentals outside the
+                       // beta-CDF inversion and the kinematics)
+    int learned;       // learned beta proposal where a component has one attached
     void* out_xs;      // may be null
     void* out_a;       // may be null
     void* out_b;       // may be null
@@ -65,6 +68,10 @@ namespace ncgb {
   cudaError_t launchScatterMulti( const MatSlot* d_slots, const int64_t* d_offsets, int nmat,
                                   const Batch& b, const LaunchCfg& cfg, cudaStream_t s );
   int maxSabBlocksPerSM();
+  // (alpha, beta) of component 'comp' per neutron: out_a = alpha, out_b = beta;
+  // neutron i uses stream (seed, index_offset + i, callseq, stream); failures
+  // counted in work->nfail.
+  cudaError_t launchSabAB( const ncgb_material_view& m, int comp, const Batch& b, cudaStream_t s );
   cudaError_t launchXS( const ncgb_material_view& m, const Batch& b, uint64_t repeat, cudaStream_t s );
   int scatterLaunchesPerBatch();
   void setPhaseTiming( bool on );

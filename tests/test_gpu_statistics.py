@@ -21,13 +21,15 @@ pytestmark = pytest.mark.gpu
 
 N = 10 ** 8
 CASES = [(W.PE293, 0.001), (W.PE293, 0.0253), (W.PE293, 0.5), (W.AL2O3, 0.0253), (W.AL2O3, 0.2)]
-NTESTS = 3 * len(CASES)
+# the mixed-precision mode must sample the same distributions
+CASES_MIXED = [(W.PE293, 0.0253), (W.AL2O3, 0.0253)]
+NTESTS = 3 * (len(CASES) + len(CASES_MIXED))
 ALPHA = 0.01 / NTESTS
 
 
-def gpu_samples(cfg, e0, n, seed):
+def gpu_samples(cfg, e0, n, seed, mode="exact"):
     import torch
-    sc = NC.createScatter(cfg, seed=seed)
+    sc = NC.createScatter(cfg, seed=seed).set_mode(mode)
     e = torch.full((n,), e0, dtype=torch.float64, device="cuda")
     ef = torch.empty_like(e)
     mu = torch.empty_like(e)
@@ -73,11 +75,14 @@ def ks_two_sample_large(x, y, nsub=2_000_000, seed=0):
     return ks_2samp(x[r.integers(0, len(x), nsub)], y[r.integers(0, len(y), nsub)]).pvalue
 
 
-@pytest.mark.parametrize("cfg,e0", CASES, ids=["%s@%g" % (c.split(".")[0], e) for c, e in CASES])
-def test_gpu_vs_oracle_distributions(cfg, e0):
+ALL = [(c, e, "exact") for c, e in CASES] + [(c, e, "mixed") for c, e in CASES_MIXED]
+
+
+@pytest.mark.parametrize("cfg,e0,mode", ALL, ids=["%s@%g-%s" % (c.split(".")[0], e, m) for c, e, m in ALL])
+def test_gpu_vs_oracle_distributions(cfg, e0, mode):
     pytest.importorskip("scipy")
     bundle_path(cfg)
-    gef, gmu = gpu_samples(cfg, e0, N, seed=1001)
+    gef, gmu = gpu_samples(cfg, e0, N, seed=1001, mode=mode)
     oef, omu = oracle_samples(cfg, e0, N, seed=2002)
     # 2D histogram in (log E'/E, mu): 60 x 50 bins, edges from the pooled range
     lg = np.log(np.maximum(gef, 1e-30) / e0)
