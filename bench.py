@@ -73,8 +73,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="al2o3_large",
+    ap.add_argument("--workload", default="pe",
                     choices=["al2o3_large", "al_small", "pe", "crystal_batch"])
+    ap.add_argument("--sampler", default="auto", choices=["auto", "plain", "learned"],
+                    help="S(alpha,beta) beta sampling: plain percentile inversion, or the learned proposal "
+                         "(trained on the GPU before timing; the plain sampler is timed beside it). "
+                         "auto: learned for the polyethylene workload, plain otherwise")
+    ap.add_argument("--train-samples", type=int, default=1 << 26)
+    ap.add_argument("--train-steps", type=int, default=6000)
     ap.add_argument("--mode", default="exact", choices=["exact", "mixed"],
                     help="arithmetic mode of the GPU path (mixed: FP32 incoherent-elastic exponentials "
                          "and alpha inversion, FP64 elsewhere)")
@@ -220,7 +226,9 @@ def dist_env():
 def config_of(args, wl, world):
     cfgs = wl["cfgs"]
     return {"workload": args.workload, "cfg": cfgs[0] if len(cfgs) == 1 else "%d instances" % len(cfgs),
-            "neutrons_per_gpu": int(sum(wl["counts"])), "io": wl["io"], "sampler": "plain (Alg.1 tables)",
+            "neutrons_per_gpu": int(sum(wl["counts"])), "io": wl["io"],
+            "sampler": "plain (Alg.1 tables)" if getattr(args, "sampler", "plain") != "learned"
+            else "learned beta proposal (exact rejection), plain Alg.1 elsewhere",
             "mode": getattr(args, "mode", "exact"), "parallelism": "replicas%d" % world}
 
 
@@ -278,6 +286,9 @@ class SingleRunner:
         self.sc.scatter_device(self.d_e, self.d_xs, self.d_ef, self.d_mu, None, stream=stream)
 
     timed_step = step
+
+    def set_sampler(self, sampler):
+        self.sc.set_sampler(sampler)
 
     def e2e_step(self):
         self.sc.xs_scatter_host_ptr(self.h_e.data_ptr(), self.n, self.h_xs.data_ptr(), self.h_ef.data_ptr(),
@@ -358,10 +369,29 @@ def run_gb300(args):
     import ncrystal_gb300 as NC
 
     wl = workload(args.workload, rank)
+    if args.sampler == "auto":
+        args.sampler = "learned" if args.workload == "pe" else "plain"
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     R = (BatchRunner if len(wl["cfgs"]) > 1 else SingleRunner)(NC, torch, wl, dev, 0xB0057 + 977 * rank, args.mode)
     n = R.n
+    learned = None
+    if args.sampler == "learned":
+        # Train the proposal networks on the GPU (untimed), attach them.
+        import ncrystal_gb300.learn as LR
+        if len(wl["cfgs"]) != 1 or not wl["cfgs"][0].startswith("Polyethylene_CH2.ncmat"):
+            raise SystemExit("bench: the learned proposal is trained for polyethylene workloads")
+        t0 = time.perf_counter()
+        nets, infos = LR.train_proposals(n_total=args.train_samples, steps=args.train_steps, seed=3 + rank)
+        torch.cuda.synchronize()
+        acc = LR.attach(R.sc, nets)
+        learned = {"train_wall_s": time.perf_counter() - t0, "mean_envelope_acceptance": acc,
+                   "components": {str(c): {k: v for k, v in i.items() if k != "loss_trace"}
+                                  for c, i in infos.items()},
+                   "final_loss": {str(c): i["loss_trace"][-1] if i["loss_trace"] else None
+                                  for c, i in infos.items()},
+                   "network": "4x128 hidden, BF16 mma.sync + FP32 accumulation, trained by the library's kernels"}
+        R.set_sampler("learned")
     esz = 4 if R.f32 else 8
     io_bytes = 4 * esz * n  # energies in, xs / E' / mu out
 
@@ -412,6 +442,30 @@ def run_gb300(args):
         ms = float(t.item())
     ms_per_step = ms / args.steps
     value = world * n * args.steps / (ms / 1e3)
+
+    plain = None
+    if learned is not None:
+        # the plain sampler on the same handle, same inputs, same timing rules
+        R.set_sampler("plain")
+        for _ in range(args.warmup):
+            R.timed_step(stream)
+        barrier()
+        pev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        for a, b in pev:
+            if flush is not None:
+                flush.fill_(1.0)
+            a.record(stream)
+            R.timed_step(stream)
+            b.record(stream)
+        barrier()
+        pms = sum(a.elapsed_time(b) for a, b in pev)
+        if dist:
+            t = torch.tensor([pms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            pms = float(t.item())
+        plain = {"value": world * n * args.steps / (pms / 1e3), "ms_per_step": pms / args.steps}
+        R.set_sampler("learned")
     peak, peak_kind = measured_peaks()
     # Algorithmic bytes per launch (inputs read + results written, nothing
     # else): k_pick reads every energy, writes every xs and the (E', mu) of the
@@ -459,6 +513,10 @@ def run_gb300(args):
         cfgd["inputs"] = "device-resident, not re-read from host"
         if len(wl["cfgs"]) > 1:
             cfgd["timed_launch"] = "CUDA graph replay of the autotuned batch launch"
+        if learned is not None:
+            cfgd["learned"] = learned
+            cfgd["plain_sampler"] = plain
+            cfgd["learned_vs_plain"] = value / plain["value"]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,

@@ -8,9 +8,13 @@
  *
  *   key      = (seed & 0xffffffff, seed >> 32)
  *   counter  = (block, neutron index, call sequence number, stream index)
- *   draw j   = block j/2, output words (x0,x1) for even j and (x2,x3) for odd j,
+ *   words    = the four 32-bit outputs (x0,x1,x2,x3) of each block, in order
+ *   double   = the next two words (a new block when fewer than two are left),
  *              u = ((x_lo | x_hi << 32) >> 11) + 1) * 2^-53, in (0,1]
+ *   32 bits  = the next word (used by the learned beta proposal only)
  *
+ * A stream of doubles only thus takes (x0,x1) and (x2,x3) of block 0, then of
+ * block 1, and so on.
  * The same definition is used by the CUDA kernels, by the CPU oracle and by the
  * harness that drives the reference library with identical numbers, so that a
  * neutron's draws are the same on all three.  Header-only, plain C99 (plus
@@ -31,9 +35,9 @@ typedef struct {
   uint32_t key0, key1;    /* from the seed */
   uint32_t ctr1, ctr2, ctr3; /* neutron index, call sequence, stream index */
   uint32_t block;         /* next block to generate */
-  uint32_t have;          /* 0, 1 or 2 cached doubles */
+  uint32_t have;          /* words of the current block not yet used (0..4) */
   uint32_t pad;
-  uint64_t cache[2];
+  uint32_t word[4];
 } ncgb_rng;
 
 NCGB_HD void ncgb_mulhilo32( uint32_t a, uint32_t b, uint32_t* hi, uint32_t* lo )
@@ -73,24 +77,37 @@ NCGB_HD void ncgb_rng_init( ncgb_rng* r, uint64_t seed, uint32_t neutron,
   r->block = 0;
   r->have = 0;
   r->pad = 0;
-  r->cache[0] = r->cache[1] = 0;
+  r->word[0] = r->word[1] = r->word[2] = r->word[3] = 0;
 }
 
-/* Uniform double in (0,1]. */
+NCGB_HD void ncgb_rng_refill( ncgb_rng* r )
+{
+  uint32_t ctr[4] = { r->block, r->ctr1, r->ctr2, r->ctr3 };
+  ncgb_philox4x32_10( ctr, r->key0, r->key1, r->word );
+  r->block += 1;
+  r->have = 4;
+}
+
 NCGB_HD double ncgb_rng_generate( ncgb_rng* r )
 {
-  if ( r->have == 0 ) {
-    uint32_t ctr[4] = { r->block, r->ctr1, r->ctr2, r->ctr3 };
-    uint32_t o[4];
-    ncgb_philox4x32_10( ctr, r->key0, r->key1, o );
-    r->block += 1;
-    r->cache[0] = (uint64_t)o[0] | ( (uint64_t)o[1] << 32 );
-    r->cache[1] = (uint64_t)o[2] | ( (uint64_t)o[3] << 32 );
-    r->have = 2;
-  }
-  uint64_t bits = r->cache[2 - r->have];
-  r->have -= 1;
+  if ( r->have < 2 )
+    ncgb_rng_refill( r );
+  const uint32_t i = 4 - r->have;
+  const uint64_t bits = (uint64_t)r->word[i] | ( (uint64_t)r->word[i + 1] << 32 );
+  r->have -= 2;
   return (double)( ( bits >> 11 ) + 1 ) * ( 1.0 / 9007199254740992.0 );
 }
+
+NCGB_HD uint32_t ncgb_rng_u32( ncgb_rng* r )
+{
+  if ( r->have == 0 )
+    ncgb_rng_refill( r );
+  const uint32_t w = r->word[4 - r->have];
+  r->have -= 1;
+  return w;
+}
+
+/* Doubles drawn so far by a stream that drew doubles only. */
+NCGB_HD uint32_t ncgb_rng_ndoubles( const ncgb_rng* r ) { return ( 4 * r->block - r->have ) / 2; }
 
 #endif

@@ -61,23 +61,39 @@ typedef struct {
 } ncgb_beta_bin;
 
 /* Learned beta proposal of one sampler (egrid point): a partition of the
- * sampler's regular beta range into NCGB_LP_K intervals with knots placed by
- * a trained network, a piecewise-constant envelope (the maximum of the
- * sampler's piecewise-linear beta density on each interval) and an alias
- * table over the interval masses.  No reference counterpart. */
-#define NCGB_LP_K 63
+ * sampler's regular beta range into NCGB_LP_K intervals placed from a trained
+ * network's quantiles, a piecewise-constant envelope (the maximum of the
+ * sampler's piecewise-linear beta density on each interval), an alias table
+ * over the interval masses, and per interval the density's linear pieces in
+ * the coordinate of the 32-bit draw that places beta in the interval.  No
+ * reference counterpart. */
+#define NCGB_LP_K 126
+#define NCGB_LP_NKNOTS 62   /* network quantile knots per egrid point */
 typedef struct {
   double c1;        /* probability of the special first beta bin (0 if none) */
+  uint32_t c1_thr;  /* the first bin is taken when a 32-bit draw is below this */
   float accept;     /* expected acceptance of the envelope */
   int32_t enabled;  /* 0: the plain percentile inversion is used */
+  int32_t pad;
 } ncgb_lp_hdr;
 typedef struct {
-  double q;         /* knot k (interval k is [q_k, q_k+1]) */
+  float aprob;      /* alias table: probability of keeping slot k */
+  int32_t alias;    /* alias table: the other interval of slot k */
+} ncgb_lp_slot;
+typedef struct {
+  double q;         /* interval k: beta = q + (2w+1) h for a 32-bit draw w */
+  double h;         /* (interval width) * 2^-33 */
   float env;        /* envelope height on interval k */
-  float aprob;      /* alias table: keep probability of slot k */
-  int32_t bin;      /* beta-bin j of the sampler with bx[j] <= q_k < bx[j+1] */
-  int32_t alias;    /* alias table: other interval of slot k */
+  int32_t seg_lo;   /* its linear pieces: lp_seg[seg_lo .. seg_lo + seg_n) */
+  int32_t seg_n;
+  int32_t pad;
 } ncgb_lp_cell;
+typedef struct {
+  uint32_t w0;      /* first draw w of the piece (beta(w0) >= bx[bin]) */
+  float y0;         /* density at w0 */
+  float slope;      /* density change per unit of w */
+  int32_t bin;      /* the sampler's beta bin of the piece */
+} ncgb_lp_seg;
 
 /* One alpha cell [alpha_i, alpha_i+1] of a beta row: the constants of the
  * log-linear in-cell inversion (NCSABUtils.hh:282-304) for the middle part of
@@ -136,9 +152,12 @@ typedef struct {
   const double* inv_dbeta;        /* [nb] 1/(beta[i+1]-beta[i]) */
   const ncgb_beta_bin* bbin;      /* [offset + j]: bin j of a sampler, j < nbeta-1 */
   const ncgb_alpha_cell* acell;   /* [nb*na] */
-  /* learned beta proposal (NULL: none attached): lp_hdr[ne], lp_cell[ne*(NCGB_LP_K+1)] */
+  /* learned beta proposal (NULL: none attached): lp_hdr[ne], lp_slot[ne*NCGB_LP_K],
+   * lp_cell[ne*NCGB_LP_K], lp_seg[...] */
   const ncgb_lp_hdr* lp_hdr;
+  const ncgb_lp_slot* lp_slot;
   const ncgb_lp_cell* lp_cell;
+  const ncgb_lp_seg* lp_seg;
 } ncgb_sab_view;
 
 typedef struct {

@@ -237,6 +237,81 @@ int ncgb_batch_set_mode( ncgb_batch_t, int mode );
 void ncgb_batch_xs_scatter_many( ncgb_batch_t, const double* ekin, const int64_t* offsets, unsigned long n,
                                  double* xs, double* ekin_final, double* mu );
 
+/* ===================== Part 3: learned beta proposal (no reference counterpart)
+ *
+ * A small network (4 hidden layers of 128, BF16 tensor-core GEMMs with FP32
+ * accumulation, trained on the GPU by this library's own forward and backward
+ * kernels) predicts, from (log E, T), 62 quantile knots of the beta
+ * distribution of an S(alpha,beta) component.  Attached to a component, the
+ * knots of each sampler energy (egrid point) become a piecewise-constant
+ * envelope over the sampler's own piecewise-linear beta density; beta is then
+ * drawn by exact rejection from that envelope instead of by the percentile
+ * inversion.  The sampled distribution is unchanged (the first beta bin's
+ * special treatment and the alpha sampling stay as in the plain sampler);
+ * egrid points outside the network's trained (E, T) range or with an envelope
+ * acceptance below 'min_accept' keep the plain inversion. */
+#define NCGB_SAMPLER_PLAIN 0
+#define NCGB_SAMPLER_LEARNED 1
+/* Which sampler a handle (or a batch) uses; clones inherit it.  LEARNED uses
+ * the proposals attached to the handle's material, PLAIN ignores them. */
+int ncgb_set_sampler( ncrystal_scatter_t, int sampler );
+int ncgb_get_sampler( ncrystal_scatter_t );
+int ncgb_batch_set_sampler( ncgb_batch_t, int sampler );
+
+/* Composition of a handle's material: number of components, temperature (K),
+ * and per component its type (NCGB_COMP_*), scale and egrid size (SAB). */
+int ncgb_material_info( ncrystal_scatter_t, int* ncomp, double* temperature );
+int ncgb_component_info( ncrystal_scatter_t, int comp, int* type, double* scale, unsigned long* ne );
+int ncgb_sab_egrid( ncrystal_scatter_t, int comp, double* egrid_out );
+
+/* (alpha, beta) sampled by S(alpha,beta) component 'comp' alone
+ * (SABSampler::sampleAlphaBeta, NCSABSampler.cc:158-227) at d_ekin[n]; the
+ * training set of the proposal.  Streams and call sequence as
+ * ncgb_scatter_device; asynchronous on 'stream'. */
+int ncgb_sab_sample_device( ncrystal_scatter_t, int comp, const double* d_ekin, unsigned long n,
+                            double* d_alpha, double* d_beta, int32_t* d_status, void* stream );
+
+typedef struct { void * internal; } ncgb_mlp_t;
+/* Network on the current device, He-uniform initial weights from 'seed'. */
+ncgb_mlp_t ncgb_mlp_create( unsigned long long seed );
+void ncgb_mlp_destroy( ncgb_mlp_t* );
+unsigned long ncgb_mlp_nparams( void );
+/* FP32 master weights, flat: W_l [in][out] row-major then b_l, l = 0..4. */
+int ncgb_mlp_get_params( ncgb_mlp_t, float* out );
+int ncgb_mlp_set_params( ncgb_mlp_t, const float* in );
+/* (E, T) range the inputs are normalised over and the network is valid in. */
+int ncgb_mlp_set_ranges( ncgb_mlp_t, double emin, double emax, double tmin, double tmax );
+/* Pinball loss and its gradient (flat layout, host array) on the first n
+ * samples (device arrays: log E, T, asinh(beta)). */
+int ncgb_mlp_gradients( ncgb_mlp_t, const float* d_loge, const float* d_temp, const float* d_target,
+                        unsigned long n, float* h_grad, float* h_loss, void* stream );
+/* Adam training: 'steps' batches drawn with replacement from n samples; the
+ * mean loss of every 'trace_every' steps is written to h_trace (optional). */
+int ncgb_mlp_train( ncgb_mlp_t, const float* d_loge, const float* d_temp, const float* d_target,
+                    unsigned long n, unsigned long steps, unsigned int batch, float lr, unsigned long long seed,
+                    float* h_trace, unsigned long trace_every, void* stream );
+/* Knots (62 asinh(beta) values per point) at n points. */
+int ncgb_mlp_knots( ncgb_mlp_t, const float* d_loge, const float* d_temp, unsigned long n, float* d_knots,
+                    void* stream );
+/* Attach the network's proposal to SAB component 'comp' of the handle's
+ * material (shared by all handles of that material; batches copy the
+ * material's tables when created).  mean_accept: mean envelope acceptance of
+ * the enabled egrid points. */
+int ncgb_attach_proposal( ncrystal_scatter_t, int comp, ncgb_mlp_t, double min_accept, double* mean_accept );
+/* Same from explicit knots[ne*62] (host, asinh(beta)), e.g. for comparisons. */
+int ncgb_attach_proposal_knots( ncrystal_scatter_t, int comp, const float* knots, double min_accept,
+                                double* mean_accept );
+int ncgb_detach_proposal( ncrystal_scatter_t, int comp );
+/* Per egrid point: envelope acceptance and whether the proposal is used. */
+int ncgb_proposal_acceptance( ncrystal_scatter_t, int comp, float* accept, int32_t* enabled );
+/* Host-only: the same tables from host material tables (ncgb_tables_load),
+ * and tables for ncgb_tables_view to carry (the CPU oracle's input). */
+int ncgb_tables_build_proposal( void* tables, int comp, const float* knots, const unsigned char* allowed,
+                                double min_accept, void* hdr_out, void* slot_out, void* cell_out, void* seg_out,
+                                unsigned long* nseg );
+int ncgb_tables_set_proposal( void* tables, int comp, const void* hdr, const void* slot, const void* cell,
+                              const void* seg, unsigned long nseg );
+
 /* Phase timing for benchmarks: while enabled, every scatter batch records
  * CUDA events on its stream before and after its two kernels (the pick /
  * cross-section pass and the S(alpha,beta) pass).  ncgb_phase_times waits for

@@ -107,6 +107,34 @@ def lib():
                                            _C.c_void_p, _C.c_void_p, _C.c_void_p]),
         "ncgb_batch_config": (_C.c_int, [_Handle, _C.POINTER(_C.c_int), _C.POINTER(_C.c_int)]),
         "ncgb_batch_set_mode": (_C.c_int, [_Handle, _C.c_int]),
+        "ncgb_batch_set_sampler": (_C.c_int, [_Handle, _C.c_int]),
+        "ncgb_set_sampler": (_C.c_int, [H, _C.c_int]),
+        "ncgb_get_sampler": (_C.c_int, [H]),
+        "ncgb_material_info": (_C.c_int, [H, _C.POINTER(_C.c_int), _dblp]),
+        "ncgb_component_info": (_C.c_int, [H, _C.c_int, _C.POINTER(_C.c_int), _dblp, _C.POINTER(_C.c_ulong)]),
+        "ncgb_sab_egrid": (_C.c_int, [H, _C.c_int, _C.c_void_p]),
+        "ncgb_sab_sample_device": (_C.c_int, [H, _C.c_int, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p,
+                                              _C.c_void_p, _C.c_void_p]),
+        "ncgb_mlp_create": (_Handle, [_C.c_ulonglong]),
+        "ncgb_mlp_destroy": (None, [_C.c_void_p]),
+        "ncgb_mlp_nparams": (_C.c_ulong, []),
+        "ncgb_mlp_get_params": (_C.c_int, [_Handle, _C.c_void_p]),
+        "ncgb_mlp_set_params": (_C.c_int, [_Handle, _C.c_void_p]),
+        "ncgb_mlp_set_ranges": (_C.c_int, [_Handle, _C.c_double, _C.c_double, _C.c_double, _C.c_double]),
+        "ncgb_mlp_gradients": (_C.c_int, [_Handle, _C.c_void_p, _C.c_void_p, _C.c_void_p, _C.c_ulong, _C.c_void_p,
+                                          _C.POINTER(_C.c_float), _C.c_void_p]),
+        "ncgb_mlp_train": (_C.c_int, [_Handle, _C.c_void_p, _C.c_void_p, _C.c_void_p, _C.c_ulong, _C.c_ulong,
+                                      _C.c_uint, _C.c_float, _C.c_ulonglong, _C.c_void_p, _C.c_ulong, _C.c_void_p]),
+        "ncgb_mlp_knots": (_C.c_int, [_Handle, _C.c_void_p, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p]),
+        "ncgb_attach_proposal": (_C.c_int, [H, _C.c_int, _Handle, _C.c_double, _dblp]),
+        "ncgb_attach_proposal_knots": (_C.c_int, [H, _C.c_int, _C.c_void_p, _C.c_double, _dblp]),
+        "ncgb_detach_proposal": (_C.c_int, [H, _C.c_int]),
+        "ncgb_proposal_acceptance": (_C.c_int, [H, _C.c_int, _C.c_void_p, _C.c_void_p]),
+        "ncgb_tables_build_proposal": (_C.c_int, [_C.c_void_p, _C.c_int, _C.c_void_p, _C.c_void_p, _C.c_double,
+                                                  _C.c_void_p, _C.c_void_p, _C.c_void_p, _C.c_void_p,
+                                                  _C.POINTER(_C.c_ulong)]),
+        "ncgb_tables_set_proposal": (_C.c_int, [_C.c_void_p, _C.c_int, _C.c_void_p, _C.c_void_p, _C.c_void_p,
+                                                _C.c_void_p, _C.c_ulong]),
         "ncgb_set_mode": (_C.c_int, [H, _C.c_int]),
         "ncgb_get_mode": (_C.c_int, [H]),
         "ncgb_batch_xs_scatter_many": (None, [_Handle, _C.c_void_p, _C.c_void_p, _C.c_ulong, _C.c_void_p,
@@ -218,6 +246,8 @@ class Process:
 
 
 MODES = {"exact": 0, "mixed": 1}
+SAMPLERS = {"plain": 0, "learned": 1}
+COMP_SAB = 3
 
 
 def _mode_code(mode):
@@ -241,6 +271,84 @@ class Scatter(Process):
         if lib().ncgb_set_mode(self._h, _mode_code(mode)):
             _check()
         return self
+
+    # ---- learned beta proposal ----------------------------------------------
+    @property
+    def sampler(self):
+        """"plain" (percentile inversion) or "learned" (attached proposals)."""
+        m = lib().ncgb_get_sampler(self._h)
+        _check()
+        return {v: k for k, v in SAMPLERS.items()}[m]
+
+    def set_sampler(self, sampler):
+        if sampler not in SAMPLERS:
+            raise NCBadInput("sampler must be one of %s" % sorted(SAMPLERS))
+        if lib().ncgb_set_sampler(self._h, SAMPLERS[sampler]):
+            _check()
+        return self
+
+    def material_info(self):
+        """-> (ncomp, temperature K, [(type, scale, ne), ...])."""
+        L = lib()
+        nc, T = _C.c_int(), _C.c_double()
+        if L.ncgb_material_info(self._h, _C.byref(nc), _C.byref(T)):
+            _check()
+        comps = []
+        for c in range(nc.value):
+            t, sc, ne = _C.c_int(), _C.c_double(), _C.c_ulong()
+            if L.ncgb_component_info(self._h, c, _C.byref(t), _C.byref(sc), _C.byref(ne)):
+                _check()
+            comps.append((t.value, sc.value, ne.value))
+        return nc.value, T.value, comps
+
+    def sab_components(self):
+        return [i for i, (t, _, _) in enumerate(self.material_info()[2]) if t == COMP_SAB]
+
+    def sab_egrid(self, comp):
+        ne = self.material_info()[2][comp][2]
+        out = _np.empty(ne)
+        if lib().ncgb_sab_egrid(self._h, comp, out.ctypes.data):
+            _check()
+        return out
+
+    def sab_sample_device(self, comp, ekin, alpha, beta, status=None, stream=None):
+        """(alpha, beta) of S(alpha,beta) component 'comp' at the energies of the
+        float64 CUDA tensor 'ekin' (ncgb_sab_sample_device)."""
+        import torch
+        if stream is None:
+            stream = torch.cuda.current_stream(ekin.device)
+        if lib().ncgb_sab_sample_device(self._h, comp, ekin.data_ptr(), ekin.numel(), alpha.data_ptr(),
+                                        beta.data_ptr(), 0 if status is None else status.data_ptr(),
+                                        stream.cuda_stream):
+            _check()
+
+    def attach_proposal(self, comp, net, min_accept=0.5):
+        """Attach network 'net' (an MLP) as the beta proposal of component
+        'comp'; returns the mean envelope acceptance of the enabled egrid points."""
+        a = _C.c_double()
+        if lib().ncgb_attach_proposal(self._h, comp, net._h, float(min_accept), _C.byref(a)):
+            _check()
+        return a.value
+
+    def attach_proposal_knots(self, comp, knots, min_accept=0.5):
+        k = _np.ascontiguousarray(knots, dtype=_np.float32)
+        a = _C.c_double()
+        if lib().ncgb_attach_proposal_knots(self._h, comp, k.ctypes.data, float(min_accept), _C.byref(a)):
+            _check()
+        return a.value
+
+    def detach_proposal(self, comp):
+        if lib().ncgb_detach_proposal(self._h, comp):
+            _check()
+
+    def proposal_acceptance(self, comp):
+        """-> (acceptance[ne] float32, enabled[ne] bool) per egrid point."""
+        ne = self.material_info()[2][comp][2]
+        acc = _np.zeros(ne, dtype=_np.float32)
+        en = _np.zeros(ne, dtype=_np.int32)
+        if lib().ncgb_proposal_acceptance(self._h, comp, acc.ctypes.data, en.ctypes.data):
+            _check()
+        return acc, en.astype(bool)
 
     def sampleScatterIsotropic(self, ekin, repeat=None):
         """Returns (ekin_final, mu) -- NCrystal core.py:1492."""
@@ -372,6 +480,14 @@ class Batch:
             _check()
         return self
 
+    def set_sampler(self, sampler):
+        """"plain" or "learned" (proposals attached before the batch was made)."""
+        if sampler not in SAMPLERS:
+            raise NCBadInput("sampler must be one of %s" % sorted(SAMPLERS))
+        if lib().ncgb_batch_set_sampler(self._h, SAMPLERS[sampler]):
+            _check()
+        return self
+
     def _args(self, ekin, offsets, xs, ef, mu, status, stream):
         import torch
         p = (lambda t: 0 if t is None else t.data_ptr())
@@ -409,6 +525,71 @@ class Batch:
     def xs_scatter_host_ptr(self, ekin_ptr, offsets_ptr, n, xs_ptr, ef_ptr, mu_ptr):
         lib().ncgb_batch_xs_scatter_many(self._h, ekin_ptr, offsets_ptr, n, xs_ptr, ef_ptr, mu_ptr)
         _check()
+
+
+class MLP:
+    """The proposal network (ncgb_mlp_*): 4 hidden layers of 128, trained and
+    evaluated on the current CUDA device by the library's own kernels."""
+
+    def __init__(self, seed=1, emin=1e-5, emax=2.0, tmin=250.0, tmax=350.0):
+        L = lib()
+        self._h = L.ncgb_mlp_create(int(seed))
+        _check()
+        if not self._h.internal:
+            raise NCException("could not create the network")
+        self.ranges = (emin, emax, tmin, tmax)
+        if L.ncgb_mlp_set_ranges(self._h, emin, emax, tmin, tmax):
+            _check()
+
+    def __del__(self):
+        try:
+            if self._h is not None and self._h.internal:
+                lib().ncgb_mlp_destroy(_C.byref(self._h))
+        except Exception:
+            pass
+
+    @staticmethod
+    def nparams():
+        return int(lib().ncgb_mlp_nparams())
+
+    def params(self):
+        out = _np.empty(self.nparams(), dtype=_np.float32)
+        if lib().ncgb_mlp_get_params(self._h, out.ctypes.data):
+            _check()
+        return out
+
+    def set_params(self, p):
+        p = _np.ascontiguousarray(p, dtype=_np.float32)
+        assert p.size == self.nparams()
+        if lib().ncgb_mlp_set_params(self._h, p.ctypes.data):
+            _check()
+
+    def gradients(self, loge, temp, target):
+        """(mean pinball loss, flat gradient) on float32 CUDA tensors."""
+        g = _np.empty(self.nparams(), dtype=_np.float32)
+        loss = _C.c_float()
+        if lib().ncgb_mlp_gradients(self._h, loge.data_ptr(), temp.data_ptr(), target.data_ptr(), loge.numel(),
+                                    g.ctypes.data, _C.byref(loss), None):
+            _check()
+        return loss.value, g
+
+    def train(self, loge, temp, target, steps, batch=8192, lr=2e-3, seed=7, trace_every=0):
+        ntr = steps // trace_every if trace_every else 0
+        tr = _np.zeros(max(1, ntr), dtype=_np.float32)
+        if lib().ncgb_mlp_train(self._h, loge.data_ptr(), temp.data_ptr(), target.data_ptr(), loge.numel(),
+                                int(steps), int(batch), float(lr), int(seed), tr.ctypes.data if ntr else None,
+                                int(trace_every), None):
+            _check()
+        return tr[:ntr]
+
+    def knots(self, loge, temp):
+        """(n, 62) asinh(beta) knots at float32 CUDA tensors (log E, T)."""
+        import torch
+        out = torch.empty((loge.numel(), 62), dtype=torch.float32, device=loge.device)
+        if lib().ncgb_mlp_knots(self._h, loge.data_ptr(), temp.data_ptr(), loge.numel(), out.data_ptr(), None):
+            _check()
+        torch.cuda.synchronize()
+        return out
 
 
 def phase_timing(enable):

@@ -10,6 +10,8 @@
 // no CPU evaluation path in this library.
 #include "ncgb_host.hh"
 #include "ncgb_launch.hh"
+#include "ncgb_mlp.hh"
+#include "ncgb_proposal.hh"
 #include "ncrystal_gb300.h"
 
 #include <cuda_runtime.h>
@@ -91,15 +93,20 @@ namespace {
     int device = -1;
     void* d_arena = nullptr;
     ncgb_material_view view;
+    // learned beta proposals attached per component (device tables + host headers)
+    void* d_lp[NCGB_MAX_COMP] = {};
+    std::vector<ncgb_lp_hdr> h_lp[NCGB_MAX_COMP];
     ~DeviceMaterial()
     {
-      if ( d_arena ) {
-        int cur = -1;
-        cudaGetDevice( &cur );
-        cudaSetDevice( device );
+      int cur = -1;
+      cudaGetDevice( &cur );
+      cudaSetDevice( device );
+      if ( d_arena )
         cudaFree( d_arena );
-        cudaSetDevice( cur );
-      }
+      for ( void* p : d_lp )
+        if ( p )
+          cudaFree( p );
+      cudaSetDevice( cur );
     }
   };
 
@@ -249,6 +256,7 @@ namespace {
     uint64_t seed = kDefaultSeed;
     uint32_t streamidx = 0;
     int mode = defaultMode();
+    int sampler = NCGB_SAMPLER_PLAIN;
     std::atomic<uint32_t> callseq{0};
     ScatterObj() { fp.typeid_ = kScatterTypeID; fp.obj = this; }
   };
@@ -345,6 +353,7 @@ namespace {
     b.callseq = call;
     b.stream = o.streamidx;
     b.fast = ( o.mode == NCGB_MODE_MIXED );
+    b.learned = ( o.sampler == NCGB_SAMPLER_LEARNED );
     b.work = s.d_work;
     b.queue = static_cast<ncgb::QEntry*>( s.d_queue );
     return b;
@@ -592,6 +601,7 @@ static ncrystal_scatter_t cloneWithStream( ncrystal_scatter_t sc, uint32_t strea
   o->seed = src.seed;
   o->streamidx = streamidx;
   o->mode = src.mode;
+  o->sampler = src.sampler;
   return makeHandle( o.release() );
 }
 
@@ -948,6 +958,7 @@ namespace {
     ncgb::LaunchCfg cfg;
     bool tuned = false;
     int mode = defaultMode();
+    int sampler = NCGB_SAMPLER_PLAIN;
     std::atomic<uint32_t> callseq{0};
     // CUDA graph of (counter reset, k_pick, k_sab) for one set of arrays
     cudaGraphExec_t exec = nullptr;
@@ -981,6 +992,7 @@ namespace {
     b.out_b = d_mu;
     b.status = d_status;
     b.fast = ( bo.mode == NCGB_MODE_MIXED );
+    b.learned = ( bo.sampler == NCGB_SAMPLER_LEARNED );
     b.work = s.d_work;
     ensure( s.d_queue, s.cap_queue, n * sizeof(ncgb::QEntry) );
     b.queue = static_cast<ncgb::QEntry*>( s.d_queue );
@@ -1112,6 +1124,18 @@ int ncgb_batch_set_mode( ncgb_batch_t bt, int mode )
   return 1;
 }
 
+int ncgb_batch_set_sampler( ncgb_batch_t bt, int sampler )
+{
+  try {
+    BatchObj& bo = extractBatch( bt.internal, "ncgb_batch_set_sampler" );
+    if ( sampler != NCGB_SAMPLER_PLAIN && sampler != NCGB_SAMPLER_LEARNED )
+      throw TypedError( "BadInput", "ncgb_batch_set_sampler: unknown sampler" );
+    bo.sampler = sampler;
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
 int ncgb_batch_config( ncgb_batch_t bt, int* pick_block, int* sab_blocks_per_sm )
 {
   try {
@@ -1205,6 +1229,354 @@ void ncgb_batch_xs_scatter_many( ncgb_batch_t bt, const double* ekin, const int6
     return;
   } NCGB_CATCH;
   fillSentinels<double>( n, xs, ef, mu );
+}
+
+}
+
+// ---- learned beta proposal (no reference counterpart) ------------------------------
+namespace {
+
+  const ncgb_comp_view& sabComp( ScatterObj& o, int comp, const char* fct )
+  {
+    if ( comp < 0 || comp >= o.mat->view.ncomp )
+      throw TypedError( "BadInput", std::string( fct ) + ": component index out of range" );
+    const ncgb_comp_view& c = o.mat->view.comp[comp];
+    if ( c.type != NCGB_COMP_SAB )
+      throw TypedError( "BadInput", std::string( fct ) + ": component is not an S(alpha,beta) component" );
+    return c;
+  }
+
+  ncgb_sab_view hostSab( ScatterObj& o, int comp )
+  {
+    const ncgb_material_view hv = o.mat->tables->relocate( o.mat->tables->arena().data() );
+    return hv.comp[comp].sab;
+  }
+
+  // Builds the proposal tables from knots[ne*62] on the host, uploads them and
+  // points the material's view at them.
+  double attachKnots( ScatterObj& o, int comp, const float* knots, const unsigned char* allowed, double min_accept )
+  {
+    const ncgb_sab_view hs = hostSab( o, comp );
+    ncgb::Proposal P = ncgb::buildProposal( hs, knots, NCGB_LP_NKNOTS, allowed, min_accept );
+    DeviceMaterial& dm = *o.mat;
+    checkCuda( cudaSetDevice( dm.device ), "cudaSetDevice" );
+    const std::size_t hb = ( P.hdr.size() * sizeof(ncgb_lp_hdr) + 255 ) & ~std::size_t(255);
+    const std::size_t sb = ( P.slot.size() * sizeof(ncgb_lp_slot) + 255 ) & ~std::size_t(255);
+    const std::size_t cb = ( P.cell.size() * sizeof(ncgb_lp_cell) + 255 ) & ~std::size_t(255);
+    const std::size_t gb = P.seg.size() * sizeof(ncgb_lp_seg);
+    void* d = nullptr;
+    checkCuda( cudaMalloc( &d, hb + sb + cb + gb ), "cudaMalloc (proposal tables)" );
+    char* dc = static_cast<char*>( d );
+    checkCuda( cudaMemcpy( dc, P.hdr.data(), P.hdr.size() * sizeof(ncgb_lp_hdr), cudaMemcpyHostToDevice ), "H2D" );
+    checkCuda( cudaMemcpy( dc + hb, P.slot.data(), P.slot.size() * sizeof(ncgb_lp_slot), cudaMemcpyHostToDevice ),
+               "H2D" );
+    checkCuda( cudaMemcpy( dc + hb + sb, P.cell.data(), P.cell.size() * sizeof(ncgb_lp_cell),
+                           cudaMemcpyHostToDevice ), "H2D" );
+    checkCuda( cudaMemcpy( dc + hb + sb + cb, P.seg.data(), gb, cudaMemcpyHostToDevice ), "H2D" );
+    checkCuda( cudaDeviceSynchronize(), "proposal upload" );
+    if ( dm.d_lp[comp] )
+      cudaFree( dm.d_lp[comp] );
+    dm.d_lp[comp] = d;
+    dm.h_lp[comp] = P.hdr;
+    dm.view.comp[comp].sab.lp_hdr = reinterpret_cast<const ncgb_lp_hdr*>( dc );
+    dm.view.comp[comp].sab.lp_slot = reinterpret_cast<const ncgb_lp_slot*>( dc + hb );
+    dm.view.comp[comp].sab.lp_cell = reinterpret_cast<const ncgb_lp_cell*>( dc + hb + sb );
+    dm.view.comp[comp].sab.lp_seg = reinterpret_cast<const ncgb_lp_seg*>( dc + hb + sb + cb );
+    double sum = 0.0;
+    int n = 0;
+    for ( auto& h : P.hdr )
+      if ( h.enabled ) { sum += h.accept; ++n; }
+    return n ? sum / n : 0.0;
+  }
+
+  constexpr uint32_t kMlpTypeID = 0x6e636d6c; // "ncml"
+  struct MlpObj {
+    uint32_t typeid_ = kMlpTypeID;
+    ncgb_mlp::Net* net = nullptr;
+    ~MlpObj() { ncgb_mlp::destroy( net ); }
+  };
+
+  MlpObj& extractMlp( void* internal, const char* fct )
+  {
+    auto m = static_cast<MlpObj*>( internal );
+    if ( !m || m->typeid_ != kMlpTypeID )
+      throw TypedError( "LogicError", std::string( "Invalid network handle passed to " ) + fct );
+    return *m;
+  }
+}
+
+extern "C" {
+
+int ncgb_set_sampler( ncrystal_scatter_t sc, int sampler )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_set_sampler" );
+    if ( sampler != NCGB_SAMPLER_PLAIN && sampler != NCGB_SAMPLER_LEARNED )
+      throw TypedError( "BadInput", "ncgb_set_sampler: unknown sampler" );
+    o.sampler = sampler;
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_get_sampler( ncrystal_scatter_t sc )
+{
+  try {
+    return extract( sc.internal, "ncgb_get_sampler" ).sampler;
+  } NCGB_CATCH;
+  return -1;
+}
+
+int ncgb_component_info( ncrystal_scatter_t sc, int comp, int* type, double* scale, unsigned long* ne )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_component_info" );
+    const ncgb_material_view& v = o.mat->view;
+    if ( comp < 0 || comp >= v.ncomp )
+      throw TypedError( "BadInput", "ncgb_component_info: component index out of range" );
+    if ( type ) *type = v.comp[comp].type;
+    if ( scale ) *scale = v.comp[comp].scale;
+    if ( ne ) *ne = v.comp[comp].type == NCGB_COMP_SAB ? (unsigned long)v.comp[comp].sab.ne : 0ul;
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_material_info( ncrystal_scatter_t sc, int* ncomp, double* temperature )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_material_info" );
+    if ( ncomp ) *ncomp = o.mat->view.ncomp;
+    if ( temperature ) *temperature = o.mat->tables->temperature();
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_sab_egrid( ncrystal_scatter_t sc, int comp, double* egrid_out )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_sab_egrid" );
+    sabComp( o, comp, "ncgb_sab_egrid" );
+    const ncgb_sab_view hs = hostSab( o, comp );
+    std::memcpy( egrid_out, hs.egrid, hs.ne * sizeof(double) );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_sab_sample_device( ncrystal_scatter_t sc, int comp, const double* d_ekin, unsigned long n,
+                            double* d_alpha, double* d_beta, int32_t* d_status, void* stream )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_sab_sample_device" );
+    sabComp( o, comp, "ncgb_sab_sample_device" );
+    checkSize( n, 1 );
+    if ( !d_ekin || !d_alpha || !d_beta )
+      throw TypedError( "BadInput", "ncgb_sab_sample_device: null array" );
+    Scratch& s = scratchFor( *o.mat );
+    cudaStream_t st = static_cast<cudaStream_t>( stream );
+    ncgb::Batch b = makeBatch( o, s, nextCall( o ) );
+    b.ekin = d_ekin;
+    b.n_ekin = b.n_out = n;
+    b.out_a = d_alpha;
+    b.out_b = d_beta;
+    b.status = d_status;
+    checkCuda( cudaStreamWaitEvent( st, s.done, 0 ), "cudaStreamWaitEvent" );
+    checkCuda( ncgb::launchSabAB( o.mat->view, comp, b, st ), "S(alpha,beta) sampling kernel" );
+    checkCuda( cudaEventRecord( s.done, st ), "cudaEventRecord" );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_attach_proposal_knots( ncrystal_scatter_t sc, int comp, const float* knots, double min_accept,
+                                double* mean_accept )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_attach_proposal_knots" );
+    sabComp( o, comp, "ncgb_attach_proposal_knots" );
+    if ( !knots )
+      throw TypedError( "BadInput", "ncgb_attach_proposal_knots: null knots" );
+    const double a = attachKnots( o, comp, knots, nullptr, min_accept );
+    if ( mean_accept ) *mean_accept = a;
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_attach_proposal( ncrystal_scatter_t sc, int comp, ncgb_mlp_t net, double min_accept, double* mean_accept )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_attach_proposal" );
+    MlpObj& m = extractMlp( net.internal, "ncgb_attach_proposal" );
+    sabComp( o, comp, "ncgb_attach_proposal" );
+    if ( ncgb_mlp::device( m.net ) != o.mat->device )
+      throw TypedError( "BadInput", "ncgb_attach_proposal: network and material on different devices" );
+    const ncgb_sab_view hs = hostSab( o, comp );
+    const int ne = (int)hs.ne;
+    const double T = o.mat->tables->temperature();
+    const ncgb_mlp::Ranges rg = ncgb_mlp::getRanges( m.net );
+    // the network is evaluated at the sampler energies (egrid points) of this temperature
+    std::vector<float> loge( ne ), temp( ne, (float)T );
+    std::vector<unsigned char> allowed( ne, 0 );
+    const bool t_ok = T >= rg.t_min - 1e-3 && T <= rg.t_max + 1e-3;
+    for ( int i = 0; i < ne; ++i ) {
+      loge[i] = (float)std::log( hs.egrid[i] );
+      allowed[i] = ( t_ok && loge[i] >= rg.loge_min && loge[i] <= rg.loge_max ) ? 1 : 0;
+    }
+    checkCuda( cudaSetDevice( o.mat->device ), "cudaSetDevice" );
+    float* d = nullptr;
+    checkCuda( cudaMalloc( &d, (std::size_t)ne * ( 2 + ncgb_mlp::kOut ) * sizeof(float) ), "cudaMalloc" );
+    std::unique_ptr<float, decltype(&cudaFree)> guard( d, &cudaFree );
+    float* d_loge = d;
+    float* d_temp = d + ne;
+    float* d_knots = d + 2 * ne;
+    checkCuda( cudaMemcpy( d_loge, loge.data(), ne * sizeof(float), cudaMemcpyHostToDevice ), "H2D" );
+    checkCuda( cudaMemcpy( d_temp, temp.data(), ne * sizeof(float), cudaMemcpyHostToDevice ), "H2D" );
+    ncgb_mlp::knots( m.net, d_loge, d_temp, ne, d_knots, nullptr );
+    std::vector<float> knots( (std::size_t)ne * ncgb_mlp::kOut );
+    checkCuda( cudaMemcpy( knots.data(), d_knots, knots.size() * sizeof(float), cudaMemcpyDeviceToHost ), "D2H" );
+    const double a = attachKnots( o, comp, knots.data(), allowed.data(), min_accept );
+    if ( mean_accept ) *mean_accept = a;
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_detach_proposal( ncrystal_scatter_t sc, int comp )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_detach_proposal" );
+    sabComp( o, comp, "ncgb_detach_proposal" );
+    DeviceMaterial& dm = *o.mat;
+    checkCuda( cudaDeviceSynchronize(), "synchronize before detaching" );
+    dm.view.comp[comp].sab.lp_hdr = nullptr;
+    dm.view.comp[comp].sab.lp_slot = nullptr;
+    dm.view.comp[comp].sab.lp_cell = nullptr;
+    dm.view.comp[comp].sab.lp_seg = nullptr;
+    if ( dm.d_lp[comp] )
+      cudaFree( dm.d_lp[comp] );
+    dm.d_lp[comp] = nullptr;
+    dm.h_lp[comp].clear();
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_proposal_acceptance( ncrystal_scatter_t sc, int comp, float* accept, int32_t* enabled )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_proposal_acceptance" );
+    const ncgb_comp_view& c = sabComp( o, comp, "ncgb_proposal_acceptance" );
+    const auto& h = o.mat->h_lp[comp];
+    for ( int64_t i = 0; i < c.sab.ne; ++i ) {
+      if ( accept ) accept[i] = h.empty() ? 0.f : h[i].accept;
+      if ( enabled ) enabled[i] = h.empty() ? 0 : h[i].enabled;
+    }
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+ncgb_mlp_t ncgb_mlp_create( unsigned long long seed )
+{
+  try {
+    int dev = 0;
+    checkCuda( cudaGetDevice( &dev ), "cudaGetDevice" );
+    std::unique_ptr<MlpObj> m( new MlpObj );
+    m->net = ncgb_mlp::create( dev, seed );
+    return ncgb_mlp_t{ m.release() };
+  } NCGB_CATCH;
+  return ncgb_mlp_t{ nullptr };
+}
+
+void ncgb_mlp_destroy( ncgb_mlp_t* net )
+{
+  try {
+    if ( !net || !net->internal )
+      return;
+    MlpObj& m = extractMlp( net->internal, "ncgb_mlp_destroy" );
+    cudaDeviceSynchronize();
+    delete &m;
+    net->internal = nullptr;
+  } NCGB_CATCH;
+}
+
+unsigned long ncgb_mlp_nparams( void ) { return (unsigned long)ncgb_mlp::nparams(); }
+
+int ncgb_mlp_get_params( ncgb_mlp_t net, float* out )
+{
+  try {
+    ncgb_mlp::getParams( extractMlp( net.internal, "ncgb_mlp_get_params" ).net, out );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_mlp_set_params( ncgb_mlp_t net, const float* in )
+{
+  try {
+    ncgb_mlp::setParams( extractMlp( net.internal, "ncgb_mlp_set_params" ).net, in );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_mlp_set_ranges( ncgb_mlp_t net, double emin, double emax, double tmin, double tmax )
+{
+  try {
+    MlpObj& m = extractMlp( net.internal, "ncgb_mlp_set_ranges" );
+    if ( !( emin > 0.0 && emax > emin && tmax > tmin ) )
+      throw TypedError( "BadInput", "ncgb_mlp_set_ranges: need 0 < emin < emax and tmin < tmax" );
+    ncgb_mlp::setRanges( m.net, ncgb_mlp::Ranges{ (float)std::log( emin ), (float)std::log( emax ), (float)tmin,
+                                                  (float)tmax } );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_mlp_gradients( ncgb_mlp_t net, const float* d_loge, const float* d_temp, const float* d_target,
+                        unsigned long n, float* h_grad, float* h_loss, void* stream )
+{
+  try {
+    MlpObj& m = extractMlp( net.internal, "ncgb_mlp_gradients" );
+    if ( n == 0 || n > ( 1ul << 22 ) )
+      throw TypedError( "BadInput", "ncgb_mlp_gradients: n must be in [1, 2^22]" );
+    const float l = ncgb_mlp::gradients( m.net, d_loge, d_temp, d_target, (int)n, h_grad,
+                                         static_cast<cudaStream_t>( stream ) );
+    if ( h_loss ) *h_loss = l;
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_mlp_train( ncgb_mlp_t net, const float* d_loge, const float* d_temp, const float* d_target,
+                    unsigned long n, unsigned long steps, unsigned int batch, float lr, unsigned long long seed,
+                    float* h_trace, unsigned long trace_every, void* stream )
+{
+  try {
+    MlpObj& m = extractMlp( net.internal, "ncgb_mlp_train" );
+    if ( batch == 0 || batch % 64 || batch > ( 1u << 20 ) )
+      throw TypedError( "BadInput", "ncgb_mlp_train: batch must be a multiple of 64 up to 2^20" );
+    ncgb_mlp::train( m.net, d_loge, d_temp, d_target, n, steps, (int)batch, lr, seed, h_trace, trace_every,
+                     static_cast<cudaStream_t>( stream ) );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_mlp_knots( ncgb_mlp_t net, const float* d_loge, const float* d_temp, unsigned long n, float* d_knots,
+                    void* stream )
+{
+  try {
+    MlpObj& m = extractMlp( net.internal, "ncgb_mlp_knots" );
+    if ( n == 0 || n > ( 1ul << 22 ) )
+      throw TypedError( "BadInput", "ncgb_mlp_knots: n must be in [1, 2^22]" );
+    ncgb_mlp::knots( m.net, d_loge, d_temp, (int)n, d_knots, static_cast<cudaStream_t>( stream ) );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
 }
 
 }

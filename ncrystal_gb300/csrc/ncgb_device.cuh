@@ -31,21 +31,37 @@ namespace ncgb_dev {
   __device__ __forceinline__ long long ldgbits( const double* p ) { return __double_as_longlong( __ldg(p) ); }
   __device__ __forceinline__ long long bits( double x ) { return __double_as_longlong(x); }
 
+  __device__ __forceinline__ void refill( ncgb_rng& r )
+  {
+    uint32_t ctr[4] = { r.block, r.ctr1, r.ctr2, r.ctr3 };
+    ncgb_philox4x32_10( ctr, r.key0, r.key1, r.word );
+    r.block += 1;
+    r.have = 4;
+  }
+
+  // The next 32-bit word of the stream (ncgb_rng_u32), selected without
+  // dynamic indexing so that the words stay in registers.
+  __device__ __forceinline__ uint32_t rand_u32( ncgb_rng& r )
+  {
+    if ( r.have == 0 )
+      refill( r );
+    const uint32_t h = r.have;
+    const uint32_t w = h == 4 ? r.word[0] : h == 3 ? r.word[1] : h == 2 ? r.word[2] : r.word[3];
+    r.have = h - 1;
+    return w;
+  }
+
   // Uniform double in (0,1]: same value as ncgb_rng_generate, built with
   // integer ops (k in [1, 2^53] -> k * 2^-53, exact).
   __device__ __forceinline__ double rand01( ncgb_rng& r )
   {
-    if ( r.have == 0 ) {
-      uint32_t ctr[4] = { r.block, r.ctr1, r.ctr2, r.ctr3 };
-      uint32_t o[4];
-      ncgb_philox4x32_10( ctr, r.key0, r.key1, o );
-      r.block += 1;
-      r.cache[0] = (uint64_t)o[0] | ( (uint64_t)o[1] << 32 );
-      r.cache[1] = (uint64_t)o[2] | ( (uint64_t)o[3] << 32 );
-      r.have = 2;
-    }
-    const uint64_t k = ( r.cache[2 - r.have] >> 11 ) + 1;
-    r.have -= 1;
+    if ( r.have < 2 )
+      refill( r );
+    const uint32_t h = r.have;
+    const uint32_t lo = h == 4 ? r.word[0] : h == 3 ? r.word[1] : r.word[2];
+    const uint32_t hi = h == 4 ? r.word[1] : h == 3 ? r.word[2] : r.word[3];
+    r.have = h - 2;
+    const uint64_t k = ( ( (uint64_t)lo | ( (uint64_t)hi << 32 ) ) >> 11 ) + 1;
     const int p = 63 - __clzll( (long long)k );           // highest set bit, 0..53
     const uint64_t mant = ( k << ( 52 - ( p < 52 ? p : 52 ) ) ) & 0xFFFFFFFFFFFFFull;
     const uint64_t b = ( p == 53 ) ? 0x3FF0000000000000ull
@@ -493,53 +509,51 @@ namespace ncgb_dev {
   // One attempt of SABSamplerAtE_Alg1::sampleAlphaBeta's loop
   // (NCSABSamplerModels.cc:59-148) at energy-grid point ie, sampling energy
   // x = E/kT.  Returns 1 with (alpha, beta) on acceptance, 0 on rejection.
-  // Order-preserving integer key of a double (any sign): compares on the
-  // integer pipe.
-  __device__ __forceinline__ long long okey( double v )
-  {
-    const long long b = __double_as_longlong( v );
-    return b ^ ( ( b >> 63 ) & 0x7fffffffffffffffLL );
-  }
-
   // Learned proposal for the regular beta range of sampler ie (tables built by
-  // ncgb_proposal.cc): an interval from the alias table, beta uniform in it,
-  // accepted with probability y(beta)/env.  Returns 1 with (beta, ibs), or 0
-  // if 1000 proposals were all rejected.
-  __device__ __forceinline__ int lpBeta( const ncgb_sab_view& s, int64_t ie, const double* bx, const double* by,
-                                         ncgb_rng& rng, double& beta, int64_t& ibs )
+  // ncgb_proposal.cc): an interval from the alias table, a 32-bit draw w
+  // placing beta = q + (2w+1) h in it, accepted with probability y/env, y from
+  // the interval's linear pieces in w.  A proposal uses integer and FP32
+  // arithmetic only; beta is formed in FP64 once accepted, after the lanes
+  // that entered together have reconverged (so that the FP64 work after this
+  // call is not split across lanes accepting at different tries).  Returns 1
+  // with (beta, ibs), or 0 if 1000 proposals were all rejected.
+  __device__ __forceinline__ int lpBeta( const ncgb_sab_view& s, int64_t ie, ncgb_rng& rng, double& beta,
+                                         int64_t& ibs )
   {
-    const ncgb_lp_cell* cells = s.lp_cell + ie * ( NCGB_LP_K + 1 );
-    for ( int tries = 0; tries < 1000; ++tries ) {
-      const double t = rand01( rng ) * (double)NCGB_LP_K;
-      int j = (int)t;
-      if ( j > NCGB_LP_K - 1 )
-        j = NCGB_LP_K - 1;
-      const float fr = (float)( t - (double)j );
-      const int k = ( fr < __ldg( &cells[j].aprob ) ) ? j : __ldg( &cells[j].alias );
-      const double q0 = ldg( &cells[k].q ), q1 = ldg( &cells[k + 1].q );
-      const double b = fma( rand01( rng ), q1 - q0, q0 );
-      // largest bin j in [bin_k, bin_k+1] with bx[j] <= b
-      int64_t lo = __ldg( &cells[k].bin ), hi = __ldg( &cells[k + 1].bin );
-      const long long kb = okey( b );
+    const unsigned lanes = __activemask();
+    const ncgb_lp_slot* slots = s.lp_slot + ie * NCGB_LP_K;
+    const ncgb_lp_cell* cells = s.lp_cell + ie * NCGB_LP_K;
+    const ncgb_lp_cell* c = cells;
+    const ncgb_lp_seg* g = s.lp_seg;
+    uint32_t w = 0;
+    int ok = 0;
+    for ( int tries = 0; tries < 1000 && !ok; ++tries ) {
+      const uint64_t prod = (uint64_t)rand_u32( rng ) * (uint64_t)NCGB_LP_K;
+      const int j = (int)( prod >> 32 );
+      const float fr = (float)( (uint32_t)prod >> 8 ) * ( 1.0f / 16777216.0f );
+      const int k = ( fr < __ldg( &slots[j].aprob ) ) ? j : __ldg( &slots[j].alias );
+      c = cells + k;
+      w = rand_u32( rng );
+      // last piece with w0 <= w
+      int lo = __ldg( &c->seg_lo ), hi = lo + __ldg( &c->seg_n ) - 1;
       while ( lo < hi ) {
-        const int64_t mid = ( lo + hi + 1 ) >> 1;
-        if ( okey( ldg( bx + mid ) ) <= kb )
+        const int mid = ( lo + hi + 1 ) >> 1;
+        if ( __ldg( &s.lp_seg[mid].w0 ) <= w )
           lo = mid;
         else
           hi = mid - 1;
       }
-      const double x0 = ldg( bx + lo );
-      const float dx = (float)( ldg( bx + lo + 1 ) - x0 );
-      const float tt = dx > 0.0f ? (float)( b - x0 ) / dx : 0.0f;
-      const float y0 = (float)ldg( by + lo );
-      const float y = fmaf( (float)ldg( by + lo + 1 ) - y0, tt, y0 );
-      if ( (float)rand01( rng ) * __ldg( &cells[k].env ) < y ) {
-        beta = b;
-        ibs = lo;
-        return 1;
-      }
+      g = s.lp_seg + lo;
+      const float y = fmaf( __ldg( &g->slope ), (float)( w - __ldg( &g->w0 ) ), __ldg( &g->y0 ) );
+      const float ua = (float)( rand_u32( rng ) >> 8 ) * ( 1.0f / 16777216.0f );
+      ok = ( ua * __ldg( &c->env ) < y );
     }
-    return 0;
+    __syncwarp( lanes );
+    if ( ok ) {
+      beta = fma( (double)( 2ull * w + 1ull ), ldg( &c->h ), ldg( &c->q ) );
+      ibs = __ldg( &g->bin );
+    }
+    return ok;
   }
 
   // One attempt of SABSamplerAtE_Alg1::sampleAlphaBeta.  Returns 1 with
@@ -561,9 +575,9 @@ namespace ncgb_dev {
     if ( Learned && s.lp_hdr && __ldg( &s.lp_hdr[ie].enabled ) ) {
       // the special first bin keeps its probability bcdf[1]; the regular
       // range is drawn from the learned proposal
-      if ( rand01( rng ) <= ldg( &s.lp_hdr[ie].c1 ) )
+      if ( rand_u32( rng ) < __ldg( &s.lp_hdr[ie].c1_thr ) )
         return alg1FirstBin<Fast>( s, infos, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
-      if ( !lpBeta( s, ie, bx, s.by + off, rng, beta, ibs ) )
+      if ( !lpBeta( s, ie, rng, beta, ibs ) )
         return -1;
     } else {
       beta = percentile( bx, s.bcdf + off, s.bbin + off, nbs, rand01( rng ), ibs );

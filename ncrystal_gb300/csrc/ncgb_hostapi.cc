@@ -2,6 +2,7 @@
 // tables in host memory, without touching a GPU.  The tests and the CPU
 // oracle use it to read exactly the tables the kernels read.
 #include "ncgb_host.hh"
+#include "ncgb_proposal.hh"
 #include "ncrystal_gb300.h"
 
 #include <cstring>
@@ -11,8 +12,22 @@
 namespace {
   struct HostTables {
     std::shared_ptr<ncgb::MaterialTables> mt;
+    ncgb::Proposal lp[NCGB_MAX_COMP];   // learned proposals set for the oracle
   };
   thread_local std::string t_lasterr;
+
+  ncgb_material_view hostView( HostTables* h )
+  {
+    ncgb_material_view v = h->mt->relocate( h->mt->arena().data() );
+    for ( int ic = 0; ic < v.ncomp; ++ic )
+      if ( !h->lp[ic].hdr.empty() ) {
+        v.comp[ic].sab.lp_hdr = h->lp[ic].hdr.data();
+        v.comp[ic].sab.lp_slot = h->lp[ic].slot.data();
+        v.comp[ic].sab.lp_cell = h->lp[ic].cell.data();
+        v.comp[ic].sab.lp_seg = h->lp[ic].seg.data();
+      }
+    return v;
+  }
 }
 
 extern "C" {
@@ -36,8 +51,68 @@ int ncgb_tables_view( void* handle, ncgb_material_view* out )
 {
   if ( !handle || !out )
     return 1;
+  *out = hostView( static_cast<HostTables*>( handle ) );
+  return 0;
+}
+
+// Learned-proposal tables of SAB component 'comp' from knots[ne*62]
+// (asinh(beta) per egrid point), allowed[ne] optional; hdr_out[ne],
+// slot_out[ne*NCGB_LP_K], cell_out[ne*NCGB_LP_K] and seg_out[*nseg] receive
+// them.  Returns 0 on success, 2 (with *nseg set to the number of pieces) if
+// seg_out is NULL or *nseg too small, 1 on error.
+int ncgb_tables_build_proposal( void* handle, int comp, const float* knots, const unsigned char* allowed,
+                                double min_accept, void* hdr_out, void* slot_out, void* cell_out, void* seg_out,
+                                unsigned long* nseg )
+{
+  try {
+    if ( !handle || !knots || !nseg )
+      throw ncgb::Error( "ncgb_tables_build_proposal: null argument" );
+    auto* h = static_cast<HostTables*>( handle );
+    ncgb_material_view v = h->mt->relocate( h->mt->arena().data() );
+    if ( comp < 0 || comp >= v.ncomp || v.comp[comp].type != NCGB_COMP_SAB )
+      throw ncgb::Error( "ncgb_tables_build_proposal: component is not an S(alpha,beta) component" );
+    ncgb::Proposal P = ncgb::buildProposal( v.comp[comp].sab, knots, NCGB_LP_NKNOTS, allowed, min_accept );
+    if ( !seg_out || *nseg < P.seg.size() ) {
+      *nseg = P.seg.size();
+      return 2;
+    }
+    if ( !hdr_out || !slot_out || !cell_out )
+      throw ncgb::Error( "ncgb_tables_build_proposal: null output array" );
+    *nseg = P.seg.size();
+    std::memcpy( hdr_out, P.hdr.data(), P.hdr.size() * sizeof(ncgb_lp_hdr) );
+    std::memcpy( slot_out, P.slot.data(), P.slot.size() * sizeof(ncgb_lp_slot) );
+    std::memcpy( cell_out, P.cell.data(), P.cell.size() * sizeof(ncgb_lp_cell) );
+    std::memcpy( seg_out, P.seg.data(), P.seg.size() * sizeof(ncgb_lp_seg) );
+    return 0;
+  } catch ( std::exception& e ) {
+    t_lasterr = e.what();
+    return 1;
+  }
+}
+
+// Makes ncgb_tables_view carry these proposal tables for component 'comp'
+// (copies; hdr NULL removes them).
+int ncgb_tables_set_proposal( void* handle, int comp, const void* hdr, const void* slot, const void* cell,
+                              const void* seg, unsigned long nseg )
+{
+  if ( !handle )
+    return 1;
   auto* h = static_cast<HostTables*>( handle );
-  *out = h->mt->relocate( h->mt->arena().data() );
+  ncgb_material_view v = h->mt->relocate( h->mt->arena().data() );
+  if ( comp < 0 || comp >= v.ncomp || v.comp[comp].type != NCGB_COMP_SAB )
+    return 1;
+  ncgb::Proposal& P = h->lp[comp];
+  if ( !hdr ) {
+    P = ncgb::Proposal();
+    return 0;
+  }
+  if ( !slot || !cell || !seg )
+    return 1;
+  const std::size_t ne = v.comp[comp].sab.ne;
+  P.hdr.assign( static_cast<const ncgb_lp_hdr*>( hdr ), static_cast<const ncgb_lp_hdr*>( hdr ) + ne );
+  P.slot.assign( static_cast<const ncgb_lp_slot*>( slot ), static_cast<const ncgb_lp_slot*>( slot ) + ne * NCGB_LP_K );
+  P.cell.assign( static_cast<const ncgb_lp_cell*>( cell ), static_cast<const ncgb_lp_cell*>( cell ) + ne * NCGB_LP_K );
+  P.seg.assign( static_cast<const ncgb_lp_seg*>( seg ), static_cast<const ncgb_lp_seg*>( seg ) + nseg );
   return 0;
 }
 

@@ -168,7 +168,7 @@ namespace {
           q.idx = (uint32_t)o;
           q.mat = (uint16_t)k;
           q.comp = (uint8_t)qcomp;
-          q.ndraws = (uint8_t)( 2 * rng.block - rng.have );
+          q.ndraws = (uint8_t)ncgb_rng_ndoubles( &rng );
           b.queue[pos] = q;
         }
       }

@@ -1,0 +1,630 @@
+// The learned beta proposal's network: a small MLP trained and evaluated on
+// the GPU by the kernels of this file (no counterpart in NCrystal).
+//
+//   features(log E, T) [32] -> 128 -> 128 -> 128 -> 128 -> 62 raw outputs
+//   ReLU after every hidden layer; the 62 outputs o become monotone knots
+//   g_0 = o_0, g_i = g_(i-1) + softplus(o_i): the conditional quantiles of
+//   asinh(beta) at the levels tau_i = (i+1)/63 (quantile regression, pinball
+//   loss).
+//
+// GEMMs run on the tensor cores as mma.sync m16n8k16 with BF16 operands and
+// FP32 accumulation; master weights, Adam moments, the loss and the softplus
+// chain stay FP32.  Weights are stored [in][out] row-major, activations
+// [sample][feature] row-major, both BF16 copies for the GEMMs.
+
+#include "ncgb_mlp.hh"
+#include "ncgb_philox.h"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace ncgb_mlp {
+
+  using bf16 = __nv_bfloat16;
+
+  // ---- tiled BF16 GEMM, C[M x N] = sum_k A(m,k) B(k,n) -----------------------
+  // A(m,k) = A[m*sAm + k*sAk], B(k,n) = B[k*sBk + n*sBn].  blockIdx.z splits K
+  // into chunks of 'kchunk' (results then added atomically).
+  enum EpiMode { EPI_STORE = 0, EPI_MASK = 1, EPI_ATOMIC = 2 };
+
+  struct GemmArgs {
+    const bf16* A; long sAm, sAk;
+    const bf16* B; long sBk, sBn;
+    int M, N, K, kchunk;
+    int mode;
+    const float* bias;   // EPI_STORE: added per column
+    int relu;            // EPI_STORE: ReLU before the BF16 store
+    float* Cf;           // FP32 output (optional in EPI_STORE, required in EPI_ATOMIC)
+    bf16* Cb;            // BF16 output (optional)
+    long ldc;
+    const bf16* mask;    // EPI_MASK: value kept where mask > 0 (ReLU derivative)
+    long ldm;
+  };
+
+  constexpr int BM = 64, BN = 64, BK = 32, PADK = 40;
+
+  __device__ __forceinline__ uint32_t ld32( const bf16* p ) { return *reinterpret_cast<const uint32_t*>( p ); }
+
+  __global__ void __launch_bounds__(128) k_gemm( const GemmArgs g )
+  {
+    __shared__ __align__(16) bf16 As[BM][PADK];
+    __shared__ __align__(16) bf16 Bs[BN][PADK];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int gid = lane >> 2, tig = lane & 3;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int kbeg = blockIdx.z * g.kchunk;
+    const int kend = min( g.K, kbeg + g.kchunk );
+    const int wm = ( warp >> 1 ) * 32, wn = ( warp & 1 ) * 32;
+    float acc[2][4][4];
+#pragma unroll
+    for ( int i = 0; i < 2; ++i )
+#pragma unroll
+      for ( int j = 0; j < 4; ++j )
+#pragma unroll
+        for ( int r = 0; r < 4; ++r )
+          acc[i][j][r] = 0.f;
+    const bf16 zero = __float2bfloat16( 0.f );
+    for ( int k0 = kbeg; k0 < kend; k0 += BK ) {
+      // stage the A and B tiles, the unit-stride dimension fastest across threads
+      for ( int i = tid; i < BM * BK; i += 128 ) {
+        int r, kk;
+        if ( g.sAk == 1 ) { r = i / BK; kk = i % BK; } else { kk = i / BM; r = i % BM; }
+        const int m = m0 + r, k = k0 + kk;
+        As[r][kk] = ( m < g.M && k < kend ) ? g.A[(long)m * g.sAm + (long)k * g.sAk] : zero;
+      }
+      for ( int i = tid; i < BN * BK; i += 128 ) {
+        int c, kk;
+        if ( g.sBk == 1 ) { c = i / BK; kk = i % BK; } else { kk = i / BN; c = i % BN; }
+        const int n = n0 + c, k = k0 + kk;
+        Bs[c][kk] = ( n < g.N && k < kend ) ? g.B[(long)k * g.sBk + (long)n * g.sBn] : zero;
+      }
+      __syncthreads();
+#pragma unroll
+      for ( int ks = 0; ks < BK; ks += 16 ) {
+        uint32_t a[2][4], b[4][2];
+#pragma unroll
+        for ( int mi = 0; mi < 2; ++mi ) {
+          const int r = wm + mi * 16 + gid;
+          a[mi][0] = ld32( &As[r][ks + 2 * tig] );
+          a[mi][1] = ld32( &As[r + 8][ks + 2 * tig] );
+          a[mi][2] = ld32( &As[r][ks + 2 * tig + 8] );
+          a[mi][3] = ld32( &As[r + 8][ks + 2 * tig + 8] );
+        }
+#pragma unroll
+        for ( int ni = 0; ni < 4; ++ni ) {
+          const int c = wn + ni * 8 + gid;
+          b[ni][0] = ld32( &Bs[c][ks + 2 * tig] );
+          b[ni][1] = ld32( &Bs[c][ks + 2 * tig + 8] );
+        }
+#pragma unroll
+        for ( int mi = 0; mi < 2; ++mi )
+#pragma unroll
+          for ( int ni = 0; ni < 4; ++ni )
+            asm volatile( "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+                          "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                          : "+f"( acc[mi][ni][0] ), "+f"( acc[mi][ni][1] ), "+f"( acc[mi][ni][2] ),
+                            "+f"( acc[mi][ni][3] )
+                          : "r"( a[mi][0] ), "r"( a[mi][1] ), "r"( a[mi][2] ), "r"( a[mi][3] ),
+                            "r"( b[ni][0] ), "r"( b[ni][1] ) );
+      }
+      __syncthreads();
+    }
+    // epilogue: acc[mi][ni][0,1] at row gid, cols 2*tig+{0,1}; [2,3] at row gid+8
+#pragma unroll
+    for ( int mi = 0; mi < 2; ++mi )
+#pragma unroll
+      for ( int ni = 0; ni < 4; ++ni )
+#pragma unroll
+        for ( int h = 0; h < 2; ++h ) {
+          const int m = m0 + wm + mi * 16 + gid + 8 * h;
+          if ( m >= g.M )
+            continue;
+#pragma unroll
+          for ( int e = 0; e < 2; ++e ) {
+            const int n = n0 + wn + ni * 8 + 2 * tig + e;
+            if ( n >= g.N )
+              continue;
+            float v = acc[mi][ni][2 * h + e];
+            const long o = (long)m * g.ldc + n;
+            if ( g.mode == EPI_ATOMIC ) {
+              atomicAdd( g.Cf + o, v );
+              continue;
+            }
+            if ( g.mode == EPI_MASK ) {
+              if ( !( __bfloat162float( g.mask[(long)m * g.ldm + n] ) > 0.f ) )
+                v = 0.f;
+            } else {
+              if ( g.bias )
+                v += g.bias[n];
+            }
+            if ( g.Cf )
+              g.Cf[o] = v;
+            if ( g.Cb )
+              g.Cb[o] = __float2bfloat16( ( g.relu && v < 0.f ) ? 0.f : v );
+          }
+        }
+  }
+
+  // ---- features of (log E, T) -------------------------------------------------
+  // x0 = log E mapped linearly from [log emin, log emax] to [-1, 1]; x1 = T
+  // mapped from [tmin, tmax] to [-1, 1]; features x0, x1, x0*x1 and
+  // sin/cos(k pi x0), k = 1..8; the rest zero.
+  __device__ __forceinline__ void features( float loge, float temp, const Ranges& rg, bf16* out )
+  {
+    const float x0 = 2.f * ( loge - rg.loge_min ) / ( rg.loge_max - rg.loge_min ) - 1.f;
+    const float x1 = 2.f * ( temp - rg.t_min ) / ( rg.t_max - rg.t_min ) - 1.f;
+    float f[kIn];
+#pragma unroll
+    for ( int i = 0; i < kIn; ++i )
+      f[i] = 0.f;
+    f[0] = x0;
+    f[1] = x1;
+    f[2] = x0 * x1;
+#pragma unroll
+    for ( int k = 1; k <= 8; ++k ) {
+      float s, c;
+      sincospif( k * x0, &s, &c );
+      f[1 + 2 * k] = s;
+      f[2 + 2 * k] = c;
+    }
+#pragma unroll
+    for ( int i = 0; i < kIn; ++i )
+      out[i] = __float2bfloat16( f[i] );
+  }
+
+  // Training batch: samples drawn with replacement (Philox stream (seed, step)).
+  __global__ void k_gather( const float* loge, const float* temp, const float* target, uint64_t n,
+                            int batch, uint64_t seed, uint32_t step, Ranges rg, bf16* x0, float* tgt )
+  {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( b >= batch )
+      return;
+    ncgb_rng r;
+    ncgb_rng_init( &r, seed, (uint32_t)b, step, 0x6d6c7000u );
+    const uint64_t i = (uint64_t)( ncgb_rng_generate( &r ) * (double)n ) % n;
+    features( loge[i], temp[i], rg, x0 + (long)b * kIn );
+    tgt[b] = target[i];
+  }
+
+  // Features of the first 'n' samples in order (gradient check, inference).
+  __global__ void k_features( const float* loge, const float* temp, int n, Ranges rg, bf16* x0 )
+  {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( b < n )
+      features( loge[b], temp[b], rg, x0 + (long)b * kIn );
+    else if ( b < ( ( n + BM - 1 ) / BM ) * BM )
+      for ( int i = 0; i < kIn; ++i )
+        x0[(long)b * kIn + i] = __float2bfloat16( 0.f );
+  }
+
+  __device__ __forceinline__ float softplusf( float x ) { return x > 20.f ? x : log1pf( expf( x ) ); }
+  __device__ __forceinline__ float sigmoidf( float x ) { return 1.f / ( 1.f + expf( -x ) ); }
+
+  // Pinball loss over the 62 quantile levels and its gradient with respect to
+  // the raw outputs (scaled by 1/batch); loss summed into *loss.
+  __global__ void k_loss( const float* out, const float* tgt, int batch, bf16* d_out, float* loss )
+  {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.f;
+    if ( b < batch ) {
+      const float* o = out + (long)b * kOutPad;
+      const float a = tgt[b];
+      float gk[kOut];
+      float g = 0.f;
+      for ( int i = 0; i < kOut; ++i ) {
+        g = ( i == 0 ) ? o[0] : g + softplusf( o[i] );
+        const float tau = float( i + 1 ) / float( kOut + 1 );
+        const float r = a - g;
+        l += r * ( r < 0.f ? tau - 1.f : tau );
+        gk[i] = ( ( a < g ) ? 1.f : 0.f ) - tau;
+      }
+      const float inv = 1.f / float( batch );
+      float suffix = 0.f;
+      bf16* d = d_out + (long)b * kOutPad;
+      for ( int i = kOut - 1; i >= 0; --i ) {
+        suffix += gk[i];
+        const float v = ( i == 0 ? suffix : suffix * sigmoidf( o[i] ) ) * inv;
+        d[i] = __float2bfloat16( v );
+      }
+      for ( int i = kOut; i < kOutPad; ++i )
+        d[i] = __float2bfloat16( 0.f );
+      l *= inv;
+    }
+    // warp sum, one atomic per warp
+    for ( int s = 16; s > 0; s >>= 1 )
+      l += __shfl_down_sync( 0xffffffffu, l, s );
+    if ( ( threadIdx.x & 31 ) == 0 && loss )
+      atomicAdd( loss, l );
+  }
+
+  // Knots g (asinh(beta) quantiles) from raw outputs, for inference.
+  __global__ void k_knots( const float* out, int n, float* knots )
+  {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( b >= n )
+      return;
+    const float* o = out + (long)b * kOutPad;
+    float g = 0.f;
+    for ( int i = 0; i < kOut; ++i ) {
+      g = ( i == 0 ) ? o[0] : g + softplusf( o[i] );
+      knots[(long)b * kOut + i] = g;
+    }
+  }
+
+  // Column sums of a [rows x cols] BF16 matrix added into grad[cols].
+  __global__ void k_colsum( const bf16* m, int rows, int cols, int rows_per_block, float* grad )
+  {
+    const int c = threadIdx.x;
+    if ( c >= cols )
+      return;
+    const int r0 = blockIdx.x * rows_per_block;
+    const int r1 = min( rows, r0 + rows_per_block );
+    float s = 0.f;
+    for ( int r = r0; r < r1; ++r )
+      s += __bfloat162float( m[(long)r * cols + c] );
+    atomicAdd( grad + c, s );
+  }
+
+  __global__ void k_adam( float* w, float* m, float* v, const float* grad, bf16* wb, int n,
+                          float lr, float b1, float b2, float c1, float c2, float eps )
+  {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i >= n )
+      return;
+    const float g = grad[i];
+    const float mi = b1 * m[i] + ( 1.f - b1 ) * g;
+    const float vi = b2 * v[i] + ( 1.f - b2 ) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * ( mi / c1 ) / ( sqrtf( vi / c2 ) + eps );
+    w[i] = wi;
+    wb[i] = __float2bfloat16( wi );
+  }
+
+  __global__ void k_tobf16( const float* w, bf16* wb, int n )
+  {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( i < n )
+      wb[i] = __float2bfloat16( w[i] );
+  }
+
+  // ---- host side ---------------------------------------------------------------
+  struct Net {
+  public:
+    Net( int device, uint64_t seed );
+    ~Net();
+    Net( const Net& ) = delete;
+    Net& operator=( const Net& ) = delete;
+
+    int device() const { return m_device; }
+    const Layout& params() const { return m_L; }
+    Ranges& ranges() { return m_rg; }
+    const Ranges& ranges() const { return m_rg; }
+    void setParams( const float* host );
+    void getParams( float* host ) const;
+
+    // Loss and gradients (summed into h_grad, flat layout) on the first n
+    // samples; returns the mean pinball loss.
+    float gradients( const float* d_loge, const float* d_temp, const float* d_target, int n, float* h_grad,
+                     cudaStream_t s );
+    // Adam steps on batches drawn with replacement from n samples; the mean
+    // loss of every 'trace_every' steps goes to h_trace.
+    void train( const float* d_loge, const float* d_temp, const float* d_target, uint64_t n, uint64_t steps,
+                int batch, float lr, uint64_t seed, float* h_trace, uint64_t trace_every, cudaStream_t s );
+    // Knots (asinh(beta) quantiles, kOut per point) at n points.
+    void knots( const float* d_loge, const float* d_temp, int n, float* d_knots, cudaStream_t s );
+
+  private:
+    void alloc();
+    void ensureBatch( int batch );
+    void forward( int batch, cudaStream_t s );
+    void backward( int batch, cudaStream_t s );
+    float readLoss( cudaStream_t s );
+
+    int m_device;
+    Layout m_L;
+    Ranges m_rg{ -11.512925f, 0.6931472f, 250.f, 350.f };
+    uint64_t m_step = 0;
+    float* m_w = nullptr;   // FP32 master weights
+    float* m_m = nullptr;   // Adam moments
+    float* m_v = nullptr;
+    float* m_g = nullptr;   // gradients
+    bf16* m_wb = nullptr;  // BF16 copy for the GEMMs
+    void* m_act = nullptr;
+    float* m_loss = nullptr;
+    int m_cap = 0;
+    bf16* m_x0 = nullptr;
+    bf16* m_h[4] = {};
+    float* m_out = nullptr;
+    bf16* m_dout = nullptr;
+    bf16* m_dh[2] = {};
+    float* m_tgt = nullptr;
+  };
+
+
+  namespace {
+    void check( cudaError_t e, const char* what )
+    {
+      if ( e != cudaSuccess )
+        throw std::runtime_error( std::string( what ) + ": " + cudaGetErrorString( e ) );
+    }
+
+    int cdiv( long a, long b ) { return int( ( a + b - 1 ) / b ); }
+
+    void gemm( const GemmArgs& g, cudaStream_t s )
+    {
+      dim3 grid( cdiv( g.N, BN ), cdiv( g.M, BM ), cdiv( g.K, g.kchunk ) );
+      k_gemm<<<grid, 128, 0, s>>>( g );
+    }
+
+    GemmArgs base()
+    {
+      GemmArgs g;
+      std::memset( &g, 0, sizeof(g) );
+      return g;
+    }
+  }
+
+  Layout layout()
+  {
+    Layout L;
+    const int din[kLayers] = { kIn, kHidden, kHidden, kHidden, kHidden };
+    const int dout[kLayers] = { kHidden, kHidden, kHidden, kHidden, kOutPad };
+    long off = 0;
+    for ( int l = 0; l < kLayers; ++l ) {
+      L.din[l] = din[l];
+      L.dout[l] = dout[l];
+      L.w[l] = off;
+      off += (long)din[l] * dout[l];
+      L.b[l] = off;
+      off += dout[l];
+    }
+    L.total = off;
+    return L;
+  }
+
+  Net::Net( int device, uint64_t seed ) : m_device( device )
+  {
+    check( cudaSetDevice( device ), "cudaSetDevice" );
+    m_L = layout();
+    // He-uniform initial weights from the Philox stream (seed, layer); zero
+    // hidden biases; output biases that start the 62 knots evenly spaced over
+    // [-4, 4] in asinh(beta) (softplus(-1.98) = 8/62); the output layer's
+    // padding columns stay zero.
+    std::vector<float> h( m_L.total, 0.f );
+    h[m_L.b[kLayers - 1]] = -4.f;
+    for ( int o = 1; o < kOut; ++o )
+      h[m_L.b[kLayers - 1] + o] = -1.98f;
+    for ( int l = 0; l < kLayers; ++l ) {
+      ncgb_rng r;
+      ncgb_rng_init( &r, seed, (uint32_t)l, 0u, 0x6d6c7001u );
+      const float lim = std::sqrt( 6.f / float( l == 0 ? kInUsed : m_L.din[l] ) ) * ( l == kLayers - 1 ? 0.1f : 1.f );
+      for ( int i = 0; i < m_L.din[l]; ++i )
+        for ( int o = 0; o < m_L.dout[l]; ++o ) {
+          const float u = float( ncgb_rng_generate( &r ) );
+          const bool used = ( l != 0 || i < kInUsed ) && ( l != kLayers - 1 || o < kOut );
+          h[m_L.w[l] + (long)i * m_L.dout[l] + o] = used ? ( 2.f * u - 1.f ) * lim : 0.f;
+        }
+    }
+    alloc();
+    setParams( h.data() );
+  }
+
+  void Net::alloc()
+  {
+    const std::size_t n = m_L.total;
+    check( cudaMalloc( &m_w, n * sizeof(float) ), "cudaMalloc (mlp)" );
+    check( cudaMalloc( &m_m, n * sizeof(float) ), "cudaMalloc (mlp)" );
+    check( cudaMalloc( &m_v, n * sizeof(float) ), "cudaMalloc (mlp)" );
+    check( cudaMalloc( &m_g, n * sizeof(float) ), "cudaMalloc (mlp)" );
+    check( cudaMalloc( &m_wb, n * sizeof(bf16) ), "cudaMalloc (mlp)" );
+    check( cudaMemset( m_m, 0, n * sizeof(float) ), "cudaMemset" );
+    check( cudaMemset( m_v, 0, n * sizeof(float) ), "cudaMemset" );
+    check( cudaMemset( m_g, 0, n * sizeof(float) ), "cudaMemset" );
+  }
+
+  Net::~Net()
+  {
+    int cur = -1;
+    cudaGetDevice( &cur );
+    cudaSetDevice( m_device );
+    for ( void* p : { (void*)m_w, (void*)m_m, (void*)m_v, (void*)m_g, (void*)m_wb, m_act, (void*)m_loss } )
+      if ( p )
+        cudaFree( p );
+    cudaSetDevice( cur );
+  }
+
+  void Net::setParams( const float* h )
+  {
+    check( cudaMemcpy( m_w, h, m_L.total * sizeof(float), cudaMemcpyHostToDevice ), "cudaMemcpy (mlp)" );
+    k_tobf16<<<cdiv( m_L.total, 256 ), 256>>>( m_w, m_wb, (int)m_L.total );
+    check( cudaGetLastError(), "k_tobf16" );
+    check( cudaDeviceSynchronize(), "mlp params" );
+  }
+
+  void Net::getParams( float* h ) const
+  {
+    check( cudaMemcpy( h, m_w, m_L.total * sizeof(float), cudaMemcpyDeviceToHost ), "cudaMemcpy (mlp)" );
+  }
+
+  void Net::ensureBatch( int batch )
+  {
+    if ( batch <= m_cap )
+      return;
+    if ( m_act ) {
+      check( cudaDeviceSynchronize(), "mlp resize" );
+      cudaFree( m_act );
+      m_act = nullptr;
+    }
+    if ( !m_loss )
+      check( cudaMalloc( &m_loss, 64 ), "cudaMalloc (mlp)" );
+    const long bp = (long)cdiv( batch, BM ) * BM;
+    // x0 | h1..h4 | out(f32) | dout | dh (2 ping-pong) | tgt
+    const long bytes = bp * kIn * 2 + 4 * bp * kHidden * 2 + bp * kOutPad * 4 + bp * kOutPad * 2
+                       + 2 * bp * kHidden * 2 + bp * 4 + 1024;
+    check( cudaMalloc( &m_act, bytes ), "cudaMalloc (mlp activations)" );
+    char* p = static_cast<char*>( m_act );
+    auto take = [&]( long n ) { char* q = p; p += ( n + 255 ) & ~255L; return q; };
+    m_x0 = reinterpret_cast<bf16*>( take( bp * kIn * 2 ) );
+    for ( int l = 0; l < 4; ++l )
+      m_h[l] = reinterpret_cast<bf16*>( take( bp * kHidden * 2 ) );
+    m_out = reinterpret_cast<float*>( take( bp * kOutPad * 4 ) );
+    m_dout = reinterpret_cast<bf16*>( take( bp * kOutPad * 2 ) );
+    m_dh[0] = reinterpret_cast<bf16*>( take( bp * kHidden * 2 ) );
+    m_dh[1] = reinterpret_cast<bf16*>( take( bp * kHidden * 2 ) );
+    m_tgt = reinterpret_cast<float*>( take( bp * 4 ) );
+    m_cap = batch;
+  }
+
+  // Forward pass on m_x0 (rows = batch, padded to BM with zero features).
+  void Net::forward( int batch, cudaStream_t s )
+  {
+    const bf16* in = m_x0;
+    for ( int l = 0; l < kLayers; ++l ) {
+      GemmArgs g = base();
+      g.A = in; g.sAm = m_L.din[l]; g.sAk = 1;
+      g.B = m_wb + m_L.w[l]; g.sBk = m_L.dout[l]; g.sBn = 1;
+      g.M = batch; g.N = m_L.dout[l]; g.K = m_L.din[l]; g.kchunk = g.K;
+      g.mode = EPI_STORE;
+      g.bias = m_w + m_L.b[l];
+      g.ldc = m_L.dout[l];
+      if ( l < kLayers - 1 ) {
+        g.relu = 1;
+        g.Cb = m_h[l];
+        in = m_h[l];
+      } else {
+        g.Cf = m_out;
+      }
+      gemm( g, s );
+    }
+  }
+
+  // Backward pass from m_dout (dL/d raw outputs); gradients added into m_g.
+  void Net::backward( int batch, cudaStream_t s )
+  {
+    const int kchunk = 1024;
+    const bf16* dz = m_dout;   // dL/dz of layer l
+    for ( int l = kLayers - 1; l >= 0; --l ) {
+      const bf16* a_in = ( l == 0 ) ? m_x0 : m_h[l - 1];
+      // dW_l += a_in^T dz
+      GemmArgs gw = base();
+      gw.A = a_in; gw.sAm = 1; gw.sAk = m_L.din[l];
+      gw.B = dz; gw.sBk = m_L.dout[l]; gw.sBn = 1;
+      gw.M = m_L.din[l]; gw.N = m_L.dout[l]; gw.K = batch; gw.kchunk = kchunk;
+      gw.mode = EPI_ATOMIC;
+      gw.Cf = m_g + m_L.w[l];
+      gw.ldc = m_L.dout[l];
+      gemm( gw, s );
+      // db_l += colsum(dz)
+      const int rpb = 256;
+      k_colsum<<<cdiv( batch, rpb ), 128, 0, s>>>( dz, batch, m_L.dout[l], rpb, m_g + m_L.b[l] );
+      if ( l == 0 )
+        break;
+      // dz_(l-1) = (dz W_l^T) * (h_(l-1) > 0)
+      bf16* dn = m_dh[l & 1];
+      GemmArgs gd = base();
+      gd.A = dz; gd.sAm = m_L.dout[l]; gd.sAk = 1;
+      gd.B = m_wb + m_L.w[l]; gd.sBk = 1; gd.sBn = m_L.dout[l];
+      gd.M = batch; gd.N = m_L.din[l]; gd.K = m_L.dout[l]; gd.kchunk = gd.K;
+      gd.mode = EPI_MASK;
+      gd.mask = m_h[l - 1]; gd.ldm = m_L.din[l];
+      gd.Cb = dn; gd.ldc = m_L.din[l];
+      gemm( gd, s );
+      dz = dn;
+    }
+  }
+
+  float Net::readLoss( cudaStream_t s )
+  {
+    float l = 0.f;
+    check( cudaMemcpyAsync( &l, m_loss, sizeof(float), cudaMemcpyDeviceToHost, s ), "loss D2H" );
+    check( cudaStreamSynchronize( s ), "loss" );
+    return l;
+  }
+
+  float Net::gradients( const float* d_loge, const float* d_temp, const float* d_target, int n, float* h_grad,
+                        cudaStream_t s )
+  {
+    ensureBatch( n );
+    k_features<<<cdiv( cdiv( n, BM ) * BM, 128 ), 128, 0, s>>>( d_loge, d_temp, n, m_rg, m_x0 );
+    check( cudaMemcpyAsync( m_tgt, d_target, n * sizeof(float), cudaMemcpyDeviceToDevice, s ), "D2D" );
+    check( cudaMemsetAsync( m_g, 0, m_L.total * sizeof(float), s ), "memset" );
+    check( cudaMemsetAsync( m_loss, 0, sizeof(float), s ), "memset" );
+    forward( n, s );
+    k_loss<<<cdiv( n, 128 ), 128, 0, s>>>( m_out, m_tgt, n, m_dout, m_loss );
+    backward( n, s );
+    check( cudaGetLastError(), "mlp kernels" );
+    check( cudaMemcpyAsync( h_grad, m_g, m_L.total * sizeof(float), cudaMemcpyDeviceToHost, s ), "D2H" );
+    return readLoss( s );
+  }
+
+  void Net::train( const float* d_loge, const float* d_temp, const float* d_target, uint64_t n, uint64_t steps,
+                   int batch, float lr, uint64_t seed, float* h_trace, uint64_t trace_every, cudaStream_t s )
+  {
+    if ( batch <= 0 || batch % BM )
+      throw std::runtime_error( "mlp training batch must be a positive multiple of 64" );
+    if ( n == 0 )
+      throw std::runtime_error( "mlp training set is empty" );
+    ensureBatch( batch );
+    check( cudaMemsetAsync( m_loss, 0, sizeof(float), s ), "memset" );
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    uint64_t traced = 0;
+    for ( uint64_t it = 0; it < steps; ++it ) {
+      ++m_step;
+      // cosine decay to 5% of lr
+      const float frac = steps > 1 ? float( it ) / float( steps - 1 ) : 0.f;
+      const float lrt = lr * ( 0.05f + 0.95f * 0.5f * ( 1.f + std::cos( 3.14159265f * frac ) ) );
+      k_gather<<<cdiv( batch, 128 ), 128, 0, s>>>( d_loge, d_temp, d_target, n, batch, seed, (uint32_t)m_step,
+                                                   m_rg, m_x0, m_tgt );
+      check( cudaMemsetAsync( m_g, 0, m_L.total * sizeof(float), s ), "memset" );
+      forward( batch, s );
+      k_loss<<<cdiv( batch, 128 ), 128, 0, s>>>( m_out, m_tgt, batch, m_dout, m_loss );
+      backward( batch, s );
+      const float c1 = 1.f - std::pow( b1, float( m_step ) ), c2 = 1.f - std::pow( b2, float( m_step ) );
+      k_adam<<<cdiv( m_L.total, 256 ), 256, 0, s>>>( m_w, m_m, m_v, m_g, m_wb, (int)m_L.total, lrt, b1, b2, c1, c2,
+                                                     eps );
+      if ( trace_every && h_trace && ( it + 1 ) % trace_every == 0 ) {
+        h_trace[traced++] = readLoss( s ) / float( trace_every );
+        check( cudaMemsetAsync( m_loss, 0, sizeof(float), s ), "memset" );
+      }
+    }
+    check( cudaGetLastError(), "mlp training kernels" );
+    check( cudaStreamSynchronize( s ), "mlp training" );
+  }
+
+  void Net::knots( const float* d_loge, const float* d_temp, int n, float* d_knots, cudaStream_t s )
+  {
+    ensureBatch( n );
+    k_features<<<cdiv( cdiv( n, BM ) * BM, 128 ), 128, 0, s>>>( d_loge, d_temp, n, m_rg, m_x0 );
+    forward( n, s );
+    k_knots<<<cdiv( n, 128 ), 128, 0, s>>>( m_out, n, d_knots );
+    check( cudaGetLastError(), "mlp inference" );
+  }
+}
+
+namespace ncgb_mlp {
+  Net* create( int device, uint64_t seed ) { return new Net( device, seed ); }
+  void destroy( Net* n ) { delete n; }
+  long nparams() { return layout().total; }
+  int device( const Net* n ) { return n->device(); }
+  void setParams( Net* n, const float* h ) { n->setParams( h ); }
+  void getParams( const Net* n, float* h ) { n->getParams( h ); }
+  void setRanges( Net* n, const Ranges& r ) { n->ranges() = r; }
+  Ranges getRanges( const Net* n ) { return n->ranges(); }
+  float gradients( Net* n, const float* a, const float* b, const float* c, int k, float* g, cudaStream_t s )
+  {
+    return n->gradients( a, b, c, k, g, s );
+  }
+  void train( Net* n, const float* a, const float* b, const float* c, uint64_t k, uint64_t steps, int batch, float lr,
+              uint64_t seed, float* tr, uint64_t te, cudaStream_t s )
+  {
+    n->train( a, b, c, k, steps, batch, lr, seed, tr, te, s );
+  }
+  void knots( Net* n, const float* a, const float* b, int k, float* out, cudaStream_t s ) { n->knots( a, b, k, out, s ); }
+}

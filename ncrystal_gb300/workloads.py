@@ -72,7 +72,14 @@ def config(name):
     raise KeyError(name)
 
 
+# Polyethylene instances the learned beta proposal is trained on (K).
+PE_TRAIN_TEMPS = [250.0, 265.0, 280.0, 293.0, 305.0, 320.0, 335.0, 350.0]
+
+
+def pe_cfg(T):
+    return "Polyethylene_CH2.ncmat;temp=%gK" % T
+
+
 # cfg-strings whose bundles the default build exports (the single-material
-# workloads; the crystal batch is exported on demand, it is ~250 MB).
-DEFAULT_BUNDLE_CFGS = [AL, AL2O3, PE293, WATER,
-                       "Polyethylene_CH2.ncmat;temp=280K", "Polyethylene_CH2.ncmat;temp=320K"]
+# workloads and the proposal's training instances).
+DEFAULT_BUNDLE_CFGS = [AL, AL2O3, WATER] + [pe_cfg(T) for T in PE_TRAIN_TEMPS]

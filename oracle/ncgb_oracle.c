@@ -378,8 +378,46 @@ static double ora_sample_alpha( const ncgb_sab_view* s, int64_t ie, size_t ibeta
   }
 }
 
+/* Learned beta proposal of sampler ie (tables of ncgb_proposal.cc; no
+ * reference counterpart): interval from the alias table, a 32-bit draw w
+ * placing beta = q + (2w+1) h in it, accepted with probability y/env, y from
+ * the interval's linear pieces in w -- the same draws and arithmetic as the
+ * GPU.  Returns 1 with (beta, bin) or 0 after 1000 rejected proposals. */
+static int ora_lp_beta( const ncgb_sab_view* s, int64_t ie, ncgb_rng* rng, double* beta_out, size_t* bin_out )
+{
+  const ncgb_lp_slot* slots = s->lp_slot + ie * NCGB_LP_K;
+  const ncgb_lp_cell* cells = s->lp_cell + ie * NCGB_LP_K;
+  for ( int tries = 0; tries < 1000; ++tries ) {
+    const uint64_t prod = (uint64_t)ncgb_rng_u32( rng ) * (uint64_t)NCGB_LP_K;
+    const int j = (int)( prod >> 32 );
+    const float fr = (float)( (uint32_t)prod >> 8 ) * ( 1.0f / 16777216.0f );
+    const int k = ( fr < slots[j].aprob ) ? j : slots[j].alias;
+    const ncgb_lp_cell* c = cells + k;
+    const uint32_t w = ncgb_rng_u32( rng );
+    int lo = c->seg_lo, hi = c->seg_lo + c->seg_n - 1;
+    while ( lo < hi ) {
+      const int mid = ( lo + hi + 1 ) >> 1;
+      if ( s->lp_seg[mid].w0 <= w )
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const ncgb_lp_seg* g = s->lp_seg + lo;
+    const float y = fmaf( g->slope, (float)( w - g->w0 ), g->y0 );
+    const float ua = (float)( ncgb_rng_u32( rng ) >> 8 ) * ( 1.0f / 16777216.0f );
+    if ( ua * c->env < y ) {
+      *beta_out = fma( (double)( 2ull * w + 1ull ), c->h, c->q );
+      *bin_out = (size_t)g->bin;
+      return 1;
+    }
+  }
+  return 0;
+}
+
 /* SABSamplerAtE_Alg1::sampleAlphaBeta, NCSABSamplerModels.cc:48-155.
- * Returns ORA_OK or ORA_LOOPCAP. */
+ * Returns ORA_OK or ORA_LOOPCAP.  With a learned proposal attached and
+ * enabled for sampler ie, beta of the regular range comes from ora_lp_beta
+ * and the first bin keeps its probability bcdf[1]. */
 static int ora_alg1( const ncgb_sab_view* s, int64_t ie, double ekin_div_kT, ncgb_rng* rng,
                      double* alpha_out, double* beta_out )
 {
@@ -391,10 +429,20 @@ static int ora_alg1( const ncgb_sab_view* s, int64_t ie, double ekin_div_kT, ncg
   const size_t ioff = (size_t)s->smp_ibetaoffset[ie];
   const double fbkep = s->smp_fbkep[ie];
   const double* bg = s->beta;
+  const int learned = s->lp_hdr && s->lp_hdr[ie].enabled;
   for ( int iloop = 0; iloop < 100; ++iloop ) {
-    size_t ibs;
-    double beta = ora_percentile( bx, by, bcdf, nbs, ncgb_rng_generate( rng ), &ibs );
-    if ( ibs == 0 && fbkep <= 0.0 ) {
+    size_t ibs = 0;
+    double beta = 0.0;
+    int first_bin;
+    if ( learned ) {
+      first_bin = ncgb_rng_u32( rng ) < s->lp_hdr[ie].c1_thr;
+      if ( !first_bin && !ora_lp_beta( s, ie, rng, &beta, &ibs ) )
+        return ORA_LOOPCAP;
+    } else {
+      beta = ora_percentile( bx, by, bcdf, nbs, ncgb_rng_generate( rng ), &ibs );
+      first_bin = ( ibs == 0 && fbkep <= 0.0 );
+    }
+    if ( first_bin ) {
       const double b0 = fbkep;
       const double b1 = bx[1];
       if ( b1 < -ekin_div_kT )
@@ -1111,7 +1159,7 @@ int64_t ncgb_oracle_scatter_many( const ncgb_material_view* m, const double* eki
     ncgb_rng_init( &rng, seed, (uint32_t)( i + index_offset ), callseq, stream );
     int st = ncgb_oracle_scatter( m, &rng, ekin[i], &out_ef[i], &out_mu[i] );
     if ( out_status ) out_status[i] = st;
-    if ( out_ndraws ) out_ndraws[i] = (int32_t)( 2 * rng.block - rng.have );
+    if ( out_ndraws ) out_ndraws[i] = (int32_t)ncgb_rng_ndoubles( &rng );
     if ( st ) ++nbad;
   }
   return nbad;

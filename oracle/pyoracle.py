@@ -83,6 +83,47 @@ class HostMaterial:
             raise KeyError(name)
         return v.value
 
+    # ---- learned beta proposal tables -----------------------------------------
+    LP_HDR = np.dtype([("c1", "<f8"), ("c1_thr", "<u4"), ("accept", "<f4"), ("enabled", "<i4"), ("pad", "<i4")])
+    LP_SLOT = np.dtype([("aprob", "<f4"), ("alias", "<i4")])
+    LP_CELL = np.dtype([("q", "<f8"), ("h", "<f8"), ("env", "<f4"), ("seg_lo", "<i4"), ("seg_n", "<i4"),
+                        ("pad", "<i4")])
+    LP_SEG = np.dtype([("w0", "<u4"), ("y0", "<f4"), ("slope", "<f4"), ("bin", "<i4")])
+    LP_K = 126
+
+    def build_proposal(self, comp, knots, allowed=None, min_accept=0.5):
+        """The library's proposal tables from knots[ne, 62] (asinh(beta)):
+        -> (hdr[ne], slot[ne, K], cell[ne, K], seg[nseg]) structured arrays."""
+        k = np.ascontiguousarray(knots, dtype=np.float32)
+        ne = k.shape[0]
+        al = None if allowed is None else np.ascontiguousarray(allowed, dtype=np.uint8)
+        nseg = C.c_ulong(0)
+        args = (C.c_void_p(self._h), comp, _P(k), None if al is None else _P(al), float(min_accept))
+        rc = self._L.ncgb_tables_build_proposal(*args, None, None, None, None, C.byref(nseg))
+        if rc != 2:
+            raise RuntimeError(self._L.ncgb_tables_lasterror().decode())
+        hdr = np.zeros(ne, dtype=self.LP_HDR)
+        slot = np.zeros((ne, self.LP_K), dtype=self.LP_SLOT)
+        cell = np.zeros((ne, self.LP_K), dtype=self.LP_CELL)
+        seg = np.zeros(max(1, nseg.value), dtype=self.LP_SEG)
+        if self._L.ncgb_tables_build_proposal(*args, _P(hdr), _P(slot), _P(cell), _P(seg), C.byref(nseg)):
+            raise RuntimeError(self._L.ncgb_tables_lasterror().decode())
+        return hdr, slot, cell, seg[:nseg.value]
+
+    def set_proposal(self, comp, tables):
+        """Make the oracle sample component 'comp' with these proposal tables
+        ((hdr, slot, cell, seg) from build_proposal, or None to remove them)."""
+        if tables is None:
+            rc = self._L.ncgb_tables_set_proposal(C.c_void_p(self._h), comp, None, None, None, None, 0)
+        else:
+            hdr, slot, cell, seg = (np.ascontiguousarray(a, dtype=d) for a, d in
+                                    zip(tables, (self.LP_HDR, self.LP_SLOT, self.LP_CELL, self.LP_SEG)))
+            rc = self._L.ncgb_tables_set_proposal(C.c_void_p(self._h), comp, _P(hdr), _P(slot), _P(cell), _P(seg),
+                                                  len(seg))
+        if rc:
+            raise RuntimeError("ncgb_tables_set_proposal failed")
+        self._L.ncgb_tables_view(C.c_void_p(self._h), self.view)
+
     # ---- oracle evaluation ----------------------------------------------------
     def xs(self, ekin):
         e = np.ascontiguousarray(ekin, dtype=np.float64)
