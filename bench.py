@@ -223,6 +223,17 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(x, dist, dev):
+    """The largest value of x over all ranks (x itself without a process
+    group): timings of replicas are combined by their slowest rank."""
+    if not dist:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def config_of(args, wl, world):
     cfgs = wl["cfgs"]
     return {"workload": args.workload, "cfg": cfgs[0] if len(cfgs) == 1 else "%d instances" % len(cfgs),
@@ -435,11 +446,7 @@ def run_gb300(args):
             R.timed_step(stream)
             b.record(stream)
         barrier()
-    ms = sum(a.elapsed_time(b) for a, b in evs)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs), dist, dev)
     ms_per_step = ms / args.steps
     value = world * n * args.steps / (ms / 1e3)
 
@@ -459,11 +466,7 @@ def run_gb300(args):
             R.timed_step(stream)
             b.record(stream)
         barrier()
-        pms = sum(a.elapsed_time(b) for a, b in pev)
-        if dist:
-            t = torch.tensor([pms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            pms = float(t.item())
+        pms = max_over_ranks(sum(a.elapsed_time(b) for a, b in pev), dist, dev)
         plain = {"value": world * n * args.steps / (pms / 1e3), "ms_per_step": pms / args.steps}
         R.set_sampler("learned")
     peak, peak_kind = measured_peaks()
@@ -494,11 +497,7 @@ def run_gb300(args):
     for _ in range(e2e_steps):
         R.e2e_step()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
     e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT, "steps": e2e_steps}
     e2e.update(R.e2e_info())
 
