@@ -115,6 +115,8 @@ typedef struct {
   int32_t n;
   double msd[NCGB_MAX_ELINC];
   double sigma[NCGB_MAX_ELINC]; /* bound incoherent xs * scale */
+  float msd_f[NCGB_MAX_ELINC];  /* FP32 copies (mixed-precision mode) */
+  float sigma_f[NCGB_MAX_ELINC];
 } ncgb_elinc_view;
 
 typedef struct {
@@ -130,6 +132,8 @@ typedef struct {
   /* energy grid */
   const double* egrid;  /* [ne] */
   const double* xs;     /* [ne] */
+  const float* egrid_f; /* [ne] FP32 copy (mixed-precision mode) */
+  const float* xsf;     /* [2*ne] (xs_i, (xs_i+1 - xs_i)/(egrid_i+1 - egrid_i)) in FP32 */
   /* kernel grid, S stored beta-major: idx = ibeta*na + ialpha */
   const double* alpha;  /* [na] */
   const double* beta;   /* [nb] */
@@ -166,7 +170,7 @@ typedef struct {
 
 typedef struct {
   int32_t type;
-  int32_t pad0;
+  float scale_f;               /* FP32 copy of scale (mixed-precision mode) */
   double scale, elow, ehigh;
   ncgb_bragg_view bragg;
   ncgb_elinc_view elinc;

@@ -99,6 +99,12 @@ namespace ncgb_dev {
   __device__ __forceinline__ double clampd( double x, double lo, double hi ) { return x < lo ? lo : ( x > hi ? hi : x ); }
   __device__ __forceinline__ double maxd( double a, double b ) { return a < b ? b : a; }
   __device__ __forceinline__ bool contains( double lo, double hi, double e ) { return e >= lo && e <= hi; }
+  // The same for lo >= 0 and e >= 0 (not NaN), compared as int64 bit patterns.
+  __device__ __forceinline__ bool containsNN( double lo, double hi, double e )
+  {
+    const long long b = bits( e );
+    return b >= bits( lo ) && b <= bits( hi );
+  }
   __device__ __forceinline__ bool finited( double x ) { return ( bits(x) & 0x7FF0000000000000LL ) != 0x7FF0000000000000LL; }
   __device__ __forceinline__ double infd() { return __longlong_as_double( 0x7FF0000000000000LL ); }
 
@@ -171,6 +177,43 @@ namespace ncgb_dev {
   constexpr double kElIncXS = 16.0 * 9.86960440108935861883449099987615113531369941 * 12.22430978582345950656;
   constexpr double kElIncMu = 8.0 * 9.86960440108935861883449099987615113531369941 * 12.22430978582345950656;
 
+  // ---- FP32 cross-sections of the mixed-precision mode ---------------------------
+  // Same formulas as the FP64 ones below, in FP32 (relative error ~1e-7).
+  __device__ __forceinline__ float oneMinusExpMtDivTf( float t )
+  {
+    if ( t < 0.01f )
+      return 1.0f + t * ( -0.5f + t * 0.16666667f * ( 1.0f - 0.25f * t ) );
+    if ( t > 24.0f )
+      return 1.0f / t;
+    return expm1f( -t ) / ( -t );
+  }
+
+  __device__ __forceinline__ float elincXSf( const ncgb_elinc_view& v, float ekin )
+  {
+    const float e = (float)kElIncXS * ekin;
+    float xs = 0.0f;
+    for ( int i = 0; i < v.n && i < NCGB_MAX_ELINC; ++i )
+      xs = fmaf( v.sigma_f[i], oneMinusExpMtDivTf( v.msd_f[i] * e ), xs );
+    return xs;
+  }
+
+  // first i in [0, n) with a[i] > x, for non-negative floats (int compares)
+  __device__ __forceinline__ int upper_bound_f( const float* a, int n, float x )
+  {
+    const int key = __float_as_int( x );
+    int lo = 0, len = n;
+    while ( len > 0 ) {
+      const int half = len >> 1;
+      if ( __float_as_int( __ldg( a + lo + half ) ) <= key ) {
+        lo += half + 1;
+        len -= half + 1;
+      } else {
+        len = half;
+      }
+    }
+    return lo;
+  }
+
   // ElIncXS::evaluate (NCElIncXS.cc:117-128)
   template<bool Fast>
   __device__ __forceinline__ double elincXS( const ncgb_elinc_view& v, double ekin )
@@ -229,10 +272,46 @@ namespace ncgb_dev {
     return xs * s.internal_scale;
   }
 
+  // SAB cross-section in FP32 below Emax (FP64 above: the extender).
+  __device__ __forceinline__ float sabXSf( const ncgb_sab_view& s, double ekin, float ef )
+  {
+    const int ne = s.ne;
+    const int iu = upper_bound_f( s.egrid_f, ne, ef );
+    if ( iu == ne )
+      return (float)sabXS( s, ekin );
+    float xs;
+    if ( iu == 0 ) {
+      xs = ef > 0.0f ? sqrtf( __ldg( s.egrid_f ) / ef ) * __ldg( s.xsf ) : __int_as_float( 0x7f800000 );
+    } else {
+      const float2 p = __ldg( reinterpret_cast<const float2*>( s.xsf ) + ( iu - 1 ) );
+      xs = fmaf( p.y, ef - __ldg( s.egrid_f + iu - 1 ), p.x );
+    }
+    return xs * (float)s.internal_scale;
+  }
+
+  __device__ __forceinline__ float compXSf( const ncgb_comp_view& c, double ekin, float ef )
+  {
+    if ( !containsNN( c.elow, c.ehigh, ekin ) )
+      return 0.0f;
+    int64_t idx;
+    switch ( c.type ) {
+      case NCGB_COMP_ELINC: return elincXSf( c.elinc, ef );
+      case NCGB_COMP_BRAGG: {
+        if ( c.bragg.n == 0 || ekin < c.bragg.threshold )
+          return 0.0f;
+        idx = upper_bound_nn( c.bragg.two_dE + 1, c.bragg.n - 1, ekin );
+        return (float)ldg( c.bragg.fdm_commul + idx ) / ef;
+      }
+      case NCGB_COMP_SAB: return sabXSf( c.sab, ekin, ef );
+      case NCGB_COMP_FREEGAS: return (float)( c.fg.sigma_free * freeGasShape( c.fg.ca * ekin ) );
+      default: return 0.0f;
+    }
+  }
+
   template<bool Fast>
   __device__ __forceinline__ double compXS( const ncgb_comp_view& c, double ekin )
   {
-    if ( !contains( c.elow, c.ehigh, ekin ) )
+    if ( !containsNN( c.elow, c.ehigh, ekin ) )
       return 0.0;
     int64_t dummy;
     switch ( c.type ) {
@@ -249,9 +328,46 @@ namespace ncgb_dev {
   // with the cumulative cross-sections in registers (fully unrolled).
   struct XSPick { double xs; int comp; };
 
+  // Mixed-precision mode: the same with FP32 cumulative sums (the Bragg plane
+  // search and the FP64 Bragg sums themselves are unchanged).
+  template<bool Pick>
+  __device__ __forceinline__ XSPick xsAndPickF( const ncgb_material_view& m, double ekin, ncgb_rng& rng )
+  {
+    const float ef = (float)ekin;
+    float commul[NCGB_MAX_COMP];
+    float tot = 0.0f;
+#pragma unroll
+    for ( int i = 0; i < NCGB_MAX_COMP; ++i ) {
+      if ( i < m.ncomp )
+        tot = fmaf( m.comp[i].scale_f, compXSf( m.comp[i], ekin, ef ), tot );
+      commul[i] = tot;
+    }
+    XSPick r{ (double)tot, 0 };
+    if ( !Pick || m.ncomp <= 1 )
+      return r;
+    const float choice = tot * (float)rand01( rng );
+    const int n = m.ncomp;
+    int pick = n - 1;
+    if ( n < 5 ) {
+#pragma unroll
+      for ( int i = NCGB_MAX_COMP - 1; i >= 0; --i )
+        if ( i < n && commul[i] > choice )
+          pick = i;
+    } else {
+#pragma unroll
+      for ( int i = NCGB_MAX_COMP - 1; i >= 0; --i )
+        if ( i < n && commul[i] >= choice )
+          pick = i;
+    }
+    r.comp = pick;
+    return r;
+  }
+
   template<bool Pick, bool Fast>
   __device__ __forceinline__ XSPick xsAndPick( const ncgb_material_view& m, double ekin, ncgb_rng& rng )
   {
+    if ( Fast )
+      return xsAndPickF<Pick>( m, ekin, rng );
     double commul[NCGB_MAX_COMP];
     double tot = 0.0;
 #pragma unroll
@@ -304,6 +420,28 @@ namespace ncgb_dev {
   // ElIncXS::sampleMuMonoAtomic, NCElIncXS.cc:81-115.  The reference's
   // rejection loop is unbounded; its acceptance is above 98% here, and the
   // cap only guards the GPU.
+  // FP32 version of elincMuMono (mixed-precision mode).
+  __device__ __noinline__ float elincMuMonoF( ncgb_rng& rng, float ekin, float msd, int& status )
+  {
+    const float a = ( (float)kElIncMu * ekin ) * msd;
+    if ( a < 0.01f ) {
+      const float maxval = 1.0f + a * ( 1.0f + a * ( 0.5f + a * ( 0.16666667f + a * 0.041666668f ) ) );
+      for ( int it = 0; it < 100000; ++it ) {
+        const float mu = (float)rand01( rng ) * 2.0f - 1.0f;
+        const float x = a * mu;
+        if ( (float)rand01( rng ) * maxval < 1.0f + x * ( 1.0f + x * ( 0.5f + x * ( 0.16666667f + x * 0.041666668f ) ) ) )
+          return mu;
+      }
+      status = NCGB_ST_LOOPCAP;
+      return 1.0f;
+    }
+    // for a > 20, log1p(R*expm1(2a))/a - 1 = 1 + log(R)/a to within exp(-40),
+    // which also avoids FP32 overflow of expm1(2a)
+    const float r = (float)rand01( rng );
+    const float m = a > 20.0f ? 1.0f + logf( r ) / a : log1pf( r * expm1f( 2.0f * a ) ) / a - 1.0f;
+    return fminf( 1.0f, fmaxf( -1.0f, m ) );
+  }
+
   template<bool Fast>
   __device__ __noinline__ double elincMuMono( ncgb_rng& rng, double ekin, double msd, int& status )
   {
@@ -331,9 +469,32 @@ namespace ncgb_dev {
 
   // ElIncXS::EPointAnalysis::sampleMu, NCElIncXS.cc:178-191 (element picked
   // by pickRandIdxByWeight on the cumulative contributions).
+  // FP32 version of elincMu (mixed-precision mode).
+  __device__ __noinline__ double elincMuF( const ncgb_elinc_view& v, ncgb_rng& rng, double ekin, int& status )
+  {
+    const float ef = (float)ekin;
+    if ( v.n == 1 )
+      return (double)elincMuMonoF( rng, ef, v.msd_f[0], status );
+    const float e = (float)kElIncXS * ef;
+    float tot = 0.0f;
+    for ( int i = 0; i < v.n && i < NCGB_MAX_ELINC; ++i )
+      tot = fmaf( v.sigma_f[i], oneMinusExpMtDivTf( v.msd_f[i] * e ), tot );
+    const float choice = tot * (float)rand01( rng );
+    int pick = v.n - 1;
+    float c = 0.0f;
+    const bool linear = v.n < 5;
+    for ( int i = 0; i < v.n && i < NCGB_MAX_ELINC; ++i ) {
+      c = fmaf( v.sigma_f[i], oneMinusExpMtDivTf( v.msd_f[i] * e ), c );
+      if ( linear ? ( c > choice ) : ( c >= choice ) ) { pick = i; break; }
+    }
+    return (double)elincMuMonoF( rng, ef, v.msd_f[pick], status );
+  }
+
   template<bool Fast>
   __device__ __noinline__ double elincMu( const ncgb_elinc_view& v, ncgb_rng& rng, double ekin, int& status )
   {
+    if ( Fast )
+      return elincMuF( v, rng, ekin, status );
     if ( v.n == 1 )
       return elincMuMono<Fast>( rng, ekin, v.msd[0], status );
     const double e = kElIncXS * ekin;

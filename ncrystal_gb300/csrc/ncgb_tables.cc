@@ -484,6 +484,7 @@ namespace ncgb {
       const std::string p = "c" + std::to_string(ic) + ".";
       ncgb_comp_view& c = v.comp[ic];
       c.scale = b.f64s(p+"scale");
+      c.scale_f = static_cast<float>( c.scale );
       c.elow = b.f64s(p+"elow");
       c.ehigh = b.f64s(p+"ehigh");
       const std::string& type = b.str(p+"type");
@@ -507,6 +508,8 @@ namespace ncgb {
         for ( std::size_t i = 0; i < msd.size(); ++i ) {
           c.elinc.msd[i] = msd[i];
           c.elinc.sigma[i] = sig[i];
+          c.elinc.msd_f[i] = static_cast<float>( msd[i] );
+          c.elinc.sigma_f[i] = static_cast<float>( sig[i] );
         }
       } else if ( type == "SABScatter" ) {
         c.type = NCGB_COMP_SAB;
@@ -567,6 +570,17 @@ namespace ncgb {
           inv_dbeta[i] = 1.0 / ( in.beta[i+1] - in.beta[i] );
         s.inv_dE = encodeOff<double>( mt->put( inv_dE ) );
         s.inv_dbeta = encodeOff<double>( mt->put( inv_dbeta ) );
+        // FP32 cross-section tables of the mixed-precision mode (xs before
+        // internal_scale, as in the FP64 tables)
+        std::vector<float> egf( in.egrid.size() ), xsf( 2 * in.egrid.size(), 0.0f );
+        for ( std::size_t i = 0; i < in.egrid.size(); ++i ) {
+          egf[i] = static_cast<float>( in.egrid[i] );
+          xsf[2*i] = static_cast<float>( d.xs[i] );
+          if ( i + 1 < in.egrid.size() )
+            xsf[2*i+1] = static_cast<float>( ( d.xs[i+1] - d.xs[i] ) / ( in.egrid[i+1] - in.egrid[i] ) );
+        }
+        s.egrid_f = encodeOff<float>( mt->put( egf ) );
+        s.xsf = encodeOff<float>( mt->put( xsf ) );
         std::vector<ncgb_beta_bin> bbin( d.bx.size() );
         std::memset( bbin.data(), 0, bbin.size() * sizeof(ncgb_beta_bin) );
         for ( std::size_t ie = 0; ie < d.kind.size(); ++ie ) {
@@ -677,6 +691,8 @@ namespace ncgb {
       s.bcdf = reloc( s.bcdf, base );
       s.info = reloc( s.info, base );
       s.inv_dE = reloc( s.inv_dE, base );
+      s.egrid_f = reloc( s.egrid_f, base );
+      s.xsf = reloc( s.xsf, base );
       s.inv_dbeta = reloc( s.inv_dbeta, base );
       s.bbin = reloc( s.bbin, base );
       s.acell = reloc( s.acell, base );
