@@ -50,6 +50,16 @@ typedef struct {
   double inv_back;     /* 1/(1-prob_notback) */
 } ncgb_alpha_info;
 
+/* FP32 copy of ncgb_alpha_info for the mixed-precision mode. */
+typedef struct {
+  float front_alpha, front_sval, front_logsval;
+  float back_alpha, back_sval, back_logsval;
+  float prob_front, prob_notback;
+  float inv_front, inv_middle, inv_back;
+  uint32_t front_idx, back_idx;
+  float pad[3];
+} ncgb_alpha_info_f;
+
 /* One bin [x0,x1] of a beta sampler's piecewise-linear density, with the
  * constants of PointwiseDist::percentileWithIndex's in-bin inversion
  * (NCPointwiseDist.cc:84-109) precomputed: a = y0, d = y1-y0, dx = x1-x0,
@@ -156,6 +166,14 @@ typedef struct {
   const double* inv_dbeta;        /* [nb] 1/(beta[i+1]-beta[i]) */
   const ncgb_beta_bin* bbin;      /* [offset + j]: bin j of a sampler, j < nbeta-1 */
   const ncgb_alpha_cell* acell;   /* [nb*na] */
+  /* FP32 copies for the mixed-precision mode's alpha sampling */
+  const float* alpha_f;           /* [na] */
+  const float* sab_f;             /* [nb*na] */
+  const float* logsab_f;          /* [nb*na] */
+  const float* cumul_f;           /* [nb*na] */
+  const float* acell_f;           /* [nb*na*4]: inv_bin, ratio, slope (NaN: degenerate), 0 */
+  const float* inv_dbeta_f;       /* [nb] */
+  const ncgb_alpha_info_f* info_f; /* indexed like info */
   /* learned beta proposal (NULL: none attached): lp_hdr[ne], lp_slot[ne*NCGB_LP_K],
    * lp_cell[ne*NCGB_LP_K], lp_seg[...] */
   const ncgb_lp_hdr* lp_hdr;

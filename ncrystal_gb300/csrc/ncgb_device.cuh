@@ -629,11 +629,88 @@ namespace ncgb_dev {
                    p2, ldg( logsab + bi ), ldg( &info->back_logsval ) );
   }
 
+  // ---- FP32 alpha sampling of the mixed-precision mode -----------------------
+  // sampleLogLinDist_fast and SABSamplerAtE_Alg1::sampleAlpha as above, on the
+  // FP32 table copies.  The degenerate-branch tests compare the factors with
+  // zero one by one (a product of small FP32 values could underflow).
+  __device__ __forceinline__ float logLinF( float a, float fa, float b, float fb, float rnd, float logfa, float logfb )
+  {
+    float df = fb - fa;
+    if ( fa != 0.0f && fb != 0.0f && df != 0.0f ) {
+      const float L = logfb - logfa;
+      if ( a != b && L != 0.0f )
+        return a + ( b - a ) * ( log1pf( rnd * df / fa ) / L );
+      df = 0.0f;
+    }
+    if ( df == 0.0f )
+      return a + rnd * ( b - a );
+    const float xx = ( b - a ) * sqrtf( rnd );
+    return ( fa != 0.0f ) ? b - xx : a + xx;
+  }
+
+  __device__ __forceinline__ float clampRandF( float r ) { return fminf( 1.0f, fmaxf( 1.17549435e-38f, r ) ); }
+
+  __device__ __forceinline__ float sampleAlphaF( const ncgb_sab_view& s, const ncgb_alpha_info_f* infos,
+                                                 int64_t ioff, int64_t ibeta, float rp )
+  {
+    const ncgb_alpha_info_f* info = infos + ( ibeta - ioff );
+    const float prob_front = __ldg( &info->prob_front );
+    const int64_t na = s.na;
+    const float* cumul = s.cumul_f + ibeta * na;
+    const float* sab = s.sab_f + ibeta * na;
+    const float* logsab = s.logsab_f + ibeta * na;
+    if ( rp <= prob_front ) {
+      const float fa = __ldg( &info->front_alpha );
+      if ( prob_front == 2.0f )
+        return fa + rp * ( __ldg( &info->back_alpha ) - fa );
+      if ( prob_front == 1.0f )
+        return logLinF( fa, __ldg( &info->front_sval ), __ldg( &info->back_alpha ), __ldg( &info->back_sval ),
+                        rp, __ldg( &info->front_logsval ), __ldg( &info->back_logsval ) );
+      const uint32_t fi = __ldg( &info->front_idx );
+      const float p2 = clampRandF( rp * __ldg( &info->inv_front ) );
+      return logLinF( fa, __ldg( &info->front_sval ), __ldg( s.alpha_f + fi ), __ldg( sab + fi ),
+                      p2, __ldg( &info->front_logsval ), __ldg( logsab + fi ) );
+    }
+    const float prob_notback = __ldg( &info->prob_notback );
+    if ( rp <= prob_notback ) {
+      const float p2 = fminf( 1.0f, fmaxf( 0.0f, ( rp - prob_front ) * __ldg( &info->inv_middle ) ) );
+      const int il = __ldg( &info->front_idx ), iu = __ldg( &info->back_idx );
+      const float cl = __ldg( cumul + il ), cu = __ldg( cumul + iu );
+      const float sel = fmaf( p2, cu - cl, cl );
+      const int e = il + upper_bound_f( cumul + il, iu + 1 - il, sel );
+      if ( e > iu )
+        return __ldg( s.alpha_f + iu );
+      if ( e <= il )
+        return __ldg( s.alpha_f + il );
+      const int a0 = e - 1;
+      const float4 cell = __ldg( reinterpret_cast<const float4*>( s.acell_f ) + ( ibeta * na + a0 ) );
+      const float rr = clampRandF( ( sel - __ldg( cumul + a0 ) ) * cell.x );
+      if ( cell.z == cell.z )
+        return fmaf( cell.z, log1pf( rr * cell.y ), __ldg( s.alpha_f + a0 ) );
+      return logLinF( __ldg( s.alpha_f + a0 ), __ldg( sab + a0 ), __ldg( s.alpha_f + a0 + 1 ), __ldg( sab + a0 + 1 ),
+                      rr, __ldg( logsab + a0 ), __ldg( logsab + a0 + 1 ) );
+    }
+    const uint32_t bi = __ldg( &info->back_idx );
+    const float p2 = clampRandF( ( rp - prob_notback ) * __ldg( &info->inv_back ) );
+    return logLinF( __ldg( s.alpha_f + bi ), __ldg( sab + bi ), __ldg( &info->back_alpha ), __ldg( &info->back_sval ),
+                    p2, __ldg( logsab + bi ), __ldg( &info->back_logsval ) );
+  }
+
+  // alpha of row 'ibeta' at percentile rp, in the arithmetic of the mode
+  template<bool Fast>
+  __device__ __forceinline__ double rowAlpha( const ncgb_sab_view& s, int64_t off, int64_t ioff, int64_t ibeta,
+                                             double rp )
+  {
+    if ( Fast )
+      return (double)sampleAlphaF( s, s.info_f + off, ioff, ibeta, (float)rp );
+    return sampleAlpha<Fast>( s, s.info + off, ioff, ibeta, rp );
+  }
+
   // First beta bin with a kinematic endpoint (NCSABSamplerModels.cc:69-116):
   // beta uniform in the bin, alpha from the first row, up to 30 tries.
   // Returns 1 if (alpha, beta) is accepted, 0 if the attempt is rejected.
   template<bool Fast>
-  __device__ __noinline__ int alg1FirstBin( const ncgb_sab_view& s, const ncgb_alpha_info* infos, int64_t ioff,
+  __device__ __noinline__ int alg1FirstBin( const ncgb_sab_view& s, int64_t off, int64_t ioff,
                                             double fbkep, double b1, double x, ncgb_rng& rng,
                                             double& alpha_out, double& beta_out )
   {
@@ -647,7 +724,7 @@ namespace ncgb_dev {
       beta = maxd( fbkep, b0 + delta_beta * rand01( rng ) );
       if ( beta < -x )
         break;
-      alphaval = sampleAlpha<Fast>( s, infos, ioff, ioff, rand01( rng ) );
+      alphaval = rowAlpha<Fast>( s, off, ioff, ioff, rand01( rng ) );
       const ALim al = alphaLimits( -fbkep, beta );
       if ( inInterval( al.lo, al.hi, alphaval ) )
         break;
@@ -737,13 +814,13 @@ namespace ncgb_dev {
       // the special first bin keeps its probability bcdf[1]; the regular
       // range is drawn from the learned proposal
       if ( rand_u32( rng ) < __ldg( &s.lp_hdr[ie].c1_thr ) )
-        return alg1FirstBin<Fast>( s, infos, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+        return alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
       if ( !lpBeta( s, ie, rng, beta, ibs ) )
         return -1;
     } else {
       beta = percentile( bx, s.bcdf + off, s.bbin + off, nbs, rand01( rng ), ibs );
       if ( ibs == 0 && fbkep <= 0.0 )
-        return alg1FirstBin<Fast>( s, infos, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+        return alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
     }
     if ( beta <= maxd( -x, ldg( s.beta ) ) )
       return 0;
@@ -752,9 +829,17 @@ namespace ncgb_dev {
     if ( ibeta < 1 )
       return 0; // cannot happen (beta above the beta grid front); keeps indices in bounds
     const double bl = ldg( s.beta + ibeta - 1 );
-    const double alphal = sampleAlpha<Fast>( s, infos, ioff, ibeta - 1, rp );
-    const double alphah = sampleAlpha<Fast>( s, infos, ioff, ibeta, rp );
-    const double alpha = alphal + ( alphah - alphal ) * ( ( beta - bl ) * ldg( s.inv_dbeta + ibeta - 1 ) );
+    double alpha;
+    if ( Fast ) {
+      const float rpf = (float)rp;
+      const float al = sampleAlphaF( s, s.info_f + off, ioff, ibeta - 1, rpf );
+      const float ah = sampleAlphaF( s, s.info_f + off, ioff, ibeta, rpf );
+      alpha = (double)fmaf( ah - al, (float)( beta - bl ) * __ldg( s.inv_dbeta_f + ibeta - 1 ), al );
+    } else {
+      const double alphal = sampleAlpha<Fast>( s, infos, ioff, ibeta - 1, rp );
+      const double alphah = sampleAlpha<Fast>( s, infos, ioff, ibeta, rp );
+      alpha = alphal + ( alphah - alphal ) * ( ( beta - bl ) * ldg( s.inv_dbeta + ibeta - 1 ) );
+    }
     const ALim al = alphaLimits( x, beta );
     if ( inInterval( al.lo, al.hi, alpha ) ) {
       alpha_out = alpha;
@@ -847,11 +932,14 @@ namespace ncgb_dev {
           return -1;
         }
       } // else SABSamplerAtE_NoScatter: (alpha, beta) = (0, 0), no draws
-      // an Alg.1 call completed: the outer loop's tests
+      // an Alg.1 call completed: the outer loop's tests.  Alg.1 accepted
+      // (alpha, beta) only if beta >= -xsamp and alpha is inside the limits
+      // at xsamp; unless the energy is below the grid, xsamp == x and these
+      // tests repeat that computation, so their outcome is known.
       L.inner = 0;
       const double x = L.x;
-      bool accept = false;
-      if ( !( beta < -x ) ) {
+      bool accept = !L.ultra_small && __ldg( s.smp_kind + L.ie ) != 0;
+      if ( !accept && !( beta < -x ) ) {
         const ALim al = alphaLimits( x, beta );
         if ( inInterval( al.lo, al.hi, alpha ) ) {
           accept = true;

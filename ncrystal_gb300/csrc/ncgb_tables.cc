@@ -630,6 +630,45 @@ namespace ncgb {
           }
         }
         s.acell = encodeOff<ncgb_alpha_cell>( mt->put( acell.data(), acell.size() ) );
+        // FP32 copies of the alpha-sampling tables (mixed-precision mode)
+        auto tof = []( const std::vector<double>& v ) {
+          std::vector<float> f( v.size() );
+          for ( std::size_t i = 0; i < v.size(); ++i )
+            f[i] = static_cast<float>( v[i] );
+          return f;
+        };
+        s.alpha_f = encodeOff<float>( mt->put( tof( in.alpha ) ) );
+        s.sab_f = encodeOff<float>( mt->put( tof( in.sab ) ) );
+        s.logsab_f = encodeOff<float>( mt->put( tof( d.logsab ) ) );
+        s.cumul_f = encodeOff<float>( mt->put( tof( d.cumul ) ) );
+        s.inv_dbeta_f = encodeOff<float>( mt->put( tof( inv_dbeta ) ) );
+        std::vector<float> acf( 4 * acell.size(), 0.0f );
+        for ( std::size_t g = 0; g < acell.size(); ++g ) {
+          acf[4*g] = static_cast<float>( acell[g].inv_bin );
+          acf[4*g+1] = static_cast<float>( acell[g].ratio );
+          acf[4*g+2] = static_cast<float>( acell[g].slope );
+        }
+        s.acell_f = encodeOff<float>( mt->put( acf ) );
+        std::vector<ncgb_alpha_info_f> inff( d.info.size() );
+        std::memset( inff.data(), 0, inff.size() * sizeof(ncgb_alpha_info_f) );
+        for ( std::size_t i = 0; i < d.info.size(); ++i ) {
+          const ncgb_alpha_info& a = d.info[i];
+          ncgb_alpha_info_f& f = inff[i];
+          f.front_alpha = static_cast<float>( a.front_alpha );
+          f.front_sval = static_cast<float>( a.front_sval );
+          f.front_logsval = static_cast<float>( a.front_logsval );
+          f.back_alpha = static_cast<float>( a.back_alpha );
+          f.back_sval = static_cast<float>( a.back_sval );
+          f.back_logsval = static_cast<float>( a.back_logsval );
+          f.prob_front = static_cast<float>( a.prob_front );
+          f.prob_notback = static_cast<float>( a.prob_notback );
+          f.inv_front = static_cast<float>( a.inv_front );
+          f.inv_middle = static_cast<float>( a.inv_middle );
+          f.inv_back = static_cast<float>( a.inv_back );
+          f.front_idx = a.front_idx;
+          f.back_idx = a.back_idx;
+        }
+        s.info_f = encodeOff<ncgb_alpha_info_f>( mt->put( inff.data(), inff.size() ) );
       } else if ( type == "FreeGas" ) {
         c.type = NCGB_COMP_FREEGAS;
         c.fg.kT = b.f64s(p+"kT");
@@ -696,6 +735,13 @@ namespace ncgb {
       s.inv_dbeta = reloc( s.inv_dbeta, base );
       s.bbin = reloc( s.bbin, base );
       s.acell = reloc( s.acell, base );
+      s.alpha_f = reloc( s.alpha_f, base );
+      s.sab_f = reloc( s.sab_f, base );
+      s.logsab_f = reloc( s.logsab_f, base );
+      s.cumul_f = reloc( s.cumul_f, base );
+      s.acell_f = reloc( s.acell_f, base );
+      s.inv_dbeta_f = reloc( s.inv_dbeta_f, base );
+      s.info_f = reloc( s.info_f, base );
     }
     return v;
   }
