@@ -4,14 +4,22 @@
 One step = one pass of the hot path over one batch: for every neutron its
 total cross-section and one sampled isotropic scatter (E', mu).
 
-Default workload ("al2o3_large"): Al2O3_sg167_Corundum.ncmat;temp=293K;
-dcutoff=0.2 (2,886 merged Bragg d-spacings, ElInc, two S(alpha,beta)
-kernels), 2^24 neutrons with energies log-uniform in [1e-4, 1] eV (seeded),
-FP32 energies in and FP32 results out, FP64 arithmetic.  Other workloads:
-al_small (Al at 293 K, 2^20 neutrons, wavelengths uniform in [0.5, 5] Aa, FP64
-I/O), pe (Polyethylene at 293 K, 2^24, FP64 I/O) and crystal_batch (64
-(material, T) instances of 16 crystals at 77/150/293/400 K, ragged neutron
-counts log-uniform in [1e3, 1e6], one batch launch replayed as a CUDA graph).
+Default workload ("pe"): Polyethylene_CH2.ncmat;temp=293K (ElInc + two
+S(alpha,beta) kernels), 2^24 neutrons with energies log-uniform in [1e-4, 1] eV
+(seeded), FP64 I/O, the mixed-precision mode (FP64 for the Bragg sums, the
+beta-CDF inversion and the kinematics; FP32 elsewhere), and the learned beta
+proposal: its networks are trained on the GPU before timing (untimed; the
+training's size and time are reported), and the plain sampler is timed on the
+same handle and inputs beside it ("plain_sampler", "learned_vs_plain").
+Other workloads: al2o3_large (Al2O3, dcutoff 0.2, 2,886 merged Bragg
+d-spacings, 2^24 neutrons log-uniform in [1e-4, 1] eV, FP32 I/O), al_small
+(Al, 2^20 neutrons, wavelengths uniform in [0.5, 5] Aa), crystal_batch (64
+(material, T) instances of 16 crystals at 77/150/293/400 K, ragged counts
+log-uniform in [1e3, 1e6]) and mixed_batch (32 instances: water, polyethylene
+at 280/293/320 K with the learned proposal, 28 crystal instances; ragged counts
+log-uniform in [1e4, 2e6], energies log-uniform in [1e-5, 2] eV); batches are
+one launch pair replayed as a CUDA graph.  --mode exact computes in FP64
+throughout (the reference's results to rounding).
 
   value  -- device-resident batch (two kernels: k_pick, k_sab), inputs
             already in HBM
@@ -19,7 +27,8 @@ counts log-uniform in [1e3, 1e6], one batch launch replayed as a CUDA graph).
             inside the timed region
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-       [--workload al2o3_large|al_small|pe|crystal_batch]
+       [--workload pe|al2o3_large|al_small|crystal_batch|mixed_batch]
+       [--mode mixed|exact] [--sampler auto|plain|learned]
 Under torchrun (N>1) each rank runs an independent replica on its own GPU
 (the path has no cross-neutron exchange: replicas only) and rank 0 prints the
 JSON line with the whole-job throughput.
@@ -64,6 +73,12 @@ def workload(name, rank):
         return dict(cfgs=cfg["cfgs"], counts=counts, io="f64",
                     energies=[W.loguniform_energies(c, 1e-4, 1.0, 0x5EED0003 + 1000 * rank + k)
                               for k, c in enumerate(counts)])
+    if name == "mixed_batch":
+        cfg = W.config("mixed_batch")
+        counts = [int(c) for c in cfg["counts"]]
+        return dict(cfgs=cfg["cfgs"], counts=counts, io="f64",
+                    energies=[W.loguniform_energies(c, 1e-5, 2.0, 0x5EED0005 + 1000 * rank + k)
+                              for k, c in enumerate(counts)])
     raise KeyError(name)
 
 
@@ -74,14 +89,14 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="pe",
-                    choices=["al2o3_large", "al_small", "pe", "crystal_batch"])
+                    choices=["pe", "al2o3_large", "al_small", "crystal_batch", "mixed_batch"])
     ap.add_argument("--sampler", default="auto", choices=["auto", "plain", "learned"],
                     help="S(alpha,beta) beta sampling: plain percentile inversion, or the learned proposal "
                          "(trained on the GPU before timing; the plain sampler is timed beside it). "
-                         "auto: learned for the polyethylene workload, plain otherwise")
+                         "auto: learned for the workloads with polyethylene, plain otherwise")
     ap.add_argument("--train-samples", type=int, default=1 << 26)
     ap.add_argument("--train-steps", type=int, default=6000)
-    ap.add_argument("--mode", default="exact", choices=["exact", "mixed"],
+    ap.add_argument("--mode", default="mixed", choices=["exact", "mixed"],
                     help="arithmetic mode of the GPU path (mixed: FP32 incoherent-elastic exponentials "
                          "and alpha inversion, FP64 elsewhere)")
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
@@ -320,13 +335,15 @@ class BatchRunner:
     """Ragged multi-material batch: autotuned shape, CUDA-graph replay on
     device arrays; host arrays through ncgb_batch_xs_scatter_many."""
 
-    def __init__(self, NC, torch, wl, dev, seed, mode):
+    def __init__(self, NC, torch, wl, dev, seed, mode, prepare=None):
         self.torch = torch
         self.f32 = False
         e = np.concatenate(wl["energies"]).astype(np.float64)
         self.n = len(e)
         offs = np.concatenate([[0], np.cumsum(wl["counts"])]).astype(np.int64)
-        self.batch = NC.Batch([NC.createScatter(c, seed=seed + k) for k, c in enumerate(wl["cfgs"])])
+        scatters = [NC.createScatter(c, seed=seed + k) for k, c in enumerate(wl["cfgs"])]
+        self.prepared = prepare(scatters) if prepare else None   # e.g. proposals, before the batch copies views
+        self.batch = NC.Batch(scatters)
         self.batch.set_mode(mode)
         self.d_e = torch.from_numpy(e).to(dev)
         self.d_off = torch.from_numpy(offs).to(dev)
@@ -349,6 +366,9 @@ class BatchRunner:
 
     def timed_step(self, stream):
         self.batch.graph_launch(self.d_e, self.d_off, self.d_xs, self.d_ef, self.d_mu, None, stream=stream)
+
+    def set_sampler(self, sampler):
+        self.batch.set_sampler(sampler)
 
     def e2e_step(self):
         self.batch.xs_scatter_host_ptr(self.h_e.data_ptr(), self.h_off.data_ptr(), self.n, self.h_xs.data_ptr(),
@@ -380,28 +400,40 @@ def run_gb300(args):
     import ncrystal_gb300 as NC
 
     wl = workload(args.workload, rank)
+    is_pe = [c.startswith("Polyethylene_CH2.ncmat") for c in wl["cfgs"]]
     if args.sampler == "auto":
-        args.sampler = "learned" if args.workload == "pe" else "plain"
+        args.sampler = "learned" if any(is_pe) else "plain"
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
-    R = (BatchRunner if len(wl["cfgs"]) > 1 else SingleRunner)(NC, torch, wl, dev, 0xB0057 + 977 * rank, args.mode)
-    n = R.n
     learned = None
+    attach = None
     if args.sampler == "learned":
-        # Train the proposal networks on the GPU (untimed), attach them.
+        # Train the proposal networks on the GPU (untimed); attach them to the
+        # polyethylene instances (the plain sampler serves the others).
         import ncrystal_gb300.learn as LR
-        if len(wl["cfgs"]) != 1 or not wl["cfgs"][0].startswith("Polyethylene_CH2.ncmat"):
+        if not any(is_pe):
             raise SystemExit("bench: the learned proposal is trained for polyethylene workloads")
         t0 = time.perf_counter()
         nets, infos = LR.train_proposals(n_total=args.train_samples, steps=args.train_steps, seed=3 + rank)
         torch.cuda.synchronize()
-        acc = LR.attach(R.sc, nets)
-        learned = {"train_wall_s": time.perf_counter() - t0, "mean_envelope_acceptance": acc,
+        learned = {"train_wall_s": time.perf_counter() - t0,
                    "components": {str(c): {k: v for k, v in i.items() if k != "loss_trace"}
                                   for c, i in infos.items()},
                    "final_loss": {str(c): i["loss_trace"][-1] if i["loss_trace"] else None
                                   for c, i in infos.items()},
                    "network": "4x128 hidden, BF16 mma.sync + FP32 accumulation, trained by the library's kernels"}
+
+        def attach(scatters):
+            return [LR.attach(sc, nets) for sc, p in zip(scatters, is_pe) if p]
+    if len(wl["cfgs"]) > 1:
+        R = BatchRunner(NC, torch, wl, dev, 0xB0057 + 977 * rank, args.mode, prepare=attach)
+        acc = R.prepared
+    else:
+        R = SingleRunner(NC, torch, wl, dev, 0xB0057 + 977 * rank, args.mode)
+        acc = attach([R.sc]) if attach else None
+    n = R.n
+    if learned is not None:
+        learned["mean_envelope_acceptance"] = acc
         R.set_sampler("learned")
     esz = 4 if R.f32 else 8
     io_bytes = 4 * esz * n  # energies in, xs / E' / mu out

@@ -44,6 +44,13 @@ def crystal_batch_cfgs():
     return ["%s;temp=%dK" % (m, t) for m in CRYSTALS16 for t in CRYSTAL_TEMPS]
 
 
+def mixed_batch_cfgs():
+    """32 instances: liquid water (its one temperature), polyethylene at 280,
+    293 and 320 K, the 16 crystals at 293 K and the first 12 at 400 K."""
+    return ([WATER] + ["Polyethylene_CH2.ncmat;temp=%dK" % t for t in (280, 293, 320)]
+            + ["%s;temp=293K" % m for m in CRYSTALS16] + ["%s;temp=400K" % m for m in CRYSTALS16[:12]])
+
+
 def ragged_counts(ninst, lo, hi, seed):
     rng = np.random.Generator(np.random.PCG64(seed))
     return np.exp(rng.uniform(math.log(lo), math.log(hi), ninst)).astype(np.int64)
@@ -64,6 +71,11 @@ def config(name):
         cfgs = crystal_batch_cfgs()
         return dict(name=name, cfgs=cfgs, counts=list(ragged_counts(len(cfgs), 1e3, 1e6, 0x5EED0003)),
                     energies=lambda n, k=0: loguniform_energies(n, 1e-4, 1.0, 0x5EED0003 + 17 * (k + 1)),
+                    io="f64")
+    if name == "mixed_batch":
+        cfgs = mixed_batch_cfgs()
+        return dict(name=name, cfgs=cfgs, counts=list(ragged_counts(len(cfgs), 1e4, 2e6, 0x5EED0005)),
+                    energies=lambda n, k=0: loguniform_energies(n, 1e-5, 2.0, 0x5EED0005 + 31 * (k + 1)),
                     io="f64")
     if name == "pe_learned":
         return dict(name=name, cfgs=[PE293], counts=[1 << 24],
