@@ -130,6 +130,22 @@ namespace ncgb_dev {
 
   __device__ __forceinline__ bool inInterval( double lo, double hi, double x ) { return x >= lo && x <= hi; }
 
+  // The alpha limits in FP32 (mixed-precision mode) in a form free of
+  // cancellation: with s = sqrt(x+beta) + sqrt(x), alpha+ = s^2 and
+  // alpha- = (sqrt(x+beta) - sqrt(x))^2 = beta^2 / s^2 (relative error ~1e-7
+  // everywhere, including near the elastic line where the FP64 form needs its
+  // Taylor branch).  kk = x + beta is formed in FP64 by the caller.
+  struct ALimF { float lo, hi; };
+  __device__ __forceinline__ ALimF alphaLimitsF( float x, float kk, float beta )
+  {
+    ALimF r;
+    if ( !( kk >= 0.0f ) ) { r.lo = 1.0f; r.hi = -1.0f; return r; }
+    const float sq = sqrtf( kk ) + sqrtf( x );
+    r.hi = sq * sq;
+    r.lo = ( beta * beta ) / r.hi;
+    return r;
+  }
+
   __device__ __forceinline__ void neumaierAdd( double& s, double& c, double x )
   {
     double t = s + x;
@@ -834,7 +850,14 @@ namespace ncgb_dev {
       const float rpf = (float)rp;
       const float al = sampleAlphaF( s, s.info_f + off, ioff, ibeta - 1, rpf );
       const float ah = sampleAlphaF( s, s.info_f + off, ioff, ibeta, rpf );
-      alpha = (double)fmaf( ah - al, (float)( beta - bl ) * __ldg( s.inv_dbeta_f + ibeta - 1 ), al );
+      const float af = fmaf( ah - al, (float)( beta - bl ) * __ldg( s.inv_dbeta_f + ibeta - 1 ), al );
+      const ALimF lim = alphaLimitsF( (float)x, (float)( x + beta ), (float)beta );
+      if ( af >= lim.lo && af <= lim.hi ) {
+        alpha_out = (double)af;
+        beta_out = beta;
+        return 1;
+      }
+      return 0;
     } else {
       const double alphal = sampleAlpha<Fast>( s, infos, ioff, ibeta - 1, rp );
       const double alphah = sampleAlpha<Fast>( s, infos, ioff, ibeta, rp );

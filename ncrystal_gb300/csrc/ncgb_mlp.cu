@@ -508,7 +508,7 @@ namespace ncgb_mlp {
   // Backward pass from m_dout (dL/d raw outputs); gradients added into m_g.
   void Net::backward( int batch, cudaStream_t s )
   {
-    const int kchunk = 1024;
+    const int kchunk = 256;   // split-K over the batch: enough CTAs for the small weight GEMMs
     const bf16* dz = m_dout;   // dL/dz of layer l
     for ( int l = kLayers - 1; l >= 0; --l ) {
       const bf16* a_in = ( l == 0 ) ? m_x0 : m_h[l - 1];
