@@ -99,6 +99,18 @@ void ncrystal_genscatter_nonoriented_many( ncrystal_scatter_t,
                                            double* results_angle,
                                            double* results_dekin );
 
+/* Scatter with directions (ncrystal.h:782-786, ncrystal.cc:1159-1174 and
+ * :1248-1282): for non-oriented materials, an isotropic scatter followed by an
+ * outgoing direction at cosine mu to the incoming one with a uniform azimuth
+ * (randNeutronDirectionGivenScatterMu, NCRandUtils.cc:51-96).  The _many form
+ * repeats one energy and direction 'repeat' times.  On error: E' -1 and a
+ * zero direction. */
+void ncrystal_samplescatter( ncrystal_scatter_t, double ekin, const double (*direction)[3],
+                             double* ekin_final, double (*direction_final)[3] );
+void ncrystal_samplescatter_many( ncrystal_scatter_t, double ekin, const double (*direction)[3],
+                                  unsigned long repeat, double* results_ekin, double* results_dirx,
+                                  double* results_diry, double* results_dirz );
+
 /* Error handling (ncrystal.h:1031-1051; ncrystal.cc:281-322).  As in the
  * reference, an error prints its message and calls exit(1) unless
  * ncrystal_sethaltonerror(0) was called first. */
@@ -133,6 +145,13 @@ const char * ncrystal_version_str( void );
 int ncgb_scatter_device( ncrystal_scatter_t, const double* d_ekin, unsigned long n,
                          double* d_xs, double* d_ekin_final, double* d_mu,
                          int32_t* d_status, void* stream );
+
+/* Scatters with directions on device memory: d_ekin[n], d_dir[n][3] ->
+ * d_ekin_final[n], d_dir_final[n][3] (d_status optional); neutron i uses
+ * stream i as in ncgb_scatter_device, the direction's draws following the
+ * scatter's.  Asynchronous on 'stream'. */
+int ncgb_scatter_dir_device( ncrystal_scatter_t, const double* d_ekin, const double* d_dir, unsigned long n,
+                             double* d_ekin_final, double* d_dir_final, int32_t* d_status, void* stream );
 
 /* No counterpart in the reference.  Same as ncgb_scatter_device (FP64
  * arrays), but allocates nothing: its working memory is a fixed array inside

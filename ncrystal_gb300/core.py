@@ -107,6 +107,12 @@ def lib():
                                            _C.c_void_p, _C.c_void_p, _C.c_void_p]),
         "ncgb_batch_config": (_C.c_int, [_Handle, _C.POINTER(_C.c_int), _C.POINTER(_C.c_int)]),
         "ncgb_batch_set_mode": (_C.c_int, [_Handle, _C.c_int]),
+        "ncrystal_samplescatter": (None, [H, _C.c_double, _C.POINTER(_C.c_double * 3), _dblp,
+                                          _C.POINTER(_C.c_double * 3)]),
+        "ncrystal_samplescatter_many": (None, [H, _C.c_double, _C.POINTER(_C.c_double * 3), _C.c_ulong, _C.c_void_p,
+                                               _C.c_void_p, _C.c_void_p, _C.c_void_p]),
+        "ncgb_scatter_dir_device": (_C.c_int, [H, _C.c_void_p, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p,
+                                               _C.c_void_p, _C.c_void_p]),
         "ncgb_batch_set_sampler": (_C.c_int, [_Handle, _C.c_int]),
         "ncgb_set_sampler": (_C.c_int, [H, _C.c_int]),
         "ncgb_get_sampler": (_C.c_int, [H]),
@@ -367,6 +373,35 @@ class Scatter(Process):
                                                    mu.ctypes.data)
             _check()
         return ef, mu
+
+    def sampleScatter(self, ekin, direction, repeat=None):
+        """NCrystal core.py:1478: (ekin_final, (ux, uy, uz)) for one neutron, or
+        arrays (ekin_final, (ux, uy, uz)) of 'repeat' scatters of it."""
+        L = lib()
+        cdir = (_C.c_double * 3)(*[float(x) for x in direction])
+        if not repeat:
+            ef = _C.c_double()
+            out = (_C.c_double * 3)(0.0, 0.0, 0.0)
+            L.ncrystal_samplescatter(self._h, float(ekin), _C.byref(cdir), _C.byref(ef), _C.byref(out))
+            _check()
+            return ef.value, (out[0], out[1], out[2])
+        n = int(repeat)
+        ef, ux, uy, uz = (_np.empty(n) for _ in range(4))
+        L.ncrystal_samplescatter_many(self._h, float(ekin), _C.byref(cdir), n, ef.ctypes.data, ux.ctypes.data,
+                                      uy.ctypes.data, uz.ctypes.data)
+        _check()
+        return ef, (ux, uy, uz)
+
+    def scatter_dir_device(self, ekin, direction, ekin_final, direction_final, status=None, stream=None):
+        """Scatters with directions on CUDA tensors: ekin (n,) and direction
+        (n, 3) float64 in, ekin_final (n,) and direction_final (n, 3) out."""
+        import torch
+        if stream is None:
+            stream = torch.cuda.current_stream(ekin.device)
+        if lib().ncgb_scatter_dir_device(self._h, ekin.data_ptr(), direction.data_ptr(), ekin.numel(),
+                                         ekin_final.data_ptr(), direction_final.data_ptr(),
+                                         0 if status is None else status.data_ptr(), stream.cuda_stream):
+            _check()
 
     def genScatterNonOriented(self, ekin, repeat=None):
         """Obsolete NCrystal call: returns (angle, delta_ekin) arrays."""

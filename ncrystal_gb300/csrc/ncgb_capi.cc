@@ -766,6 +766,117 @@ void ncrystal_genscatter_nonoriented_many( ncrystal_scatter_t sc, const double* 
   } NCGB_CATCH;
 }
 
+// ---- sampleScatter with directions (ncrystal.cc:1159-1174, :1248-1282) -------------------
+namespace {
+  // One energy and direction per input neutron (host arrays), n_ekin x repeat
+  // outputs (index irepeat*n_ekin+i, like the _many calls).  Returns the
+  // number of failed neutrons.
+  unsigned long runScatterDir( ScatterObj& o, const double* ekin, const double* dir, unsigned long n_ekin,
+                               unsigned long repeat, double* out_ekin, double* out_dir )
+  {
+    checkSize( n_ekin, repeat );
+    const uint64_t n_out = (uint64_t)n_ekin * repeat;
+    if ( n_out == 0 )
+      return 0;
+    DeviceMaterial& dm = *o.mat;
+    Scratch& s = scratchFor( dm );
+    // d_in: energies then incoming directions; d_a: E'; d_c: outgoing directions
+    const std::size_t din = ( ( n_ekin * sizeof(double) + 255 ) & ~std::size_t(255) );
+    ensure( s.d_in, s.cap_in, din + 3 * n_ekin * sizeof(double) );
+    ensure( s.d_a, s.cap_a, n_out * sizeof(double) );
+    ensure( s.d_c, s.cap_c, 3 * n_out * sizeof(double) );
+    double* d_dir_in = reinterpret_cast<double*>( static_cast<char*>( s.d_in ) + din );
+    ncgb::Batch b = makeBatch( o, s, nextCall( o ) );
+    b.ekin = s.d_in;
+    b.n_ekin = n_ekin;
+    b.n_out = n_out;
+    b.mode = 0;
+    b.out_a = s.d_a;
+    b.dir_in = d_dir_in;
+    b.dir_out = static_cast<double*>( s.d_c );
+    resetNFail( s, s.stream );
+    checkCuda( cudaMemcpyAsync( s.d_in, ekin, n_ekin * sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
+    checkCuda( cudaMemcpyAsync( d_dir_in, dir, 3 * n_ekin * sizeof(double), cudaMemcpyHostToDevice, s.stream ),
+               "H2D" );
+    runBatch( dm, s, b, s.stream );
+    const unsigned long nfail = readNFail( s, s.stream );
+    checkCuda( cudaMemcpy( out_ekin, s.d_a, n_out * sizeof(double), cudaMemcpyDeviceToHost ), "D2H" );
+    checkCuda( cudaMemcpy( out_dir, s.d_c, 3 * n_out * sizeof(double), cudaMemcpyDeviceToHost ), "D2H" );
+    return nfail;
+  }
+}
+
+extern "C" {
+
+void ncrystal_samplescatter( ncrystal_scatter_t sc, double ekin, const double (*direction)[3],
+                             double* ekin_final, double (*direction_final)[3] )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncrystal_samplescatter" );
+    double out[3];
+    const unsigned long nfail = runScatterDir( o, &ekin, *direction, 1, 1, ekin_final, out );
+    if ( nfail )
+      throwSamplingFailure( nfail );
+    (*direction_final)[0] = out[0];
+    (*direction_final)[1] = out[1];
+    (*direction_final)[2] = out[2];
+    return;
+  } NCGB_CATCH;
+  *ekin_final = -1.0;
+  (*direction_final)[0] = (*direction_final)[1] = (*direction_final)[2] = 0.0;
+}
+
+void ncrystal_samplescatter_many( ncrystal_scatter_t sc, double ekin, const double (*direction)[3],
+                                  unsigned long repeat, double* results_ekin, double* results_dirx,
+                                  double* results_diry, double* results_dirz )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncrystal_samplescatter_many" );
+    std::vector<double> dirs( 3 * repeat );
+    const unsigned long nfail = runScatterDir( o, &ekin, *direction, 1, repeat, results_ekin, dirs.data() );
+    if ( nfail )
+      throwSamplingFailure( nfail );
+    for ( unsigned long k = 0; k < repeat; ++k ) {
+      results_dirx[k] = dirs[3*k];
+      results_diry[k] = dirs[3*k+1];
+      results_dirz[k] = dirs[3*k+2];
+    }
+    return;
+  } NCGB_CATCH;
+  for ( unsigned long k = 0; k < repeat; ++k ) {
+    results_ekin[k] = -1.0;
+    results_dirx[k] = results_diry[k] = results_dirz[k] = 0.0;
+  }
+}
+
+int ncgb_scatter_dir_device( ncrystal_scatter_t sc, const double* d_ekin, const double* d_dir, unsigned long n,
+                             double* d_ekin_final, double* d_dir_final, int32_t* d_status, void* stream )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_scatter_dir_device" );
+    checkSize( n, 1 );
+    if ( n == 0 )
+      return 0;
+    if ( !d_ekin || !d_dir || !d_dir_final )
+      throw TypedError( "BadInput", "ncgb_scatter_dir_device: null array" );
+    DeviceMaterial& dm = *o.mat;
+    Scratch& s = scratchFor( dm );
+    cudaStream_t st = static_cast<cudaStream_t>( stream );
+    ncgb::Batch b = makeBatch( o, s, nextCall( o ) );
+    b.ekin = d_ekin;
+    b.n_ekin = b.n_out = n;
+    b.out_a = d_ekin_final;
+    b.status = d_status;
+    b.dir_in = d_dir;
+    b.dir_out = d_dir_final;
+    runBatch( dm, s, b, st );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+}
+
 // ---- scalar evaluation (a batch of one) -----------------------------------------------
 
 void ncrystal_crosssection_nonoriented( ncrystal_process_t p, double ekin, double* result )

@@ -153,6 +153,45 @@ namespace ncgb_dev {
     s = t;
   }
 
+  // randDirectionGivenScatterMu, NCRandUtils.cc:51-96 (via
+  // randNeutronDirectionGivenScatterMu, NCRandUtils.hh:152-155): the outgoing
+  // direction at cosine mu to 'in' with a uniform azimuth, from a random unit
+  // vector (Marsaglia) crossed with the normalised 'in'.  Every operation is
+  // rounded separately, as the reference's C++ evaluates it, so that the
+  // result is the reference's to the bit.  Returns NCGB_ST_OK, or LOOPCAP if
+  // 100000 trial vectors were all nearly parallel to 'in'.
+  __device__ __forceinline__ int randDirGivenMu( ncgb_rng& rng, double mu, const double* in, double* out )
+  {
+    const double m2 = __dadd_rn( __dadd_rn( __dmul_rn( in[0], in[0] ), __dmul_rn( in[1], in[1] ) ),
+                                 __dmul_rn( in[2], in[2] ) );
+    const double invm = ( fabs( __dsub_rn( m2, 1.0 ) ) < 1e-14 ) ? 1.0 : __ddiv_rn( 1.0, sqrt( m2 ) );
+    const double u0 = __dmul_rn( in[0], invm ), u1 = __dmul_rn( in[1], invm ), u2 = __dmul_rn( in[2], invm );
+    double t0 = 0.0, t1 = 0.0, t2 = 0.0, tm2 = 0.0;
+    int it = 0;
+    for ( ; it < 100000; ++it ) {
+      const double x0 = __dsub_rn( 2.0 * rand01( rng ), 1.0 );
+      const double x1 = __dsub_rn( 2.0 * rand01( rng ), 1.0 );
+      const double s = __dadd_rn( __dmul_rn( x0, x0 ), __dmul_rn( x1, x1 ) );
+      if ( s < 1.0 ) {
+        const double t = 2.0 * sqrt( __dsub_rn( 1.0, s ) );
+        const double a0 = __dmul_rn( x0, t ), a1 = __dmul_rn( x1, t ), a2 = __dsub_rn( 1.0, 2.0 * s );
+        t0 = __dsub_rn( __dmul_rn( a1, u2 ), __dmul_rn( a2, u1 ) );
+        t1 = __dsub_rn( __dmul_rn( a2, u0 ), __dmul_rn( a0, u2 ) );
+        t2 = __dsub_rn( __dmul_rn( a0, u1 ), __dmul_rn( a1, u0 ) );
+        tm2 = __dadd_rn( __dadd_rn( __dmul_rn( t0, t0 ), __dmul_rn( t1, t1 ) ), __dmul_rn( t2, t2 ) );
+        if ( !( tm2 < 0.001 ) )
+          break;
+      }
+    }
+    if ( it == 100000 )
+      return NCGB_ST_LOOPCAP;
+    const double f = sqrt( __ddiv_rn( __dsub_rn( 1.0, __dmul_rn( mu, mu ) ), tm2 ) );
+    out[0] = __dadd_rn( __dmul_rn( u0, mu ), __dmul_rn( t0, f ) );
+    out[1] = __dadd_rn( __dmul_rn( u1, mu ), __dmul_rn( t1, f ) );
+    out[2] = __dadd_rn( __dmul_rn( u2, mu ), __dmul_rn( t2, f ) );
+    return NCGB_ST_OK;
+  }
+
   // convertAlphaBetaToDeltaEMu, NCKinUtils.cc:25-58.  Returns
   // NCGB_ST_CALCERROR where the reference throws (E*E' == 0).
   __device__ __forceinline__ int alphaBetaToDeltaEMu( double alpha, double beta, double ekin, double kT,

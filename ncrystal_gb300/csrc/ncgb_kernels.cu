@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "ncgb_device.cuh"
@@ -82,9 +83,38 @@ namespace {
   }
 
   // Write one neutron's scatter result (mode 0: E', mu; mode 1: acos(mu), E'-E).
-  __device__ __forceinline__ void writeScatter( const ncgb::Batch& b, uint64_t o, double e, int st,
-                                                double ef, double mu )
+  // With directions (dir_out): the outgoing direction, sampled from the
+  // neutron's stream after its scatter (ScatterIsotropicMat::sampleScatter,
+  // NCProcImpl.cc:29-37); 'scattered' is false outside the material's domain,
+  // where the direction is returned unchanged (NCProcImpl.cc:364-377).
+  // (out of line: only calls with directions pay for it in registers)
+  __device__ __noinline__ int writeDir( const ncgb::Batch& b, uint64_t o, int st, double mu, ncgb_rng& rng,
+                                        bool scattered )
   {
+    const uint64_t i = ( b.n_out == b.n_ekin ) ? o : o % b.n_ekin;
+    const double* in = b.dir_in + 3 * i;
+    double* out = b.dir_out + 3 * o;
+    if ( st == NCGB_ST_OK && scattered )
+      st = randDirGivenMu( rng, mu, in, out );
+    else if ( st == NCGB_ST_OK ) {
+      out[0] = in[0]; out[1] = in[1]; out[2] = in[2];
+    }
+    if ( st != NCGB_ST_OK ) {
+      out[0] = 0.0; out[1] = 0.0; out[2] = 0.0;
+    }
+    return st;
+  }
+
+  template<bool Dir>
+  __device__ __forceinline__ void writeScatter( const ncgb::Batch& b, uint64_t o, double e, int st,
+                                                double ef, double mu, ncgb_rng& rng, bool scattered = true )
+  {
+    if ( Dir && b.dir_out ) {
+      // a copy: the neutron's stream is not used after its result is written,
+      // and the caller's state can stay in registers
+      ncgb_rng r2 = rng;
+      st = writeDir( b, o, st, mu, r2, scattered );
+    }
     if ( b.status ) b.status[o] = st;
     if ( st != NCGB_ST_OK ) {
       atomicAdd( &b.work->nfail, 1ull );
@@ -103,7 +133,7 @@ namespace {
   }
 
   // ---- phase 1: cross-section, pick, short samplers, SAB queue ----------------
-  template<class Src, bool Fast>
+  template<class Src, bool Fast, bool Dir>
   __global__ void __launch_bounds__(512)
   k_pick( const __grid_constant__ Src src, const ncgb::Batch b )
   {
@@ -120,7 +150,7 @@ namespace {
       if ( !contains( m.dom_elow, m.dom_ehigh, e ) ) {
         // ProcComposition outside its domain: xs 0, neutron unchanged (NCProcImpl.cc:353-389)
         store( b.out_xs, b.out_f32, o, 0.0 );
-        writeScatter( b, o, e, NCGB_ST_OK, e, 1.0 );
+        writeScatter<Dir>( b, o, e, NCGB_ST_OK, e, 1.0, rng, false );
       } else {
         const XSPick p = xsAndPick<true, Fast>( m, e, rng );
         store( b.out_xs, b.out_f32, o, p.xs );
@@ -149,7 +179,7 @@ namespace {
             break;
         }
         if ( !queue )
-          writeScatter( b, o, e, st, ef, mu );
+          writeScatter<Dir>( b, o, e, st, ef, mu, rng );
       }
       // warp-aggregated append to the SAB queue
       const unsigned active = __activemask();
@@ -176,7 +206,7 @@ namespace {
   }
 
   // ---- phase 2: persistent S(alpha,beta) sampling ---------------------------
-  template<class Src, bool Fast, bool Learned>
+  template<class Src, bool Fast, bool Learned, bool Dir>
   __global__ void __launch_bounds__(256, 4)
   k_sab( const __grid_constant__ Src src, const ncgb::Batch b )
   {
@@ -212,11 +242,11 @@ namespace {
               // FreeGas component: sampled to completion here
               double ef = q.ekin, mu = 1.0;
               const int st = freeGasScatter( c.fg, m.fg_erfc_table, rng, q.ekin, ef, mu );
-              writeScatter( b, q.idx, q.ekin, st, ef, mu );
+              writeScatter<Dir>( b, q.idx, q.ekin, st, ef, mu, rng );
             } else {
               const int st = sabBegin( c.sab, m.fg_erfc_table, q.ekin, rng, L );
               if ( st != NCGB_ST_OK )
-                writeScatter( b, q.idx, q.ekin, st, q.ekin, 1.0 );
+                writeScatter<Dir>( b, q.idx, q.ekin, st, q.ekin, 1.0, rng );
               else
                 has = true;
             }
@@ -231,7 +261,7 @@ namespace {
         double ef = 0.0, mu = 0.0;
         const int st = sabStep<Fast, Learned>( src.mat( q.mat ).comp[q.comp].sab, L, rng, ef, mu );
         if ( st >= 0 ) {
-          writeScatter( b, q.idx, q.ekin, st, ef, mu );
+          writeScatter<Dir>( b, q.idx, q.ekin, st, ef, mu, rng );
           has = false;
         }
       }
@@ -306,7 +336,7 @@ namespace {
   {
     static int bps = 0;
     if ( !bps ) {
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_sab<Src, false, false>, 256, 0 );
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_sab<Src, false, false, false>, 256, 0 );
       if ( bps <= 0 ) bps = 1;
     }
     return bps;
@@ -328,6 +358,31 @@ namespace {
   std::vector<PhaseEvents> g_events;
   std::mutex g_evmtx;
 
+  template<class Src, bool Dir>
+  void launchPick( const Src& src, const ncgb::Batch& b, int pb, cudaStream_t s )
+  {
+    if ( b.fast )
+      k_pick<Src, true, Dir><<<gridFor( b.n_out, pb ), pb, 0, s>>>( src, b );
+    else
+      k_pick<Src, false, Dir><<<gridFor( b.n_out, pb ), pb, 0, s>>>( src, b );
+  }
+
+  template<class Src, bool Dir>
+  void launchSab( const Src& src, const ncgb::Batch& b, int grid, cudaStream_t s )
+  {
+    if ( b.fast ) {
+      if ( b.learned )
+        k_sab<Src, true, true, Dir><<<grid, 256, 0, s>>>( src, b );
+      else
+        k_sab<Src, true, false, Dir><<<grid, 256, 0, s>>>( src, b );
+    } else {
+      if ( b.learned )
+        k_sab<Src, false, true, Dir><<<grid, 256, 0, s>>>( src, b );
+      else
+        k_sab<Src, false, false, Dir><<<grid, 256, 0, s>>>( src, b );
+    }
+  }
+
   template<class Src>
   cudaError_t launchBoth( const Src& src, const ncgb::Batch& b, const ncgb::LaunchCfg& cfg, cudaStream_t s )
   {
@@ -345,10 +400,14 @@ namespace {
       cudaEventRecord( ev.a, s );
     }
     const int pb = ( cfg.pick_block == 128 || cfg.pick_block == 512 ) ? cfg.pick_block : 256;
-    if ( b.fast )
-      k_pick<Src, true><<<gridFor( b.n_out, pb ), pb, 0, s>>>( src, b );
-    else
-      k_pick<Src, false><<<gridFor( b.n_out, pb ), pb, 0, s>>>( src, b );
+    if ( b.dir_out ) {
+      if constexpr ( std::is_same<Src, SingleSrc>::value )
+        launchPick<Src, true>( src, b, pb, s );
+      else
+        return cudaErrorInvalidValue;   // directions: single-material calls only
+    } else {
+      launchPick<Src, false>( src, b, pb, s );
+    }
     e = cudaGetLastError();
     if ( e != cudaSuccess )
       return e;
@@ -357,16 +416,11 @@ namespace {
     const int maxb = sabBlocksPerSM<Src>();
     const int mult = ( cfg.sab_blocks_per_sm > 0 && cfg.sab_blocks_per_sm < maxb ) ? cfg.sab_blocks_per_sm : maxb;
     const int grid = numSMs() * mult;
-    if ( b.fast ) {
-      if ( b.learned )
-        k_sab<Src, true, true><<<grid, 256, 0, s>>>( src, b );
-      else
-        k_sab<Src, true, false><<<grid, 256, 0, s>>>( src, b );
+    if ( b.dir_out ) {
+      if constexpr ( std::is_same<Src, SingleSrc>::value )
+        launchSab<Src, true>( src, b, grid, s );
     } else {
-      if ( b.learned )
-        k_sab<Src, false, true><<<grid, 256, 0, s>>>( src, b );
-      else
-        k_sab<Src, false, false><<<grid, 256, 0, s>>>( src, b );
+      launchSab<Src, false>( src, b, grid, s );
     }
     e = cudaGetLastError();
     if ( timing ) {

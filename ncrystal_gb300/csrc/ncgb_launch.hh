@@ -57,6 +57,8 @@ namespace ncgb {
     void* out_xs;      // may be null
     void* out_a;       // may be null
     void* out_b;       // may be null
+    const double* dir_in;  // [n_ekin][3] incoming directions (sampleScatter with directions), or null
+    double* dir_out;       // [n_out][3] outgoing directions, or null
     int32_t* status;   // may be null
     Work* work;        // scratch, sizeof(Work)
     QEntry* queue;     // scratch, n_out entries

@@ -1164,3 +1164,73 @@ int64_t ncgb_oracle_scatter_many( const ncgb_material_view* m, const double* eki
   }
   return nbad;
 }
+
+/* randDirectionGivenScatterMu, NCRandUtils.cc:51-96: the outgoing direction
+ * at cosine mu to 'in' (normalised unless within 1e-14 of unit length) with a
+ * uniform azimuth, from Marsaglia trial vectors crossed with it.  Returns
+ * ORA_OK, or ORA_LOOPCAP after 100000 nearly parallel trial vectors (the
+ * reference's loop is unbounded). */
+static int ora_rand_dir_given_mu( ncgb_rng* rng, double mu, const double* in, double* out )
+{
+  const double m2 = in[0]*in[0] + in[1]*in[1] + in[2]*in[2];
+  const double invm = ( fabs( m2 - 1.0 ) < 1e-14 ? 1.0 : 1.0 / sqrt( m2 ) );
+  const double u0 = in[0]*invm, u1 = in[1]*invm, u2 = in[2]*invm;
+  double t0 = 0.0, t1 = 0.0, t2 = 0.0, tm2 = 0.0;
+  int it = 0;
+  for ( ; it < 100000; ++it ) {
+    const double x0 = 2.0*ncgb_rng_generate( rng ) - 1.0;
+    const double x1 = 2.0*ncgb_rng_generate( rng ) - 1.0;
+    const double s = x0*x0 + x1*x1;
+    if ( s < 1.0 ) {
+      const double t = 2.0*sqrt( 1.0 - s );
+      const double a0 = x0*t, a1 = x1*t, a2 = 1.0 - 2.0*s;
+      t0 = a1*u2 - a2*u1;
+      t1 = a2*u0 - a0*u2;
+      t2 = a0*u1 - a1*u0;
+      tm2 = t0*t0 + t1*t1 + t2*t2;
+      if ( !( tm2 < 0.001 ) )
+        break;
+    }
+  }
+  if ( it == 100000 )
+    return ORA_LOOPCAP;
+  const double f = sqrt( ( 1.0 - mu*mu ) / tm2 );
+  out[0] = u0*mu + t0*f;
+  out[1] = u1*mu + t1*f;
+  out[2] = u2*mu + t2*f;
+  return ORA_OK;
+}
+
+/* ProcComposition::sampleScatter (NCProcImpl.cc:364-377) for non-oriented
+ * materials: ScatterIsotropicMat::sampleScatter (NCProcImpl.cc:29-37) of the
+ * picked component.  Neutron i: in dir[3i..3i+2], out dirout[3i..3i+2]. */
+int64_t ncgb_oracle_scatter_dir_many( const ncgb_material_view* m, const double* ekin, const double* dir, int64_t n,
+                                      uint64_t seed, uint32_t index_offset, uint32_t callseq, uint32_t stream,
+                                      double* out_ef, double* out_dir, int32_t* out_status )
+{
+  int64_t nbad = 0;
+  for ( int64_t i = 0; i < n; ++i ) {
+    ncgb_rng rng;
+    ncgb_rng_init( &rng, seed, (uint32_t)( i + index_offset ), callseq, stream );
+    double mu = 1.0;
+    const double* in = dir + 3 * i;
+    double* out = out_dir + 3 * i;
+    int st;
+    if ( !ora_contains( m->dom_elow, m->dom_ehigh, ekin[i] ) ) {
+      out_ef[i] = ekin[i];
+      out[0] = in[0]; out[1] = in[1]; out[2] = in[2];
+      st = ORA_OK;
+    } else {
+      st = ncgb_oracle_scatter( m, &rng, ekin[i], &out_ef[i], &mu );
+      if ( st == ORA_OK )
+        st = ora_rand_dir_given_mu( &rng, mu, in, out );
+      if ( st != ORA_OK ) {
+        out_ef[i] = -1.0;
+        out[0] = out[1] = out[2] = 0.0;
+      }
+    }
+    if ( out_status ) out_status[i] = st;
+    if ( st ) ++nbad;
+  }
+  return nbad;
+}

@@ -34,6 +34,10 @@ def oracle_lib():
         L.ncgb_oracle_xs.argtypes = [C.c_void_p, C.c_double]
         L.ncgb_oracle_xs_many.restype = None
         L.ncgb_oracle_xs_many.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+        L.ncgb_oracle_scatter_dir_many.restype = C.c_int64
+        L.ncgb_oracle_scatter_dir_many.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64,
+                                                   C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                                                   C.c_void_p]
         L.ncgb_oracle_scatter_many.restype = C.c_int64
         L.ncgb_oracle_scatter_many.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64, C.c_uint32,
                                                C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -145,6 +149,24 @@ class HostMaterial:
         return ef, mu, st, nd
 
 
+def _scatter_dir(self, ekin, direction, seed, index_offset=0, callseq=0, stream=0):
+    """Scatters with directions (ProcComposition::sampleScatter): per neutron
+    i, stream (seed, i+index_offset, callseq, stream).  Returns (ekin_final,
+    direction_final[n, 3], status)."""
+    e = np.ascontiguousarray(ekin, dtype=np.float64)
+    d = np.ascontiguousarray(direction, dtype=np.float64).reshape(len(e), 3)
+    n = len(e)
+    ef = np.empty(n)
+    do = np.empty((n, 3))
+    st = np.empty(n, dtype=np.int32)
+    oracle_lib().ncgb_oracle_scatter_dir_many(self.view, _P(e), _P(d), n, seed, index_offset, callseq, stream,
+                                              _P(ef), _P(do), _P(st))
+    return ef, do, st
+
+
+HostMaterial.scatter_dir = _scatter_dir
+
+
 def refpin_lib():
     """The harness around the reference library (only where it was built)."""
     global _refpin
@@ -153,6 +175,9 @@ def refpin_lib():
         if not os.path.exists(path):
             return None
         L = C.CDLL(path)
+        L.refpin_run_dir.restype = C.c_int
+        L.refpin_run_dir.argtypes = [C.c_char_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                                     C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.refpin_run.restype = C.c_int
         L.refpin_run.argtypes = [C.c_char_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_int64,
                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -172,6 +197,24 @@ def reference_run(cfg, ekin, seed, callseq=0, stream=0):
                ndraws=np.empty(n, dtype=np.int32), status=np.empty(n, dtype=np.int32))
     rc = L.refpin_run(cfg.encode(), seed, callseq, stream, _P(e), n, _P(out["xs"]), _P(out["ekin_final"]),
                       _P(out["mu"]), _P(out["ndraws"]), _P(out["status"]))
+    if rc:
+        raise RuntimeError("reference could not create %r" % cfg)
+    return out
+
+
+def reference_run_dir(cfg, ekin, direction, seed, callseq=0, stream=0):
+    """The reference's ncrystal_samplescatter on the same per-neutron streams.
+    Returns dict(ekin_final, direction[n, 3], ndraws, status)."""
+    L = refpin_lib()
+    if L is None:
+        raise RuntimeError("reference harness not built")
+    e = np.ascontiguousarray(ekin, dtype=np.float64)
+    n = len(e)
+    d = np.ascontiguousarray(direction, dtype=np.float64).reshape(n, 3)
+    out = dict(ekin_final=np.empty(n), direction=np.empty((n, 3)), ndraws=np.empty(n, dtype=np.int32),
+               status=np.empty(n, dtype=np.int32))
+    rc = L.refpin_run_dir(cfg.encode(), seed, callseq, stream, _P(e), _P(d), n, _P(out["ekin_final"]),
+                          _P(out["direction"]), _P(out["ndraws"]), _P(out["status"]))
     if rc:
         raise RuntimeError("reference could not create %r" % cfg)
     return out

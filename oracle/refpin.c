@@ -68,3 +68,42 @@ int refpin_run( const char* cfg, uint64_t seed, uint32_t callseq, uint32_t strea
   ncrystal_setrandgen( NULL );
   return 0;
 }
+
+/* The same for ncrystal_samplescatter (ncrystal.cc:1159-1174): energy and
+ * direction dir[3i..3i+2] in, E' and the outgoing direction out. */
+int refpin_run_dir( const char* cfg, uint64_t seed, uint32_t callseq, uint32_t stream,
+                    const double* ekin, const double* dir, int64_t n,
+                    double* out_ef, double* out_dir, int32_t* out_ndraws, int32_t* out_status )
+{
+  ncrystal_sethaltonerror( 0 );
+  ncrystal_setmsghandler( NULL );
+  ncrystal_setrandgen( refpin_rand );
+  ncrystal_scatter_t sc = ncrystal_create_scatter( cfg );
+  if ( ncrystal_error() ) {
+    fprintf( stderr, "refpin: could not create %s: %s\n", cfg, ncrystal_lasterror() );
+    ncrystal_clearerror();
+    return 1;
+  }
+  ncrystal_process_t pr = ncrystal_cast_scat2proc( sc );
+  for ( int64_t i = 0; i < n; ++i ) {
+    double flush;
+    ncrystal_crosssection_nonoriented( pr, 12345.0, &flush );
+    ncgb_rng_init( &g_rng, seed, (uint32_t)i, callseq, stream );
+    g_ndraws = 0;
+    double indir[3] = { dir[3*i], dir[3*i+1], dir[3*i+2] };
+    double outdir[3];
+    ncrystal_samplescatter( sc, ekin[i], (const double (*)[3])&indir, &out_ef[i], &outdir );
+    out_dir[3*i] = outdir[0];
+    out_dir[3*i+1] = outdir[1];
+    out_dir[3*i+2] = outdir[2];
+    out_status[i] = 0;
+    if ( ncrystal_error() ) {
+      out_status[i] = 1;
+      ncrystal_clearerror();
+    }
+    out_ndraws[i] = (int32_t)g_ndraws;
+  }
+  ncrystal_unref( &sc );
+  ncrystal_setrandgen( NULL );
+  return 0;
+}

@@ -8,8 +8,11 @@ source replaced by the per-neutron Philox streams of include/ncgb_philox.h
 mu, the number of random numbers the reference consumed and whether it raised
 an error.  Neutron i uses stream (SEED, i, 0, 0).
 
+dir_*.npz: the same for the reference's ncrystal_samplescatter (scatters with
+incoming and outgoing directions).
+
 Run from the repository root where the NCrystal sources exist:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--dirs-only]
 """
 import os
 import sys
@@ -43,6 +46,25 @@ GOLDEN = {
 }
 
 
+# Scatters with directions (ncrystal_samplescatter): energies and directions
+# per material; directions random, every other one not normalised.
+DIR_GOLDEN = {
+    "dir_al": (W.AL, 201),
+    "dir_pe293": (W.PE293, 202),
+    "dir_water": (W.WATER, 203),
+    "dir_cu77": ("Cu_sg225.ncmat;temp=77K", 204),
+}
+N_DIR = 1000
+
+
+def dir_inputs(seed):
+    rng = np.random.default_rng(seed)
+    e = np.concatenate([W.loguniform_energies(N_DIR, 1e-5, 20.0, seed), [-1.0, 1e-300, 0.0253]])
+    d = rng.normal(size=(len(e), 3))
+    d[::2] /= np.linalg.norm(d[::2], axis=1)[:, None]
+    return e, d
+
+
 def edge_energies(bundle):
     """Energies on and next to table edges: Bragg thresholds and plane edges,
     SAB energy-grid points, Emax, and a few extremes."""
@@ -67,7 +89,7 @@ def main():
     B.build_library()
     cfgs = [c for c, _ in GOLDEN.values()]
     paths = B.export_bundles(cfgs)
-    for key, (cfg, gen) in GOLDEN.items():
+    for key, (cfg, gen) in ([] if "--dirs-only" in sys.argv else GOLDEN.items()):
         b = read_bundle(paths[cfg])
         ekin = np.concatenate([gen(N_RANDOM), edge_energies(b)])
         r = pyoracle.reference_run(cfg, ekin, SEED)
@@ -76,6 +98,15 @@ def main():
                             xs=r["xs"], ekin_final=r["ekin_final"], mu=r["mu"], ndraws=r["ndraws"],
                             status=r["status"])
         print("%-8s %-55s n=%d errors=%d -> %s" % (key, cfg, len(ekin), int(r["status"].sum()), out))
+    B.export_bundles([c for c, _ in DIR_GOLDEN.values()])
+    for key, (cfg, seed) in DIR_GOLDEN.items():
+        e, d = dir_inputs(seed)
+        r = pyoracle.reference_run_dir(cfg, e, d, SEED)
+        out = os.path.join(HERE, key + ".npz")
+        np.savez_compressed(out, cfg=np.array(cfg), seed=np.array(SEED, dtype=np.uint64), ekin=e, direction=d,
+                            ekin_final=r["ekin_final"], direction_final=r["direction"], ndraws=r["ndraws"],
+                            status=r["status"])
+        print("%-10s %-45s n=%d errors=%d -> %s" % (key, cfg, len(e), int(r["status"].sum()), out))
 
 
 if __name__ == "__main__":

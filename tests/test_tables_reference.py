@@ -62,3 +62,20 @@ def test_oracle_equals_live_reference(cfg):
     np.testing.assert_array_equal(nd, r["ndraws"])
     np.testing.assert_array_equal(ef, r["ekin_final"])
     np.testing.assert_array_equal(mu, r["mu"])
+
+
+@pytest.mark.parametrize("cfg", [W.AL, W.PE293, W.WATER])
+def test_oracle_directions_equal_live_reference(cfg):
+    """ncrystal_samplescatter of the reference, driven with the same streams,
+    against the oracle: identical E' and outgoing directions."""
+    m = pyoracle.HostMaterial(B.export_bundles([cfg])[cfg])
+    r = np.random.default_rng(17)
+    e = np.concatenate([W.loguniform_energies(5000, 1e-5, 20.0, 18), [-1.0, 0.0, 1e-300]])
+    d = r.normal(size=(len(e), 3))
+    ef, do, st = m.scatter_dir(e, d, 4321)
+    ref = pyoracle.reference_run_dir(cfg, e, d, 4321)
+    # the reference raises CalcError exactly where the oracle fails (E = 0 for
+    # S(alpha,beta) materials: beta = -E/kT)
+    np.testing.assert_array_equal(st != 0, ref["status"] != 0)
+    np.testing.assert_array_equal(ef, ref["ekin_final"])
+    np.testing.assert_array_equal(do, ref["direction"])
