@@ -204,6 +204,9 @@ typedef struct {
   /* erfc at the 1101 bin edges of [-2,9] plus +-infinity, for the free-gas
    * sampler's cheap bounds (NCFreeGasUtils.cc:95-147); 1103 values */
   const double* fg_erfc_table;
+  /* absorption (AbsOOV, NCAbsOOV.cc:33-44): xs = abs_c / sqrt(E); abs_c < 0:
+   * not in the bundle */
+  double abs_c;
 } ncgb_material_view;
 
 #ifdef __cplusplus

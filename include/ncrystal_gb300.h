@@ -99,6 +99,16 @@ void ncrystal_genscatter_nonoriented_many( ncrystal_scatter_t,
                                            double* results_angle,
                                            double* results_dekin );
 
+/* Absorption (ncrystal.h:669-700, ncrystal.cc:411-445, :1518-1571): the
+ * standard factory's 1/v model AbsOOV (NCStdAbsFact.cc:49-52), xs =
+ * c/sqrt(E) (NCAbsOOV.cc:33-44), evaluated on the GPU by
+ * ncrystal_crosssection_nonoriented(_many) on the cast process. */
+typedef struct { void * internal; } ncrystal_absorption_t;
+ncrystal_absorption_t ncrystal_create_absorption( const char * cfgstr );
+ncrystal_absorption_t ncrystal_clone_absorption( ncrystal_absorption_t );
+ncrystal_process_t ncrystal_cast_abs2proc( ncrystal_absorption_t );
+ncrystal_absorption_t ncrystal_cast_proc2abs( ncrystal_process_t );
+
 /* Scatter with directions (ncrystal.h:782-786, ncrystal.cc:1159-1174 and
  * :1248-1282): for non-oriented materials, an isotropic scatter followed by an
  * outgoing direction at cosine mu to the incoming one with a uniform azimuth
@@ -145,6 +155,13 @@ const char * ncrystal_version_str( void );
 int ncgb_scatter_device( ncrystal_scatter_t, const double* d_ekin, unsigned long n,
                          double* d_xs, double* d_ekin_final, double* d_mu,
                          int32_t* d_status, void* stream );
+
+/* The scatter batch with the material's absorption cross-section beside the
+ * scattering one, in the same pass over the energies (an MC step needs both):
+ * d_xs_abs[n] = c/sqrt(E) of the AbsOOV model; any output may be NULL. */
+int ncgb_xs_abs_scatter_device( ncrystal_scatter_t, const double* d_ekin, unsigned long n, double* d_xs,
+                                double* d_xs_abs, double* d_ekin_final, double* d_mu, int32_t* d_status,
+                                void* stream );
 
 /* Scatters with directions on device memory: d_ekin[n], d_dir[n][3] ->
  * d_ekin_final[n], d_dir_final[n][3] (d_status optional); neutron i uses

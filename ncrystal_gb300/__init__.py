@@ -7,7 +7,7 @@ GB300 GPU (sm_103a), behind NCrystal's own C and Python interfaces.
     ekin_final, mu = sc.sampleScatterIsotropic(ekin_array)
 """
 from .core import (NCBadInput, NCCalcError, NCException, NCFileNotFound,  # noqa: F401
-                   MLP, Batch, NCLogicError, Process, Scatter, createProcess, createScatter, lib, phase_times,
-                   phase_timing)
+                   MLP, Absorption, Batch, NCLogicError, Process, Scatter, createAbsorption, createProcess,
+                   createScatter, lib, phase_times, phase_timing)
 
 __version__ = "0.1.0"

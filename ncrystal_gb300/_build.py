@@ -174,7 +174,8 @@ def export_bundles(cfgs, outdir=None, with_derived=False, force=False):
     for cfg in cfgs:
         path = os.path.join(outdir, bundle_file_name(cfg))
         res[cfg] = path
-        if force or not os.path.exists(path):
+        # re-export when the exporter is newer than the bundle (new records)
+        if force or not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(exp):
             cmd = [exp] + (["--with-derived"] if with_derived else []) + [path, cfg]
             todo.append(cmd)
     env = dict(os.environ)

@@ -68,6 +68,7 @@
 #include "NCrystal/internal/sab/NCSABExtender.hh"
 #include "NCrystal/internal/freegas/NCFreeGas.hh"
 #include "NCrystal/internal/phys_utils/NCFreeGasUtils.hh"
+#include "NCrystal/internal/absoov/NCAbsOOV.hh"
 #undef private
 #undef protected
 
@@ -286,6 +287,18 @@ int main( int argc, char** argv )
       exportComponent(b, nc++, 1.0, top, withDerived);
     }
     b.i64("ncomp", nc);
+    // absorption: the standard factory's AbsOOV (NCStdAbsFact.cc:49-52), xs =
+    // c/sqrt(E) (NCAbsOOV.cc:33-44); c = 0 means no absorption
+    {
+      auto ab = NC::createAbsorption(cfg);
+      const NC::ProcImpl::Process& ap = ab.underlying();
+      if ( auto oov = dynamic_cast<const NC::AbsOOV*>(&ap) )
+        b.f64("abs_c", oov->m_c);
+      else if ( ap.isNull() )
+        b.f64("abs_c", 0.0);
+      else
+        throw std::runtime_error("unsupported absorption process type");
+    }
     b.write(out);
   } catch ( std::exception& e ) {
     std::fprintf(stderr,"ncgb_export error: %s\n",e.what());

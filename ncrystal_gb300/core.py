@@ -66,6 +66,13 @@ def lib():
         "ncrystal_clone_scatter_rngbyidx": (H, [H, _C.c_ulong]),
         "ncrystal_clone_scatter_rngforcurrentthread": (H, [H]),
         "ncrystal_cast_scat2proc": (H, [H]),
+        "ncrystal_create_absorption": (H, [_C.c_char_p]),
+        "ncrystal_clone_absorption": (H, [H]),
+        "ncrystal_cast_abs2proc": (H, [H]),
+        "ncrystal_cast_proc2abs": (H, [H]),
+        "ncrystal_cast_proc2scat": (H, [H]),
+        "ncgb_xs_abs_scatter_device": (_C.c_int, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p, _C.c_void_p,
+                                                  _C.c_void_p, _C.c_void_p, _C.c_void_p]),
         "ncrystal_unref": (None, [_C.c_void_p]),
         "ncrystal_refcount": (_C.c_int, [_C.c_void_p]),
         "ncrystal_valid": (_C.c_int, [_C.c_void_p]),
@@ -392,6 +399,18 @@ class Scatter(Process):
         _check()
         return ef, (ux, uy, uz)
 
+    def xs_abs_scatter_device(self, ekin, xs=None, xs_abs=None, ekin_final=None, mu=None, status=None,
+                              stream=None):
+        """One pass over float64 CUDA tensors: scattering cross-section,
+        absorption cross-section (1/v) and one isotropic scatter per neutron."""
+        import torch
+        if stream is None:
+            stream = torch.cuda.current_stream(ekin.device)
+        p = (lambda t: 0 if t is None else t.data_ptr())
+        if lib().ncgb_xs_abs_scatter_device(self._h, ekin.data_ptr(), ekin.numel(), p(xs), p(xs_abs),
+                                            p(ekin_final), p(mu), p(status), stream.cuda_stream):
+            _check()
+
     def scatter_dir_device(self, ekin, direction, ekin_final, direction_final, status=None, stream=None):
         """Scatters with directions on CUDA tensors: ekin (n,) and direction
         (n, 3) float64 in, ekin_final (n,) and direction_final (n, 3) out."""
@@ -482,6 +501,25 @@ class Scatter(Process):
                                                    mu.ctypes.data)
         _check()
         return ef, mu
+
+
+class Absorption(Process):
+    """A material's absorption process (NCrystal core.py's Absorption): the
+    1/v model, cross-sections evaluated on the GPU."""
+
+    def clone(self):
+        h = lib().ncrystal_clone_absorption(self._h)
+        _check()
+        return Absorption(h, self._cfg)
+
+
+def createAbsorption(cfgstr):
+    """NCrystal.createAbsorption on the GPU path."""
+    h = lib().ncrystal_create_absorption(cfgstr.encode())
+    _check()
+    if not h.internal:
+        raise NCException("could not create absorption for %r" % cfgstr)
+    return Absorption(h, cfgstr)
 
 
 class Batch:

@@ -23,6 +23,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -213,7 +214,8 @@ namespace {
   }
 
   // ---- handles (ncrystal.cc:104-200) ------------------------------------------
-  constexpr uint32_t kScatterTypeID = 0x7d6b0637; // same tag value as NCrystal's Scatter
+  constexpr uint32_t kScatterTypeID = 0x7d6b0637; // same tag values as NCrystal's Scatter
+  constexpr uint32_t kAbsTypeID = 0xede2eb9d;     // and Absorption (ncrystal.cc:207-231)
   constexpr uint64_t kDefaultSeed = 0x4e43727973746c21ull;
 
   // Mode of new handles and batches: the environment variable NCGB_MODE
@@ -257,6 +259,7 @@ namespace {
     uint32_t streamidx = 0;
     int mode = defaultMode();
     int sampler = NCGB_SAMPLER_PLAIN;
+    bool absorption = false;   // an absorption handle (AbsOOV of the material)
     std::atomic<uint32_t> callseq{0};
     ScatterObj() { fp.typeid_ = kScatterTypeID; fp.obj = this; }
   };
@@ -274,6 +277,25 @@ namespace {
   }
 
   ncrystal_scatter_t makeHandle( ScatterObj* o ) { return ncrystal_scatter_t{ &o->fp }; }
+
+  // Any process handle: a scatter or an absorption.
+  ScatterObj& extractProc( void* internal, const char* fct )
+  {
+    if ( !internal )
+      throw TypedError( "LogicError", std::string("Invalid (null) object handle passed to ") + fct );
+    auto fp = static_cast<FingerPrint*>( internal );
+    if ( fp->typeid_ != kScatterTypeID && fp->typeid_ != kAbsTypeID )
+      throw TypedError( "LogicError", std::string("Invalid object handle type passed to ") + fct );
+    return *fp->obj;
+  }
+
+  ScatterObj& extractAbs( void* internal, const char* fct )
+  {
+    ScatterObj& o = extractProc( internal, fct );
+    if ( !o.absorption )
+      throw TypedError( "LogicError", std::string("Invalid object handle type passed to ") + fct );
+    return o;
+  }
 
   // ---- per-thread scratch ----------------------------------------------------
   // Device buffers of one host thread: staging for host-array calls, and the
@@ -541,7 +563,7 @@ void ncrystal_invalidate( void* object )
 int ncrystal_refcount( void* object )
 {
   try {
-    return extract( internalOf( object ), "ncrystal_refcount" ).refcount.load();
+    return extractProc( internalOf( object ), "ncrystal_refcount" ).refcount.load();
   } NCGB_CATCH;
   return -999;
 }
@@ -549,14 +571,14 @@ int ncrystal_refcount( void* object )
 void ncrystal_ref( void* object )
 {
   try {
-    extract( internalOf( object ), "ncrystal_ref" ).refcount.fetch_add( 1 );
+    extractProc( internalOf( object ), "ncrystal_ref" ).refcount.fetch_add( 1 );
   } NCGB_CATCH;
 }
 
 void ncrystal_unref( void* object )
 {
   try {
-    ScatterObj& o = extract( internalOf( object ), "ncrystal_unref" );
+    ScatterObj& o = extractProc( internalOf( object ), "ncrystal_unref" );
     if ( o.refcount.fetch_sub( 1 ) == 1 ) {
       delete &o;
       internalOf( object ) = nullptr;
@@ -663,16 +685,71 @@ ncrystal_process_t ncrystal_cast_scat2proc( ncrystal_scatter_t s )
 ncrystal_scatter_t ncrystal_cast_proc2scat( ncrystal_process_t p )
 {
   try {
-    extract( p.internal, "ncrystal_cast_proc2scat" );
-    return ncrystal_scatter_t{ p.internal };
+    // ncrystal.cc:420-429: null (no error) for a valid process of another type
+    ScatterObj& o = extractProc( p.internal, "ncrystal_cast_proc2scat" );
+    return ncrystal_scatter_t{ o.absorption ? nullptr : p.internal };
   } NCGB_CATCH;
   return ncrystal_scatter_t{ nullptr };
+}
+
+ncrystal_process_t ncrystal_cast_abs2proc( ncrystal_absorption_t a )
+{
+  try {
+    extractAbs( a.internal, "ncrystal_cast_abs2proc" );
+    return ncrystal_process_t{ a.internal };
+  } NCGB_CATCH;
+  return ncrystal_process_t{ nullptr };
+}
+
+ncrystal_absorption_t ncrystal_cast_proc2abs( ncrystal_process_t p )
+{
+  try {
+    ScatterObj& o = extractProc( p.internal, "ncrystal_cast_proc2abs" );
+    return ncrystal_absorption_t{ o.absorption ? p.internal : nullptr };
+  } NCGB_CATCH;
+  return ncrystal_absorption_t{ nullptr };
+}
+
+// ncrystal.cc:1565-1571 with the standard absorption factory's AbsOOV
+// (NCStdAbsFact.cc:49-52), read from the material's bundle.
+ncrystal_absorption_t ncrystal_create_absorption( const char* cfgstr )
+{
+  try {
+    if ( !cfgstr )
+      throw TypedError( "BadInput", "null cfg-string" );
+    std::unique_ptr<ScatterObj> o( new ScatterObj );
+    o->mat = getMaterial( cfgstr );
+    if ( !( o->mat->view.abs_c >= 0.0 ) )
+      throw TypedError( "BadInput", std::string( "the material bundle of \"" ) + cfgstr
+                        + "\" carries no absorption data (export it again)" );
+    o->cfg = cfgstr;
+    o->absorption = true;
+    o->fp.typeid_ = kAbsTypeID;
+    return ncrystal_absorption_t{ &o.release()->fp };
+  } NCGB_CATCH;
+  return ncrystal_absorption_t{ nullptr };
+}
+
+ncrystal_absorption_t ncrystal_clone_absorption( ncrystal_absorption_t a )
+{
+  try {
+    ScatterObj& src = extractAbs( a.internal, "ncrystal_clone_absorption" );
+    std::unique_ptr<ScatterObj> o( new ScatterObj );
+    o->mat = src.mat;
+    o->cfg = src.cfg;
+    o->absorption = true;
+    o->fp.typeid_ = kAbsTypeID;
+    return ncrystal_absorption_t{ &o.release()->fp };
+  } NCGB_CATCH;
+  return ncrystal_absorption_t{ nullptr };
 }
 
 const char* ncrystal_name( ncrystal_process_t p )
 {
   try {
-    ScatterObj& o = extract( p.internal, "ncrystal_name" );
+    ScatterObj& o = extractProc( p.internal, "ncrystal_name" );
+    if ( o.absorption )
+      return "AbsOOV";
     return o.mat->view.ncomp > 1 ? "ProcComposition"
       : ( o.mat->view.ncomp == 0 ? "NullProcess"
           : ( o.mat->view.comp[0].type == NCGB_COMP_BRAGG ? "PowderBragg"
@@ -685,7 +762,7 @@ const char* ncrystal_name( ncrystal_process_t p )
 int ncrystal_isnonoriented( ncrystal_process_t p )
 {
   try {
-    extract( p.internal, "ncrystal_isnonoriented" );
+    extractProc( p.internal, "ncrystal_isnonoriented" );
     return 1;
   } NCGB_CATCH;
   return 0;
@@ -694,7 +771,12 @@ int ncrystal_isnonoriented( ncrystal_process_t p )
 void ncrystal_domain( ncrystal_process_t p, double* elow, double* ehigh )
 {
   try {
-    ScatterObj& o = extract( p.internal, "ncrystal_domain" );
+    ScatterObj& o = extractProc( p.internal, "ncrystal_domain" );
+    if ( o.absorption ) {   // NCAbsOOV.cc:33-37
+      *elow = 0.0;
+      *ehigh = o.mat->view.abs_c > 0.0 ? std::numeric_limits<double>::infinity() : 0.0;
+      return;
+    }
     *elow = o.mat->view.dom_elow;
     *ehigh = o.mat->view.dom_ehigh;
     return;
@@ -708,7 +790,7 @@ void ncrystal_crosssection_nonoriented_many( ncrystal_process_t p, const double*
                                              unsigned long n_ekin, unsigned long repeat, double* results )
 {
   try {
-    ScatterObj& o = extract( p.internal, "ncrystal_crosssection_nonoriented_many" );
+    ScatterObj& o = extractProc( p.internal, "ncrystal_crosssection_nonoriented_many" );
     checkSize( n_ekin, repeat );
     const uint64_t n_out = (uint64_t)n_ekin * repeat;
     if ( n_out == 0 )
@@ -724,7 +806,10 @@ void ncrystal_crosssection_nonoriented_many( ncrystal_process_t p, const double*
     b.out_xs = s.d_a;
     checkCuda( cudaStreamWaitEvent( s.stream, s.done, 0 ), "cudaStreamWaitEvent" );
     checkCuda( cudaMemcpyAsync( s.d_in, ekin, n_ekin * sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
-    checkCuda( ncgb::launchXS( dm.view, b, repeat, s.stream ), "xs kernel" );
+    if ( o.absorption )
+      checkCuda( ncgb::launchAbsXS( dm.view.abs_c, b, repeat, s.stream ), "absorption xs kernel" );
+    else
+      checkCuda( ncgb::launchXS( dm.view, b, repeat, s.stream ), "xs kernel" );
     checkCuda( cudaMemcpyAsync( results, s.d_a, n_out * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
     checkCuda( cudaEventRecord( s.done, s.stream ), "cudaEventRecord" );
     checkCuda( cudaStreamSynchronize( s.stream ), "xs kernel" );
@@ -847,6 +932,33 @@ void ncrystal_samplescatter_many( ncrystal_scatter_t sc, double ekin, const doub
     results_ekin[k] = -1.0;
     results_dirx[k] = results_diry[k] = results_dirz[k] = 0.0;
   }
+}
+
+int ncgb_xs_abs_scatter_device( ncrystal_scatter_t sc, const double* d_ekin, unsigned long n, double* d_xs,
+                                double* d_xs_abs, double* d_ekin_final, double* d_mu, int32_t* d_status,
+                                void* stream )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_xs_abs_scatter_device" );
+    checkSize( n, 1 );
+    if ( n == 0 )
+      return 0;
+    if ( d_xs_abs && !( o.mat->view.abs_c >= 0.0 ) )
+      throw TypedError( "BadInput", "ncgb_xs_abs_scatter_device: the material bundle carries no absorption data" );
+    DeviceMaterial& dm = *o.mat;
+    Scratch& s = scratchFor( dm );
+    ncgb::Batch b = makeBatch( o, s, nextCall( o ) );
+    b.ekin = d_ekin;
+    b.n_ekin = b.n_out = n;
+    b.out_xs = d_xs;
+    b.out_xs_abs = d_xs_abs;
+    b.out_a = d_ekin_final;
+    b.out_b = d_mu;
+    b.status = d_status;
+    runBatch( dm, s, b, static_cast<cudaStream_t>( stream ) );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
 }
 
 int ncgb_scatter_dir_device( ncrystal_scatter_t sc, const double* d_ekin, const double* d_dir, unsigned long n,

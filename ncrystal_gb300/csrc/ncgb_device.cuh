@@ -280,6 +280,14 @@ namespace ncgb_dev {
     return xs;
   }
 
+  // AbsOOV::crossSectionIsotropic, NCAbsOOV.cc:40-44: c/sqrt(E), infinite at
+  // E = 0 (NaN for E < 0, as in the reference).
+  __device__ __forceinline__ double absXS( double c, double ekin )
+  {
+    const double se = sqrt( ekin );
+    return se != 0.0 ? c / se : infd();
+  }
+
   // PowderBragg, NCPowderBragg.cc:152-176.  idx_out: last valid plane.
   __device__ __forceinline__ double braggXS( const ncgb_bragg_view& v, double ekin, int64_t& idx_out )
   {

@@ -147,6 +147,8 @@ namespace {
       src.rngFor( rng, k, o, b.callseq );
       bool queue = false;
       int qcomp = 0;
+      if ( b.out_xs_abs )
+        store( b.out_xs_abs, b.out_f32, o, absXS( m.abs_c, e ) );
       if ( !contains( m.dom_elow, m.dom_ehigh, e ) ) {
         // ProcComposition outside its domain: xs 0, neutron unchanged (NCProcImpl.cc:353-389)
         store( b.out_xs, b.out_f32, o, 0.0 );
@@ -295,6 +297,18 @@ namespace {
         b.status[i] = st;
       if ( st != NCGB_ST_OK )
         atomicAdd( &b.work->nfail, 1ull );
+    }
+  }
+
+  // ---- absorption cross-sections (AbsOOV) ---------------------------------------
+  __global__ void __launch_bounds__(256)
+  k_absxs( double abs_c, const ncgb::Batch b, uint64_t repeat )
+  {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for ( uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < b.n_ekin; i += stride ) {
+      const double xs = absXS( abs_c, loadE( b, i ) );
+      for ( uint64_t r = 0; r < repeat; ++r )
+        store( b.out_xs, b.out_f32, r * b.n_ekin + i, xs );
     }
   }
 
@@ -464,6 +478,14 @@ namespace ncgb {
       k_xs<true><<<gridFor( b.n_ekin, 256 ), 256, 0, s>>>( m, b, repeat );
     else
       k_xs<false><<<gridFor( b.n_ekin, 256 ), 256, 0, s>>>( m, b, repeat );
+    return cudaGetLastError();
+  }
+
+  cudaError_t launchAbsXS( double abs_c, const Batch& b, uint64_t repeat, cudaStream_t s )
+  {
+    if ( b.n_ekin == 0 || repeat == 0 )
+      return cudaSuccess;
+    k_absxs<<<gridFor( b.n_ekin, 256 ), 256, 0, s>>>( abs_c, b, repeat );
     return cudaGetLastError();
   }
 

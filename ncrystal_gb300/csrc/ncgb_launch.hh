@@ -57,6 +57,7 @@ namespace ncgb {
     void* out_xs;      // may be null
     void* out_a;       // may be null
     void* out_b;       // may be null
+    void* out_xs_abs;      // absorption cross-sections (AbsOOV) beside the scattering ones, or null
     const double* dir_in;  // [n_ekin][3] incoming directions (sampleScatter with directions), or null
     double* dir_out;       // [n_out][3] outgoing directions, or null
     int32_t* status;   // may be null
@@ -74,6 +75,8 @@ namespace ncgb {
   // neutron i uses stream (seed, index_offset + i, callseq, stream); failures
   // counted in work->nfail.
   cudaError_t launchSabAB( const ncgb_material_view& m, int comp, const Batch& b, cudaStream_t s );
+  // Absorption cross-sections c/sqrt(E) (AbsOOV) into out_xs, repeat layout as launchXS.
+  cudaError_t launchAbsXS( double abs_c, const Batch& b, uint64_t repeat, cudaStream_t s );
   cudaError_t launchXS( const ncgb_material_view& m, const Batch& b, uint64_t repeat, cudaStream_t s );
   int scatterLaunchesPerBatch();
   void setPhaseTiming( bool on );

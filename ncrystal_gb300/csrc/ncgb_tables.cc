@@ -475,6 +475,7 @@ namespace ncgb {
     v.ncomp = static_cast<int32_t>( ncomp );
     v.dom_elow = b.f64s("elow");
     v.dom_ehigh = b.f64s("ehigh");
+    v.abs_c = b.has("abs_c") ? b.f64s("abs_c") : -1.0;
     if ( ncomp == 0 ) {
       // A null process: empty domain, so xs = 0 and scatterings leave E unchanged.
       v.dom_elow = kInf;

@@ -1234,3 +1234,12 @@ int64_t ncgb_oracle_scatter_dir_many( const ncgb_material_view* m, const double*
   }
   return nbad;
 }
+
+/* AbsOOV::crossSectionIsotropic, NCAbsOOV.cc:40-44: c/sqrt(E), infinite at E = 0. */
+void ncgb_oracle_abs_xs_many( const ncgb_material_view* m, const double* ekin, int64_t n, double* out )
+{
+  for ( int64_t i = 0; i < n; ++i ) {
+    const double se = sqrt( ekin[i] );
+    out[i] = se ? m->abs_c / se : ora_inf;
+  }
+}

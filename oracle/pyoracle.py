@@ -34,6 +34,8 @@ def oracle_lib():
         L.ncgb_oracle_xs.argtypes = [C.c_void_p, C.c_double]
         L.ncgb_oracle_xs_many.restype = None
         L.ncgb_oracle_xs_many.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+        L.ncgb_oracle_abs_xs_many.restype = None
+        L.ncgb_oracle_abs_xs_many.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
         L.ncgb_oracle_scatter_dir_many.restype = C.c_int64
         L.ncgb_oracle_scatter_dir_many.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64,
                                                    C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
@@ -167,6 +169,17 @@ def _scatter_dir(self, ekin, direction, seed, index_offset=0, callseq=0, stream=
 HostMaterial.scatter_dir = _scatter_dir
 
 
+def _abs_xs(self, ekin):
+    """Absorption cross-sections (AbsOOV) of the material."""
+    e = np.ascontiguousarray(ekin, dtype=np.float64)
+    out = np.empty(len(e))
+    oracle_lib().ncgb_oracle_abs_xs_many(self.view, _P(e), len(e), _P(out))
+    return out
+
+
+HostMaterial.abs_xs = _abs_xs
+
+
 def refpin_lib():
     """The harness around the reference library (only where it was built)."""
     global _refpin
@@ -175,6 +188,8 @@ def refpin_lib():
         if not os.path.exists(path):
             return None
         L = C.CDLL(path)
+        L.refpin_abs_xs.restype = C.c_int
+        L.refpin_abs_xs.argtypes = [C.c_char_p, C.c_void_p, C.c_int64, C.c_void_p]
         L.refpin_run_dir.restype = C.c_int
         L.refpin_run_dir.argtypes = [C.c_char_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                                      C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -217,4 +232,16 @@ def reference_run_dir(cfg, ekin, direction, seed, callseq=0, stream=0):
                           _P(out["direction"]), _P(out["ndraws"]), _P(out["status"]))
     if rc:
         raise RuntimeError("reference could not create %r" % cfg)
+    return out
+
+
+def reference_abs_xs(cfg, ekin):
+    """The reference's absorption cross-sections for cfg."""
+    L = refpin_lib()
+    if L is None:
+        raise RuntimeError("reference harness not built")
+    e = np.ascontiguousarray(ekin, dtype=np.float64)
+    out = np.empty(len(e))
+    if L.refpin_abs_xs(cfg.encode(), _P(e), len(e), _P(out)):
+        raise RuntimeError("reference could not create absorption for %r" % cfg)
     return out

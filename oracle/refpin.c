@@ -107,3 +107,19 @@ int refpin_run_dir( const char* cfg, uint64_t seed, uint32_t callseq, uint32_t s
   ncrystal_setrandgen( NULL );
   return 0;
 }
+
+/* The reference's absorption cross-sections (ncrystal_create_absorption,
+ * ncrystal.cc:1565-1571, through the process interface). */
+int refpin_abs_xs( const char* cfg, const double* ekin, int64_t n, double* out_xs )
+{
+  ncrystal_sethaltonerror( 0 );
+  ncrystal_absorption_t ab = ncrystal_create_absorption( cfg );
+  if ( ncrystal_error() ) {
+    fprintf( stderr, "refpin: could not create absorption for %s: %s\n", cfg, ncrystal_lasterror() );
+    ncrystal_clearerror();
+    return 1;
+  }
+  ncrystal_crosssection_nonoriented_many( ncrystal_cast_abs2proc( ab ), ekin, (unsigned long)n, 1, out_xs );
+  ncrystal_unref( &ab );
+  return 0;
+}

@@ -9,10 +9,11 @@ mu, the number of random numbers the reference consumed and whether it raised
 an error.  Neutron i uses stream (SEED, i, 0, 0).
 
 dir_*.npz: the same for the reference's ncrystal_samplescatter (scatters with
-incoming and outgoing directions).
+incoming and outgoing directions).  abs_xs.npz: the reference's absorption
+cross-sections (ncrystal_create_absorption) for several materials.
 
 Run from the repository root where the NCrystal sources exist:
-    python tests/golden/make_golden.py [--dirs-only]
+    python tests/golden/make_golden.py [--dirs-only | --abs-only]
 """
 import os
 import sys
@@ -56,6 +57,10 @@ DIR_GOLDEN = {
 }
 N_DIR = 1000
 
+# Absorption cross-sections (ncrystal_create_absorption).
+ABS_CFGS = [W.AL, W.AL2O3, W.PE293, W.WATER, "Cu_sg225.ncmat;temp=77K",
+            "ZnO_sg186_ZincOxide.ncmat;temp=400K", "Ni_sg225.ncmat;dcutoff=0.6;vdoslux=2"]
+
 
 def dir_inputs(seed):
     rng = np.random.default_rng(seed)
@@ -89,7 +94,8 @@ def main():
     B.build_library()
     cfgs = [c for c, _ in GOLDEN.values()]
     paths = B.export_bundles(cfgs)
-    for key, (cfg, gen) in ([] if "--dirs-only" in sys.argv else GOLDEN.items()):
+    only = [a for a in sys.argv[1:] if a.endswith("-only")]
+    for key, (cfg, gen) in ([] if only else GOLDEN.items()):
         b = read_bundle(paths[cfg])
         ekin = np.concatenate([gen(N_RANDOM), edge_energies(b)])
         r = pyoracle.reference_run(cfg, ekin, SEED)
@@ -99,7 +105,7 @@ def main():
                             status=r["status"])
         print("%-8s %-55s n=%d errors=%d -> %s" % (key, cfg, len(ekin), int(r["status"].sum()), out))
     B.export_bundles([c for c, _ in DIR_GOLDEN.values()])
-    for key, (cfg, seed) in DIR_GOLDEN.items():
+    for key, (cfg, seed) in (DIR_GOLDEN.items() if not only or "--dirs-only" in only else []):
         e, d = dir_inputs(seed)
         r = pyoracle.reference_run_dir(cfg, e, d, SEED)
         out = os.path.join(HERE, key + ".npz")
@@ -107,6 +113,13 @@ def main():
                             ekin_final=r["ekin_final"], direction_final=r["direction"], ndraws=r["ndraws"],
                             status=r["status"])
         print("%-10s %-45s n=%d errors=%d -> %s" % (key, cfg, len(e), int(r["status"].sum()), out))
+    if not only or "--abs-only" in only:
+        B.export_bundles(ABS_CFGS)
+        e = np.concatenate([W.loguniform_energies(500, 1e-6, 100.0, 301), [0.0, 1e-300, 0.0253, 1e10]])
+        xs = np.stack([pyoracle.reference_abs_xs(c, e) for c in ABS_CFGS])
+        out = os.path.join(HERE, "abs_xs.npz")
+        np.savez_compressed(out, cfgs=np.array(ABS_CFGS), ekin=e, xs=xs)
+        print("abs_xs %d materials x %d energies -> %s" % (len(ABS_CFGS), len(e), out))
 
 
 if __name__ == "__main__":

@@ -16,7 +16,7 @@ from oracle.pyoracle import HostMaterial
 pytestmark = pytest.mark.gpu
 
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                if not os.path.basename(p).startswith("dir_"))
+                if not os.path.basename(p).startswith(("dir_", "abs_")))
 
 # FP64 on the GPU differs from the reference's FP64 only by libm rounding
 # (expm1/log/exp/erf of CUDA vs glibc) and fused multiply-adds.
@@ -211,3 +211,46 @@ def test_ragged_batch_matches_single_material_calls():
     # host-array entry point
     hxs, hef, hmu = batch.xs_scatter_host(e_all.cpu().numpy(), off.cpu().numpy())
     np.testing.assert_array_equal(hxs, xs.cpu().numpy())
+
+
+def test_absorption_matches_reference_golden():
+    """ncrystal_create_absorption + ncrystal_crosssection_nonoriented_many on
+    the GPU against the reference's values (AbsOOV, c/sqrt(E): a square root
+    and a division, both correctly rounded: bit for bit)."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "abs_xs.npz"))
+    for k, cfg in enumerate(g["cfgs"]):
+        cfg = str(cfg)
+        bundle_path(cfg)
+        ab = NC.createAbsorption(cfg)
+        assert ab.name == "AbsOOV"
+        np.testing.assert_array_equal(ab.crossSectionIsotropic(g["ekin"]), g["xs"][k])
+        assert ab.domain() == (0.0, np.inf)
+        assert ab.clone().crossSectionIsotropic(0.0253) == ab.crossSectionIsotropic(0.0253)
+
+
+def test_absorption_handle_casts():
+    L = NC.lib()
+    ab = NC.createAbsorption(W.AL)
+    sc = NC.createScatter(W.AL)
+    p_ab = L.ncrystal_cast_abs2proc(ab._h)
+    p_sc = L.ncrystal_cast_scat2proc(sc._h)
+    # a valid process of the other kind casts to null without an error
+    assert not L.ncrystal_cast_proc2scat(p_ab).internal
+    assert not L.ncrystal_cast_proc2abs(p_sc).internal
+    assert L.ncrystal_cast_proc2abs(p_ab).internal == ab._h.internal
+    assert not L.ncrystal_error()
+
+
+def test_fused_absorption_equals_separate_calls():
+    import torch
+    cfg = W.PE293
+    e = W.loguniform_energies(100000, 1e-5, 5.0, 71)
+    t = torch.as_tensor(e, device="cuda")
+    xs, xa, ef, mu = (torch.empty_like(t) for _ in range(4))
+    NC.createScatter(cfg, seed=3).xs_abs_scatter_device(t, xs, xa, ef, mu)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(xa.cpu().numpy(), NC.createAbsorption(cfg).crossSectionIsotropic(e))
+    sxs, sef, smu = _device_run(NC.createScatter(cfg, seed=3), e)
+    np.testing.assert_array_equal(xs.cpu().numpy(), sxs)
+    np.testing.assert_array_equal(ef.cpu().numpy(), sef)
+    np.testing.assert_array_equal(mu.cpu().numpy(), smu)

@@ -11,7 +11,7 @@ from conftest import KAT_AL_BRAGG, KAT_NI, bundle_path
 from oracle.pyoracle import HostMaterial
 
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                if not os.path.basename(p).startswith("dir_"))
+                if not os.path.basename(p).startswith(("dir_", "abs_")))
 WL2EKIN = 0.081804209605330899
 
 
@@ -81,3 +81,12 @@ def test_oracle_directions_match_reference_golden(path):
     np.testing.assert_allclose(d, g["direction_final"], rtol=0, atol=1e-13)
     inside = g["ekin"] > 0
     np.testing.assert_allclose(np.linalg.norm(d[inside], axis=1), 1.0, atol=1e-12)
+
+
+def test_oracle_absorption_matches_reference_golden():
+    """AbsOOV cross-sections c/sqrt(E) against the reference's
+    (ncrystal_create_absorption), bit for bit."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "abs_xs.npz"))
+    for k, cfg in enumerate(g["cfgs"]):
+        m = HostMaterial(bundle_path(str(cfg)))
+        np.testing.assert_array_equal(m.abs_xs(g["ekin"]), g["xs"][k])

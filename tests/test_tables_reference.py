@@ -79,3 +79,10 @@ def test_oracle_directions_equal_live_reference(cfg):
     np.testing.assert_array_equal(st != 0, ref["status"] != 0)
     np.testing.assert_array_equal(ef, ref["ekin_final"])
     np.testing.assert_array_equal(do, ref["direction"])
+
+
+@pytest.mark.parametrize("cfg", [W.AL, W.PE293, W.WATER, W.AL2O3])
+def test_oracle_absorption_equals_live_reference(cfg):
+    m = pyoracle.HostMaterial(B.export_bundles([cfg])[cfg])
+    e = np.concatenate([W.loguniform_energies(3000, 1e-7, 1e3, 5), [0.0, -1.0, np.inf]])
+    np.testing.assert_array_equal(m.abs_xs(e), pyoracle.reference_abs_xs(cfg, e))
