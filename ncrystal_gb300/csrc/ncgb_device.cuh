@@ -969,8 +969,8 @@ namespace ncgb_dev {
       L.ultra_small = ( ekin < ldg( s.egrid ) );
     } else {
       if ( s.egrid_margin > 1.0 ) {
-        const double em = ekin * s.egrid_margin;
-        while ( iu + 1 != ne && em > ldg( s.egrid + iu ) )
+        const long long em = bits( ekin * s.egrid_margin );   // non-negative: integer compares
+        while ( iu + 1 != ne && em > ldgbits( s.egrid + iu ) )
           ++iu;
       }
       L.ie = iu;
@@ -1041,6 +1041,20 @@ namespace ncgb_dev {
     if ( beta <= L.xtrue * ( -1.0 + 1e-14 ) ) { // muIsotropicAtBeta, NCKinUtils.hh:64-70
       deltaE = beta * s.kT;
       muv = rand01( rng ) * 2.0 - 1.0;
+    } else if ( Fast && !( fabs( beta ) < 0.01 * L.xtrue ) ) {
+      // Mixed mode away from the elastic line (|beta| >= 0.01 E/kT, outside
+      // getAlphaLimits' Taylor region): with a = sqrt(x), b = sqrt(x+beta),
+      // alpha- = (b-a)^2 and E + E' - alpha kT = kT (2ab - (alpha - alpha-)),
+      // so mu = 1 - (alpha - alpha-)/(2ab), in FP32 without cancellation; the
+      // energy transfer beta kT and 1 - d stay FP64.
+      deltaE = beta * s.kT;
+      const float a = sqrtf( (float)L.xtrue ), b = sqrtf( (float)( L.xtrue + beta ) );
+      const float ab = a * b;
+      if ( !( ab > 0.0f ) )
+        return NCGB_ST_CALCERROR;
+      const float bf = (float)beta, sab = a + b;
+      const float d = ( (float)alpha - ( bf * bf ) / ( sab * sab ) ) / ( 2.0f * ab );
+      muv = clampd( 1.0 - (double)d, -1.0, 1.0 );
     } else {
       const int st = alphaBetaToDeltaEMu( alpha, beta, L.ekin, s.kT, deltaE, muv );
       if ( st != NCGB_ST_OK )
