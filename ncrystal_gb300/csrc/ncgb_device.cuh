@@ -316,12 +316,44 @@ namespace ncgb_dev {
     return ( 1.0 + 0.5*inva*inva ) * erf( a ) + 0.564189583547756286948079451560772585844050629 * exp( -a_squared ) * inva;
   }
 
+  // std::upper_bound over the energy grid for E >= 0 (or NaN): the bucket of
+  // E's bit pattern narrows the range to a few entries (same result).
+  __device__ __forceinline__ int64_t egridUpper( const ncgb_sab_view& s, double e )
+  {
+    const long long eb = bits( e );
+    const long long k = ( eb >> 49 ) - s.ebkt_kmin;
+    if ( k < 0 )
+      return 0;
+    if ( k >= s.ebkt_n )
+      return s.ne;
+    int64_t i = __ldg( s.ebkt + k );
+    const int64_t hi = __ldg( s.ebkt + k + 1 );
+    while ( i < hi && !( eb < ldgbits( s.egrid + i ) ) )
+      ++i;
+    return i;
+  }
+
+  __device__ __forceinline__ int egridUpperF( const ncgb_sab_view& s, float e )
+  {
+    const int eb = __float_as_int( e );
+    const int k = ( eb >> 20 ) - s.ebkt_f_kmin;
+    if ( k < 0 )
+      return 0;
+    if ( k >= s.ebkt_f_n )
+      return s.ne;
+    int i = __ldg( s.ebkt_f + k );
+    const int hi = __ldg( s.ebkt_f + k + 1 );
+    while ( i < hi && !( eb < __float_as_int( __ldg( s.egrid_f + i ) ) ) )
+      ++i;
+    return i;
+  }
+
   // SABXSProvider::crossSection (NCSABXSProvider.cc:54-95) x SABScatter scale
   // (NCSABScatter.cc:87-90).  Requires ekin >= 0 and not NaN.
   __device__ __forceinline__ double sabXS( const ncgb_sab_view& s, double ekin )
   {
     const int64_t ne = s.ne;
-    const int64_t iu = upper_bound_nn( s.egrid, ne, ekin );
+    const int64_t iu = egridUpper( s, ekin );
     double xs;
     if ( iu == ne ) {
       xs = s.kext / ekin + s.ext_sigma_free * freeGasShape( s.ext_ca * ekin );
@@ -339,7 +371,7 @@ namespace ncgb_dev {
   __device__ __forceinline__ float sabXSf( const ncgb_sab_view& s, double ekin, float ef )
   {
     const int ne = s.ne;
-    const int iu = upper_bound_f( s.egrid_f, ne, ef );
+    const int iu = egridUpperF( s, ef );
     if ( iu == ne )
       return (float)sabXS( s, ekin );
     float xs;
@@ -945,7 +977,7 @@ namespace ncgb_dev {
                                            ncgb_rng& rng, SABLane& L )
   {
     const int64_t ne = s.ne;
-    int64_t iu = upper_bound_nn( s.egrid, ne, ekin );
+    int64_t iu = egridUpper( s, ekin );
     L.ekin = ekin;
     L.ultra_small = false;
     L.preset = false;

@@ -167,6 +167,9 @@ int ncgb_tables_array( void* handle, int comp, const char* name, const void** pt
   if ( n == "by" ) { *ptr = s.by; *count = nsmp; return 0; }
   if ( n == "bcdf" ) { *ptr = s.bcdf; *count = nsmp; return 0; }
   if ( n == "info" ) { *ptr = s.info; *count = nsmp; return 0; }
+  if ( n == "ebkt" ) { *ptr = s.ebkt; *count = (unsigned long)s.ebkt_n + 1; return 0; }
+  if ( n == "ebkt_f" ) { *ptr = s.ebkt_f; *count = (unsigned long)s.ebkt_f_n + 1; return 0; }
+  if ( n == "egrid_f" ) { *ptr = s.egrid_f; *count = ne; return 0; }
   return 1;
 }
 
@@ -181,6 +184,8 @@ int ncgb_tables_scalar( void* handle, int comp, const char* name, double* out )
   const ncgb_sab_view& s = v.comp[comp].sab;
   const std::string n( name );
   if ( n == "kext" ) { *out = s.kext; return 0; }
+  if ( n == "ebkt_kmin" ) { *out = (double)s.ebkt_kmin; return 0; }
+  if ( n == "ebkt_f_kmin" ) { *out = (double)s.ebkt_f_kmin; return 0; }
   if ( n == "k1" ) { *out = s.k1; return 0; }
   if ( n == "k2" ) { *out = s.k2; return 0; }
   if ( n == "type" ) { *out = v.comp[comp].type; return 0; }

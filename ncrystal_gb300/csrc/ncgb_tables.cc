@@ -582,6 +582,36 @@ namespace ncgb {
         }
         s.egrid_f = encodeOff<float>( mt->put( egf ) );
         s.xsf = encodeOff<float>( mt->put( xsf ) );
+        // bucket index of the energy grid (eight buckets per octave of the
+        // IEEE representation): the GPU's grid searches start at the bucket
+        // and scan a few entries, with the same result as a binary search
+        {
+          auto key64 = []( double x ) { int64_t b; std::memcpy( &b, &x, 8 ); return b >> 49; };
+          auto key32 = []( float x ) { int32_t b; std::memcpy( &b, &x, 4 ); return b >> 20; };
+          const std::size_t ne = in.egrid.size();
+          const int64_t k0 = key64( in.egrid.front() ), k1 = key64( in.egrid.back() );
+          std::vector<int32_t> bk( static_cast<std::size_t>( k1 - k0 + 2 ) );
+          std::size_t i = 0;
+          for ( int64_t k = k0; k <= k1 + 1; ++k ) {
+            while ( i < ne && key64( in.egrid[i] ) < k )
+              ++i;
+            bk[k - k0] = static_cast<int32_t>( i );
+          }
+          s.ebkt = encodeOff<int32_t>( mt->put( bk ) );
+          s.ebkt_kmin = k0;
+          s.ebkt_n = static_cast<int32_t>( bk.size() - 1 );
+          const int32_t f0 = key32( egf.front() ), f1 = key32( egf.back() );
+          std::vector<int32_t> bf( static_cast<std::size_t>( f1 - f0 + 2 ) );
+          i = 0;
+          for ( int32_t k = f0; k <= f1 + 1; ++k ) {
+            while ( i < ne && key32( egf[i] ) < k )
+              ++i;
+            bf[k - f0] = static_cast<int32_t>( i );
+          }
+          s.ebkt_f = encodeOff<int32_t>( mt->put( bf ) );
+          s.ebkt_f_kmin = f0;
+          s.ebkt_f_n = static_cast<int32_t>( bf.size() - 1 );
+        }
         std::vector<ncgb_beta_bin> bbin( d.bx.size() );
         std::memset( bbin.data(), 0, bbin.size() * sizeof(ncgb_beta_bin) );
         for ( std::size_t ie = 0; ie < d.kind.size(); ++ie ) {
@@ -732,6 +762,8 @@ namespace ncgb {
       s.info = reloc( s.info, base );
       s.inv_dE = reloc( s.inv_dE, base );
       s.egrid_f = reloc( s.egrid_f, base );
+      s.ebkt = reloc( s.ebkt, base );
+      s.ebkt_f = reloc( s.ebkt_f, base );
       s.xsf = reloc( s.xsf, base );
       s.inv_dbeta = reloc( s.inv_dbeta, base );
       s.bbin = reloc( s.bbin, base );

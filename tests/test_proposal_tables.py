@@ -158,3 +158,49 @@ def test_oracle_learned_distribution_matches_plain(kind, e0):
     assert p > alpha, (stat, p)
     assert ks_2samp(ef0, ef1).pvalue > alpha
     assert ks_2samp(mu0, mu1).pvalue > alpha
+
+
+def test_energy_grid_bucket_index_equals_binary_search(pe):
+    """The GPU's energy-grid search (bucket of E's bit pattern, then a short
+    scan; ncgb_device.cuh egridUpper / egridUpperF) gives std::upper_bound's
+    index for every energy, in FP64 and FP32."""
+    r = np.random.default_rng(3)
+    for comp in _sab_comps(pe):
+        eg = pe.array(comp, "egrid", np.float64)
+        egf = pe.array(comp, "egrid_f", np.float32)
+        bk = pe.array(comp, "ebkt", np.int32)
+        bkf = pe.array(comp, "ebkt_f", np.int32)
+        k0 = int(pe.scalar(comp, "ebkt_kmin"))
+        k0f = int(pe.scalar(comp, "ebkt_f_kmin"))
+        e = np.concatenate([np.exp(r.uniform(np.log(1e-9), np.log(1e3), 200000)), eg, np.nextafter(eg, 0),
+                            np.nextafter(eg, np.inf), [0.0, np.inf]])
+
+        def upper64(x):
+            b = np.array([x]).view(np.int64)[0]
+            k = (b >> 49) - k0
+            if k < 0:
+                return 0
+            if k >= len(bk) - 1:
+                return len(eg)
+            i, hi = bk[k], bk[k + 1]
+            while i < hi and not (b < eg[i:i + 1].view(np.int64)[0]):
+                i += 1
+            return i
+
+        def upper32(x):
+            b = np.array([x], dtype=np.float32).view(np.int32)[0]
+            k = (b >> 20) - k0f
+            if k < 0:
+                return 0
+            if k >= len(bkf) - 1:
+                return len(egf)
+            i, hi = bkf[k], bkf[k + 1]
+            while i < hi and not (b < egf[i:i + 1].view(np.int32)[0]):
+                i += 1
+            return i
+        sub = e[::50]
+        got = np.array([upper64(x) for x in sub])
+        np.testing.assert_array_equal(got, np.searchsorted(eg, sub, side="right"))
+        subf = sub.astype(np.float32)
+        gotf = np.array([upper32(x) for x in subf])
+        np.testing.assert_array_equal(gotf, np.searchsorted(egf, subf, side="right"))
