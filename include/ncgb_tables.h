@@ -144,6 +144,15 @@ typedef struct {
   const double* xs;     /* [ne] */
   const float* egrid_f; /* [ne] FP32 copy (mixed-precision mode) */
   const float* xsf;     /* [2*ne] (xs_i, (xs_i+1 - xs_i)/(egrid_i+1 - egrid_i)) in FP32 */
+  /* energy-grid bucket index: for key k = (bits of E) >> 49 (f64) or >> 20
+   * (f32) -- eight buckets per octave -- ebkt[k - kmin] is the first grid index
+   * whose key is >= k (nbkt + 1 entries, the last = ne) */
+  const int32_t* ebkt;
+  const int32_t* ebkt_f;
+  int64_t ebkt_kmin;
+  int32_t ebkt_f_kmin;
+  int32_t ebkt_n, ebkt_f_n;
+  int32_t pad1;
   /* kernel grid, S stored beta-major: idx = ibeta*na + ialpha */
   const double* alpha;  /* [na] */
   const double* beta;   /* [nb] */
