@@ -134,7 +134,7 @@ namespace {
 
   // ---- phase 1: cross-section, pick, short samplers, SAB queue ----------------
   template<class Src, bool Fast, bool Dir>
-  __global__ void __launch_bounds__(512)
+  __global__ void __launch_bounds__(512, 4)
   k_pick( const __grid_constant__ Src src, const ncgb::Batch b )
   {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
