@@ -452,9 +452,9 @@ namespace {
   {
     std::ostringstream ss;
     ss << "Sampling failed for " << nfail << " neutron(s): a rejection loop reached its limit of attempts"
-       << " (NCrystal: \"Rejection method failed to sample kinematically valid (alpha,beta) point\"), the"
-       << " (alpha,beta) -> mu conversion met E*E'=0, or a free-gas sampling (E >= Emax of a scattering"
-       << " kernel, or a FreeGas component) was requested, which this GPU path does not provide yet.";
+       << " (NCrystal: \"Rejection method failed to sample kinematically valid (alpha,beta) point\"), or the"
+       << " (alpha,beta) -> mu conversion met E*E'=0 (NCrystal: \"convertAlphaBetaToDeltaEMu invalid for"
+       << " beta=-E/kT\").";
     throw TypedError( "CalcError", ss.str() );
   }
 
@@ -1423,29 +1423,45 @@ void ncgb_batch_xs_scatter_many( ncgb_batch_t bt, const double* ekin, const int6
     checkSize( n, 1 );
     if ( n == 0 )
       return;
+    // Chunked H2D / kernels / D2H over two streams, as xsScatterHost: chunk k
+    // is a launch over neutrons [off, off+m) of the whole batch (the kernels
+    // locate materials and random streams from the global index off + o); one
+    // call sequence number for the whole call.
     Scratch& s = scratchFor( *bo.mats.front() );
-    ensure( s.d_in, s.cap_in, n * sizeof(double) );
-    ensure( s.d_a, s.cap_a, n * sizeof(double) );
-    ensure( s.d_b, s.cap_b, n * sizeof(double) );
-    ensure( s.d_c, s.cap_c, std::max<std::size_t>( n * sizeof(double), ( bo.nmat + 1 ) * sizeof(int64_t) ) );
-    void* d_off = nullptr;
-    std::size_t offbytes = ( bo.nmat + 1 ) * sizeof(int64_t);
-    // offsets live at the end of the 'c' buffer (after the mu outputs)
-    ensure( s.d_c, s.cap_c, n * sizeof(double) + offbytes + 256 );
-    d_off = static_cast<char*>( s.d_c ) + ( ( n * sizeof(double) + 255 ) & ~std::size_t(255) );
+    const uint64_t chunk = std::min<uint64_t>( n, uint64_t(1) << 22 );
+    const std::size_t offbytes = ( bo.nmat + 1 ) * sizeof(int64_t);
+    ensure( s.d_in, s.cap_in, 2 * chunk * sizeof(double) + offbytes + 256 );
+    ensure( s.d_a, s.cap_a, 2 * chunk * sizeof(double) );
+    ensure( s.d_b, s.cap_b, 2 * chunk * sizeof(double) );
+    ensure( s.d_c, s.cap_c, 2 * chunk * sizeof(double) );
+    ensure( s.d_queue, s.cap_queue, chunk * sizeof(ncgb::QEntry) );
+    int64_t* d_off = reinterpret_cast<int64_t*>( static_cast<char*>( s.d_in ) + 2 * chunk * sizeof(double) );
+    const uint32_t call = bo.callseq.fetch_add( 1, std::memory_order_relaxed );
+    cudaStream_t st[2] = { s.stream, s.stream2 };
     resetNFail( s, s.stream );
-    checkCuda( cudaMemcpyAsync( s.d_in, ekin, n * sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
     checkCuda( cudaMemcpyAsync( d_off, offsets, offbytes, cudaMemcpyHostToDevice, s.stream ), "H2D" );
-    ncgb::Batch b = multiBatch( bo, s, static_cast<const double*>( s.d_in ), n,
-                                xs ? static_cast<double*>( s.d_a ) : nullptr,
-                                ef ? static_cast<double*>( s.d_b ) : nullptr,
-                                mu ? static_cast<double*>( s.d_c ) : nullptr, nullptr );
-    checkCuda( ncgb::launchScatterMulti( bo.d_slots, static_cast<const int64_t*>( d_off ), bo.nmat, b, bo.cfg,
-                                         s.stream ), "batch kernels" );
-    if ( xs ) checkCuda( cudaMemcpyAsync( xs, s.d_a, n * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
-    if ( ef ) checkCuda( cudaMemcpyAsync( ef, s.d_b, n * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
-    if ( mu ) checkCuda( cudaMemcpyAsync( mu, s.d_c, n * sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
     checkCuda( cudaEventRecord( s.done, s.stream ), "cudaEventRecord" );
+    uint64_t k = 0;
+    for ( uint64_t off = 0; off < n; off += chunk, ++k ) {
+      const uint64_t m = std::min<uint64_t>( chunk, n - off );
+      const int h = static_cast<int>( k & 1 );
+      cudaStream_t cs = st[h];
+      double* din = static_cast<double*>( s.d_in ) + h * chunk;
+      double* da = static_cast<double*>( s.d_a ) + h * chunk;
+      double* db = static_cast<double*>( s.d_b ) + h * chunk;
+      double* dc = static_cast<double*>( s.d_c ) + h * chunk;
+      checkCuda( cudaMemcpyAsync( din, ekin + off, m * sizeof(double), cudaMemcpyHostToDevice, cs ), "H2D" );
+      ncgb::Batch b = multiBatch( bo, s, din, m, xs ? da : nullptr, ef ? db : nullptr, mu ? dc : nullptr, nullptr );
+      b.callseq = call;
+      b.index_offset = static_cast<uint32_t>( off );
+      checkCuda( cudaStreamWaitEvent( cs, s.done, 0 ), "cudaStreamWaitEvent" );
+      checkCuda( ncgb::launchScatterMulti( bo.d_slots, d_off, bo.nmat, b, bo.cfg, cs ), "batch kernels" );
+      checkCuda( cudaEventRecord( s.done, cs ), "cudaEventRecord" );
+      if ( xs ) checkCuda( cudaMemcpyAsync( xs + off, da, m * sizeof(double), cudaMemcpyDeviceToHost, cs ), "D2H" );
+      if ( ef ) checkCuda( cudaMemcpyAsync( ef + off, db, m * sizeof(double), cudaMemcpyDeviceToHost, cs ), "D2H" );
+      if ( mu ) checkCuda( cudaMemcpyAsync( mu + off, dc, m * sizeof(double), cudaMemcpyDeviceToHost, cs ), "D2H" );
+    }
+    checkCuda( cudaStreamSynchronize( s.stream2 ), "batch kernels" );
     const unsigned long bad = readNFail( s, s.stream );
     if ( bad )
       throwSamplingFailure( bad );

@@ -51,20 +51,22 @@ namespace {
     const ncgb::MatSlot* slots;
     const int64_t* offsets;   // [nmat+1]
     int nmat;
+    int64_t base;             // global index of this launch's first neutron (chunked host calls)
     __device__ __forceinline__ int find( uint64_t o ) const
     {
-      // last k with offsets[k] <= o
+      // last k with offsets[k] <= base + o
+      const int64_t g = base + (int64_t)o;
       int lo = 0, hi = nmat - 1;
       while ( lo < hi ) {
         const int mid = ( lo + hi + 1 ) >> 1;
-        if ( __ldg( offsets + mid ) <= (int64_t)o ) lo = mid; else hi = mid - 1;
+        if ( __ldg( offsets + mid ) <= g ) lo = mid; else hi = mid - 1;
       }
       return lo;
     }
     __device__ __forceinline__ const ncgb_material_view& mat( int k ) const { return slots[k].view; }
     __device__ __forceinline__ void rngFor( ncgb_rng& r, int k, uint64_t o, uint32_t callseq ) const
     {
-      const uint64_t local = o - (uint64_t)__ldg( offsets + k );
+      const uint64_t local = (uint64_t)base + o - (uint64_t)__ldg( offsets + k );
       ncgb_rng_init( &r, slots[k].seed, (uint32_t)local, callseq, slots[k].stream );
     }
   };
@@ -469,6 +471,7 @@ namespace ncgb {
     src.slots = d_slots;
     src.offsets = d_offsets;
     src.nmat = nmat;
+    src.base = (int64_t)b.index_offset;
     return launchBoth( src, b, cfg, s );
   }
 

@@ -42,7 +42,8 @@ namespace ncgb {
   };
 
   // One batch: neutron o (< n_out) has energy ekin[o % n_ekin] and draws
-  // from stream (seed, o + index_offset, callseq, stream).
+  // from stream (seed, o + index_offset, callseq, stream); in multi-material
+  // launches index_offset is the global index of the launch's first neutron.
   struct Batch {
     const void* ekin;
     int in_f32;

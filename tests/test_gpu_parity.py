@@ -254,3 +254,27 @@ def test_fused_absorption_equals_separate_calls():
     np.testing.assert_array_equal(xs.cpu().numpy(), sxs)
     np.testing.assert_array_equal(ef.cpu().numpy(), sef)
     np.testing.assert_array_equal(mu.cpu().numpy(), smu)
+
+
+def test_batch_host_call_in_chunks_matches_one_launch():
+    """The batch host call runs chunks of 2^22 neutrons on two streams; a
+    material straddling chunk boundaries keeps its random streams: the host
+    call equals one device launch of a fresh batch (same call number)."""
+    import torch
+    cfgs = [W.PE293, W.AL2O3, W.AL]
+    for c in cfgs:
+        bundle_path(c)
+    counts = [3000000, 2500000, 100]
+    e = np.concatenate([W.loguniform_energies(n, 1e-4, 1.0, 90 + k) for k, n in enumerate(counts)])
+    off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    dev = NC.Batch([NC.createScatter(c, seed=40 + k) for k, c in enumerate(cfgs)])
+    te = torch.as_tensor(e, device="cuda")
+    toff = torch.as_tensor(off, device="cuda")
+    xs, ef, mu = (torch.empty_like(te) for _ in range(3))
+    dev.scatter_device(te, toff, xs, ef, mu)
+    torch.cuda.synchronize()
+    host = NC.Batch([NC.createScatter(c, seed=40 + k) for k, c in enumerate(cfgs)])
+    hxs, hef, hmu = host.xs_scatter_host(e, off)
+    np.testing.assert_array_equal(hxs, xs.cpu().numpy())
+    np.testing.assert_array_equal(hef, ef.cpu().numpy())
+    np.testing.assert_array_equal(hmu, mu.cpu().numpy())
