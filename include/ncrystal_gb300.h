@@ -359,6 +359,32 @@ int ncgb_phase_times( double* ms_pick, double* ms_sab, unsigned long* nbatches, 
 /* Bytes of device memory holding a handle's material tables. */
 unsigned long ncgb_device_bytes( ncrystal_scatter_t );
 
+/* ===================== Part 4: MiniMC on the device ==========================
+ *
+ * The reference's MiniMC (src/minimc: standard engine with forced collisions
+ * and roulette, sphere/box/slab/cylinder geometries, constant/circular/
+ * isotropic sources, standard histogram tallies) with the neutron population
+ * resident in device memory and every collision done by this library's
+ * scatter kernels.  Results are the reference's JSON document
+ * (NCrystalMiniMCResults_v1), statistically equivalent (the random streams
+ * differ); output.metadata.device adds the step count and device time. */
+
+/* Replaces ncrystal_jsonquery (ncrystal.h:1244-1253, ncrystal.cc:2463-2473)
+ * for the MiniMC queries, entries separated by the BEL character (0x07):
+ *   ["mmc","run",CFGSTR,GEOMCFG,SRCCFG,ENGINECFG]
+ *   ["mmc","run",CFGSTR,SCENARIO,ENGINECFG]
+ *   ["mmc","scenario",CFGSTR,SCENARIO]
+ *   ["mmc","inspectcfg","geom"|"src"|"engine",CFG]
+ * (NCMMC_Query.cc:60-157).  Other queries are refused (BadInput).  Returns a
+ * string to free with ncrystal_dealloc_string, or NULL on error. */
+char* ncrystal_jsonquery( const char* query );
+/* ncrystal.h:1219 */
+void ncrystal_dealloc_string( char* );
+/* The same run for an existing scatter handle (its mode, sampler and random
+ * stream are used for the collisions; the material's absorption per the
+ * engine's absorption option).  enginecfg may be NULL. */
+char* ncgb_mmc_run( ncrystal_scatter_t, const char* geomcfg, const char* srccfg, const char* enginecfg );
+
 #ifdef __cplusplus
 }
 #endif

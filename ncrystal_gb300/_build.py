@@ -76,8 +76,9 @@ def build_library(force=False, verbose=False):
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(BUILD, exist_ok=True)
-    cu = ["ncgb_kernels.cu", "ncgb_noalloc.cu", "ncgb_mlp.cu"]
-    cc = ["ncgb_capi.cc", "ncgb_tables.cc", "ncgb_bundle.cc", "ncgb_hostapi.cc", "ncgb_proposal.cc"]
+    cu = ["ncgb_kernels.cu", "ncgb_noalloc.cu", "ncgb_mlp.cu", "ncgb_mmc.cu"]
+    cc = ["ncgb_capi.cc", "ncgb_tables.cc", "ncgb_bundle.cc", "ncgb_hostapi.cc", "ncgb_proposal.cc",
+          "ncgb_mmc.cc"]
     hdrs = _headers()
     jobs = []
     objs = []

@@ -277,6 +277,26 @@ int main( int argc, char** argv )
     b.f64("elow", dom.elow.dbl());
     b.f64("ehigh", dom.ehigh.dbl());
     b.f64("temperature", cfg.get_temp().dbl());
+    // material information used by the MiniMC engine: number density
+    // (macroXSFactor, NCMMC_Utils.hh:103-105), temperature if well defined, and
+    // the Bragg threshold as the scenario decoder takes it (the largest over
+    // the phases, NCMMC_Utils.cc:218-241); -1 where absent
+    {
+      auto info = NC::createInfo(cfg);
+      b.f64("info.numdens", info->getNumberDensity().dbl());
+      b.f64("info.temperature", info->hasTemperature() ? info->getTemperature().dbl() : -1.0);
+      NC::Optional<NC::NeutronWavelength> bt;
+      if ( info->isSinglePhase() ) {
+        bt = info->getBraggThreshold();
+      } else {
+        for ( auto& ph : info->getPhases() ) {
+          auto pbt = ph.second->getBraggThreshold();
+          if ( pbt.has_value() && ( !bt.has_value() || bt.value() < pbt.value() ) )
+            bt = pbt;
+        }
+      }
+      b.f64("info.bragg_threshold", bt.has_value() ? bt.value().dbl() : -1.0);
+    }
     int nc = 0;
     if ( auto pc = dynamic_cast<const NC::ProcImpl::ProcComposition*>(&top) ) {
       for ( auto& c : pc->components() )

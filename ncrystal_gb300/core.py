@@ -155,6 +155,9 @@ def lib():
         "ncgb_phase_timing": (None, [_C.c_int]),
         "ncgb_phase_times": (_C.c_int, [_dblp, _dblp, _C.POINTER(_C.c_ulong), _C.POINTER(_C.c_ulong)]),
         "ncgb_device_bytes": (_C.c_ulong, [H]),
+        "ncrystal_jsonquery": (_C.c_void_p, [_C.c_char_p]),
+        "ncrystal_dealloc_string": (None, [_C.c_void_p]),
+        "ncgb_mmc_run": (_C.c_void_p, [H, _C.c_char_p, _C.c_char_p, _C.c_char_p]),
         "ncgb_tables_load": (_C.c_void_p, [_C.c_char_p]),
         "ncgb_tables_lasterror": (_C.c_char_p, []),
         "ncgb_tables_view": (_C.c_int, [_C.c_void_p, _C.c_void_p]),
@@ -421,6 +424,14 @@ class Scatter(Process):
                                          ekin_final.data_ptr(), direction_final.data_ptr(),
                                          0 if status is None else status.data_ptr(), stream.cuda_stream):
             _check()
+
+    def minimc_run(self, geomcfg, srccfg, enginecfg=None):
+        """MiniMC on the device with this handle's material, mode, sampler
+        and random stream (ncgb_mmc_run); returns the results dictionary."""
+        from .minimc import _take_json
+        raw = lib().ncgb_mmc_run(self._h, geomcfg.encode(), srccfg.encode(),
+                                 None if enginecfg is None else enginecfg.encode())
+        return _take_json(raw)
 
     def genScatterNonOriented(self, ekin, repeat=None):
         """Obsolete NCrystal call: returns (angle, delta_ekin) arrays."""

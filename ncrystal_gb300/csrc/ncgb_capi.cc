@@ -10,6 +10,7 @@
 // no CPU evaluation path in this library.
 #include "ncgb_host.hh"
 #include "ncgb_launch.hh"
+#include "ncgb_mmc.hh"
 #include "ncgb_mlp.hh"
 #include "ncgb_proposal.hh"
 #include "ncrystal_gb300.h"
@@ -1158,6 +1159,23 @@ namespace ncgb {
     *seed = o.seed;
     *streamidx = o.streamidx;
     *callseq = nextCall( o );
+  }
+
+  // What the MiniMC engine needs of a scatter handle.
+  void handleInfo( ncrystal_scatter_t sc, const char* fct, mmc::HandleInfo* out )
+  {
+    ScatterObj& o = extract( sc.internal, fct );
+    out->view = o.mat->view;
+    out->device = o.mat->device;
+    out->mode = o.mode;
+    out->sampler = o.sampler;
+    out->seed = o.seed;
+    out->streamidx = o.streamidx;
+    out->numdens = o.mat->tables->m_numdens;
+    out->temperature = o.mat->tables->m_info_temperature;
+    out->bragg_threshold = o.mat->tables->m_bragg_threshold;
+    out->abs_c = o.mat->view.abs_c;
+    out->cfg = o.cfg;
   }
 
   // Routes an exception into the C interface's error state.

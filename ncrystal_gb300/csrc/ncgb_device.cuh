@@ -516,7 +516,7 @@ namespace ncgb_dev {
   // rejection loop is unbounded; its acceptance is above 98% here, and the
   // cap only guards the GPU.
   // FP32 version of elincMuMono (mixed-precision mode).
-  __device__ __noinline__ float elincMuMonoF( ncgb_rng& rng, float ekin, float msd, int& status )
+  static __device__ __noinline__ float elincMuMonoF( ncgb_rng& rng, float ekin, float msd, int& status )
   {
     const float a = ( (float)kElIncMu * ekin ) * msd;
     if ( a < 0.01f ) {
@@ -565,7 +565,7 @@ namespace ncgb_dev {
   // ElIncXS::EPointAnalysis::sampleMu, NCElIncXS.cc:178-191 (element picked
   // by pickRandIdxByWeight on the cumulative contributions).
   // FP32 version of elincMu (mixed-precision mode).
-  __device__ __noinline__ double elincMuF( const ncgb_elinc_view& v, ncgb_rng& rng, double ekin, int& status )
+  static __device__ __noinline__ double elincMuF( const ncgb_elinc_view& v, ncgb_rng& rng, double ekin, int& status )
   {
     const float ef = (float)ekin;
     if ( v.n == 1 )

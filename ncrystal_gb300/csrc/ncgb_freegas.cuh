@@ -77,7 +77,7 @@ namespace ncgb_dev {
   }
 
   // randExpDivSqrt, NCRandUtils.cc:224-330: exp(-c*x)/sqrt(x) on [a,b]
-  __device__ __noinline__ double fgRandExpDivSqrt( ncgb_rng& rng, double c, double a, double b, int& st )
+  static __device__ __noinline__ double fgRandExpDivSqrt( ncgb_rng& rng, double c, double a, double b, int& st )
   {
     const double A = c*a;
     if ( A > 0.1 ) {
@@ -130,7 +130,7 @@ namespace ncgb_dev {
     return exparg < -745.1 ? 0.0 : exp( exparg ) * sqrt( xmax/x );
   }
 
-  __device__ __noinline__ double fgRandEMix( ncgb_rng& rng, double c, double xm, double xp, int& st )
+  static __device__ __noinline__ double fgRandEMix( ncgb_rng& rng, double c, double xm, double xp, int& st )
   {
     if ( xp == xm )
       return xm;
@@ -306,7 +306,7 @@ namespace ncgb_dev {
   }
 
   // FreeGasSampler::sampleBeta, NCFreeGasUtils.cc:530-849
-  __device__ __noinline__ double fgSampleBeta( const FGSampler& s, const double* tab, ncgb_rng& rng, int& st )
+  static __device__ __noinline__ double fgSampleBeta( const FGSampler& s, const double* tab, ncgb_rng& rng, int& st )
   {
     if ( s.c_real > 1e4 ) {
       const double A = 1.0 / s.invA;
@@ -435,7 +435,7 @@ namespace ncgb_dev {
   }
 
   // FreeGasSampler::sampleAlpha, NCFreeGasUtils.cc:851-932
-  __device__ __noinline__ double fgSampleAlpha( const FGSampler& s, double beta, ncgb_rng& rng, int& st )
+  static __device__ __noinline__ double fgSampleAlpha( const FGSampler& s, double beta, ncgb_rng& rng, int& st )
   {
     if ( s.c_real < s.c || beta <= s.c * ( -1.0 + 1e-14 ) ) {
       const ALim al = alphaLimits( s.c_real, beta );
@@ -491,7 +491,7 @@ namespace ncgb_dev {
 
   // FreeGas::sampleScatterIsotropic (NCFreeGas.cc:70-75) via
   // FreeGasSampler::sampleDeltaEMu (NCFreeGasUtils.hh:146-161).
-  __device__ __noinline__ int freeGasScatter( const ncgb_freegas_view& v, const double* tab, ncgb_rng& rng,
+  static __device__ __noinline__ int freeGasScatter( const ncgb_freegas_view& v, const double* tab, ncgb_rng& rng,
                                               double ekin, double& ef, double& mu )
   {
     FGSampler s;
@@ -520,7 +520,7 @@ namespace ncgb_dev {
   // SABSampler::sampleHighE, NCSABSampler.cc:59-156.  Returns 1 with (alpha,
   // beta) from the extender, 0 if the table must be sampled at E = Emax, or a
   // negative value on failure (-1: the reference's BadInput, -2: loop cap).
-  __device__ __noinline__ int sabHighE( const ncgb_sab_view& s, const double* tab, double ekin, ncgb_rng& rng,
+  static __device__ __noinline__ int sabHighE( const ncgb_sab_view& s, const double* tab, double ekin, ncgb_rng& rng,
                                         double& alpha, double& beta )
   {
     const double emax = ldg( s.egrid + s.ne - 1 );

@@ -61,6 +61,11 @@ namespace ncgb {
     std::vector<char> m_arena;
     std::string m_cfg;
     double m_temperature = -1.0;
+    // material information (Info): atoms per Aa^3, temperature in K and Bragg
+    // threshold in Aa; -1 where the material has none or the bundle lacks it
+    double m_numdens = -1.0;
+    double m_info_temperature = -1.0;
+    double m_bragg_threshold = -1.0;
   };
 
   // SAB table derivation (restated reference algorithms), used by build():

@@ -47,6 +47,22 @@ namespace {
     }
   };
 
+  // One material; neutron o's stream index read from a per-neutron array
+  // (callers whose neutrons keep their streams while they move between
+  // batches, such as the MiniMC engine).
+  struct MappedSrc {
+    ncgb_material_view m;
+    uint64_t seed;
+    uint32_t stream, pad;
+    const uint32_t* index;
+    __device__ __forceinline__ int find( uint64_t ) const { return 0; }
+    __device__ __forceinline__ const ncgb_material_view& mat( int ) const { return m; }
+    __device__ __forceinline__ void rngFor( ncgb_rng& r, int, uint64_t o, uint32_t callseq ) const
+    {
+      ncgb_rng_init( &r, seed, __ldg( index + o ), callseq, stream );
+    }
+  };
+
   struct MultiSrc {
     const ncgb::MatSlot* slots;
     const int64_t* offsets;   // [nmat+1]
@@ -356,7 +372,8 @@ namespace {
   {
     static int bps = 0;
     if ( !bps ) {
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_sab<Src, false, false, false>, 256, 0 );
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_sab<Src, false, false, std::is_same<Src, MappedSrc>::value>,
+                                                     256, 0 );
       if ( bps <= 0 ) bps = 1;
     }
     return bps;
@@ -420,13 +437,18 @@ namespace {
       cudaEventRecord( ev.a, s );
     }
     const int pb = ( cfg.pick_block == 128 || cfg.pick_block == 512 ) ? cfg.pick_block : 256;
+    constexpr bool kMulti = std::is_same<Src, MultiSrc>::value;
+    constexpr bool kMapped = std::is_same<Src, MappedSrc>::value;
     if ( b.dir_out ) {
-      if constexpr ( std::is_same<Src, SingleSrc>::value )
+      if constexpr ( !kMulti )
         launchPick<Src, true>( src, b, pb, s );
       else
         return cudaErrorInvalidValue;   // directions: single-material calls only
     } else {
-      launchPick<Src, false>( src, b, pb, s );
+      if constexpr ( !kMapped )
+        launchPick<Src, false>( src, b, pb, s );
+      else
+        return cudaErrorInvalidValue;   // stream index arrays: with directions only
     }
     e = cudaGetLastError();
     if ( e != cudaSuccess )
@@ -437,10 +459,11 @@ namespace {
     const int mult = ( cfg.sab_blocks_per_sm > 0 && cfg.sab_blocks_per_sm < maxb ) ? cfg.sab_blocks_per_sm : maxb;
     const int grid = numSMs() * mult;
     if ( b.dir_out ) {
-      if constexpr ( std::is_same<Src, SingleSrc>::value )
+      if constexpr ( !kMulti )
         launchSab<Src, true>( src, b, grid, s );
     } else {
-      launchSab<Src, false>( src, b, grid, s );
+      if constexpr ( !kMapped )
+        launchSab<Src, false>( src, b, grid, s );
     }
     e = cudaGetLastError();
     if ( timing ) {
@@ -456,6 +479,15 @@ namespace ncgb {
 
   cudaError_t launchScatter( const ncgb_material_view& m, const Batch& b, cudaStream_t s )
   {
+    if ( b.rng_index ) {
+      MappedSrc src;
+      src.m = m;
+      src.seed = b.seed;
+      src.stream = b.stream;
+      src.pad = 0;
+      src.index = b.rng_index;
+      return launchBoth( src, b, LaunchCfg(), s );
+    }
     SingleSrc src;
     src.m = m;
     src.seed = b.seed;

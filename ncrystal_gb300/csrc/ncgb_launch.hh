@@ -62,6 +62,8 @@ namespace ncgb {
     const double* dir_in;  // [n_ekin][3] incoming directions (sampleScatter with directions), or null
     double* dir_out;       // [n_out][3] outgoing directions, or null
     int32_t* status;   // may be null
+    const uint32_t* rng_index;   // if set (with directions only): neutron o draws from stream
+                                 // (seed, rng_index[o], callseq, stream) instead
     Work* work;        // scratch, sizeof(Work)
     QEntry* queue;     // scratch, n_out entries
   };

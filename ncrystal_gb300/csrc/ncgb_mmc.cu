@@ -1,0 +1,589 @@
+// Device kernels of the MiniMC engine: source emission and the transport
+// step (forced collision, roulette, tallies).  The collisions themselves are
+// the library's scatter kernels (ncgb_kernels.cu), launched by the host
+// engine (ncgb_mmc.cc) between two transport steps.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "ncgb_device.cuh"
+#include "ncgb_mmc.hh"
+
+namespace {
+
+  using namespace ncgb_dev;
+  using namespace ncgb::mmc;
+
+  constexpr double kPi = 3.14159265358979323846;
+  constexpr double kToDeg = 57.2957795130823208767981548141051703324054725;   // 180/pi (NCDefs.hh:124)
+  constexpr double kWl2Ekin = 0.081804209605330899;                            // E[eV] = kWl2Ekin / wl[Aa]^2
+  constexpr double kEkin2Ksq = 4.0 * kPi * kPi / kWl2Ekin;                     // ekin2ksq(1.0) (NCDefs.hh:872)
+  constexpr double kDblMax = 1.7976931348623157e308;
+
+  // ---- geometry ----------------------------------------------------------------
+
+  __device__ __forceinline__ double slabExit( double x, double ux, double d )
+  {
+    // NCMMC_Utils.cc:516-537
+    if ( ux > 0.0 )
+      return ( d - x ) / ux;
+    if ( ux < 0.0 )
+      return -( d + x ) / ux;
+    return infd();
+  }
+
+  // Distance to the volume's surface from a point inside it
+  // (distToVolumeExit of NCMMC_Sphere.hh:170-216, NCMMC_Box.hh:213-226,
+  // NCMMC_Slab.hh, NCMMC_Cyl.hh); may be infinite for unbounded volumes.
+  __device__ double distExit( const Geom& g, const double* p, const double* u )
+  {
+    switch ( g.kind ) {
+      case GEOM_SPHERE: {
+        const double c = g.r * g.r - ( p[0] * p[0] + p[1] * p[1] + p[2] * p[2] );
+        const double pd = p[0] * u[0] + p[1] * u[1] + p[2] * u[2];
+        return maxd( 0.0, sqrt( maxd( 0.0, c + pd * pd ) ) - pd );
+      }
+      case GEOM_BOX:
+        return fmin( slabExit( p[0], u[0], g.dx ), fmin( slabExit( p[1], u[1], g.dy ), slabExit( p[2], u[2], g.dz ) ) );
+      case GEOM_SLAB:
+        return slabExit( p[2], u[2], g.dz );
+      default: {
+        // cylinder around y: radial exit (larger root), then the end caps
+        const double a = u[0] * u[0] + u[2] * u[2];
+        double t = infd();
+        if ( a > 0.0 ) {
+          const double b = p[0] * u[0] + p[2] * u[2];
+          const double c = p[0] * p[0] + p[2] * p[2] - g.r * g.r;
+          t = maxd( 0.0, ( -b + sqrt( maxd( 0.0, b * b - a * c ) ) ) / a );
+        }
+        if ( g.dy > 0.0 )
+          t = fmin( t, slabExit( p[1], u[1], g.dy ) );
+        return t;
+      }
+    }
+  }
+
+  // Intersection of the ray with the slab |x| <= d as a parameter interval.
+  __device__ __forceinline__ bool slabInterval( double x, double ux, double d, double& t1, double& t2 )
+  {
+    if ( ux != 0.0 ) {
+      const double inv = 1.0 / ux;
+      const double a = ( d - x ) * inv, b = ( -d - x ) * inv;
+      t1 = fmax( t1, fmin( a, b ) );
+      t2 = fmin( t2, fmax( a, b ) );
+      return true;
+    }
+    return fabs( x ) <= d;
+  }
+
+  // Distance along the ray to the volume (distToVolumeEntry): 0 inside (or on
+  // the surface pointing in), -1 when the ray misses it (NCMMC_Sphere.hh:
+  // 110-160, NCMMC_Box.hh:112-205, NCMMC_Utils.cc:539-590).
+  __device__ double distEntry( const Geom& g, const double* p, const double* u )
+  {
+    if ( g.kind == GEOM_SPHERE ) {
+      const double pd = p[0] * u[0] + p[1] * u[1] + p[2] * u[2];
+      const double c = p[0] * p[0] + p[1] * p[1] + p[2] * p[2] - g.r * g.r;
+      if ( c <= 0.0 )
+        return fmin( c, pd ) < 0.0 ? 0.0 : -1.0;
+      const double D = pd * pd - c;
+      if ( D < 0.0 )
+        return -1.0;
+      const double t = -( sqrt( D ) + pd );
+      return t >= 0.0 ? t : -1.0;
+    }
+    if ( g.kind == GEOM_SLAB ) {
+      const double a = fabs( p[2] ) - g.dz;
+      const double xu = p[2] * u[2];
+      if ( a <= 0.0 )
+        return ( a != 0.0 || !( xu > 0.0 ) ) ? 0.0 : -1.0;
+      return xu >= 0.0 ? -1.0 : a / fabs( u[2] );
+    }
+    double t1 = -infd(), t2 = infd();
+    bool hit;
+    if ( g.kind == GEOM_BOX ) {
+      hit = slabInterval( p[0], u[0], g.dx, t1, t2 ) && slabInterval( p[1], u[1], g.dy, t1, t2 )
+            && slabInterval( p[2], u[2], g.dz, t1, t2 );
+    } else {
+      // cylinder: radial interval, then the caps
+      const double a = u[0] * u[0] + u[2] * u[2];
+      const double b = p[0] * u[0] + p[2] * u[2];
+      const double c = p[0] * p[0] + p[2] * p[2] - g.r * g.r;
+      if ( a > 0.0 ) {
+        const double D = b * b - a * c;
+        hit = D >= 0.0;
+        if ( hit ) {
+          const double sd = sqrt( D );
+          t1 = ( -b - sd ) / a;
+          t2 = ( -b + sd ) / a;
+        }
+      } else {
+        hit = c <= 0.0;
+      }
+      if ( hit && g.dy > 0.0 )
+        hit = slabInterval( p[1], u[1], g.dy, t1, t2 );
+    }
+    if ( !hit || t1 >= t2 || t2 <= 0.0 )
+      return -1.0;
+    return maxd( 0.0, t1 );
+  }
+
+  // ---- random numbers ------------------------------------------------------------
+
+  // Standard normal deviate (Box-Muller on two uniforms in (0,1]).
+  __device__ __forceinline__ double randNormal( ncgb_rng& rng )
+  {
+    const double u1 = rand01( rng ), u2 = rand01( rng );
+    return sqrt( -2.0 * log( u1 ) ) * cospi( 2.0 * u2 );
+  }
+
+  // randIsotropicDirection (NCRandUtils.cc:25-50, Marsaglia 1972) with the
+  // reference's roundings (no contraction), so that |u|^2 - 1 is distributed
+  // the same way: tallies of unscattered neutrons put mu = u.u0 at the edge
+  // of the last bin.  The rejection loop is capped (acceptance pi/4).
+  __device__ void randIsotropic( ncgb_rng& rng, double* u )
+  {
+    double x0 = 0.0, x1 = 0.0, s = 0.0;
+    for ( int it = 0; it < 1000; ++it ) {
+      x0 = __dsub_rn( 2.0 * rand01( rng ), 1.0 );
+      x1 = __dsub_rn( 2.0 * rand01( rng ), 1.0 );
+      s = __dadd_rn( __dmul_rn( x0, x0 ), __dmul_rn( x1, x1 ) );
+      if ( s < 1.0 )
+        break;
+    }
+    if ( !( s < 1.0 ) ) { x0 = 0.0; x1 = 0.0; s = 0.0; }
+    const double t = 2.0 * sqrt( __dsub_rn( 1.0, s ) );
+    u[0] = __dmul_rn( x0, t );
+    u[1] = __dmul_rn( x1, t );
+    u[2] = __dsub_rn( 1.0, 2.0 * s );
+  }
+
+  __device__ __forceinline__ double wl2ekin( double wl )
+  {
+    // convertBufWl2E, NCMMC_Source.cc:98-112
+    const double wl2 = wl * wl;
+    return kWl2Ekin / maxd( 4.9406564584124654e-324, wl2 );
+  }
+
+  // setEnergy (NCMMC_Source.cc:115-375)
+  __device__ double sourceEnergy( const Source& s, ncgb_rng& rng )
+  {
+    switch ( s.ekind ) {
+      case E_FIXED:
+        return s.ea;
+      case E_UNIFORM: {
+        const double v = fmin( s.eb, s.ea + rand01( rng ) * ( s.eb - s.ea ) );
+        return s.e_is_wl ? wl2ekin( v ) : v;
+      }
+      case E_LOGNORMAL: {
+        const double v = exp( s.ea + s.eb * randNormal( rng ) );
+        return s.e_is_wl ? wl2ekin( v ) : v;
+      }
+      default: {
+        const double n1 = randNormal( rng ), n2 = randNormal( rng ), n3 = randNormal( rng );
+        return s.ea * ( n1 * n1 + n2 * n2 + n3 * n3 );
+      }
+    }
+  }
+
+  // ---- tallies -----------------------------------------------------------------
+
+  __device__ __forceinline__ long long orderKey( double x )
+  {
+    long long k = __double_as_longlong( x );
+    return k < 0 ? ( k ^ 0x7FFFFFFFFFFFFFFFLL ) : k;
+  }
+
+  // Hist1D::fill (NCHists.hh:303-345, :376-400; RunningStats1D :613-650) into
+  // group g of histogram h.
+  __device__ __forceinline__ void histFill( double* buf, const TallyHist& h, int g, double x, double w, bool weighted )
+  {
+    if ( weighted && !( w > 0.0 ) )
+      return;
+    const double wt = weighted ? w : 1.0;
+    int bin;
+    if ( x < h.xmin )
+      bin = 0;
+    else if ( x >= h.xmax )
+      bin = ( x == h.xmax ) ? h.nbins : h.nbins + 1;
+    else {
+      const double f = h.inv_delta * ( x - h.xmin );
+      bin = 1 + ( f >= (double)h.nbins ? h.nbins : (int)f );
+    }
+    double* b = buf + h.off + ( (int64_t)g * ( h.nbins + 2 ) + bin ) * 2;
+    atomicAdd( b, wt );
+    atomicAdd( b + 1, wt * wt );
+    double* st = buf + h.soff + g * kStats;
+    atomicAdd( st, wt );
+    atomicAdd( st + 1, wt * x );
+    atomicAdd( st + 2, wt * x * x );
+    const long long k = orderKey( x );
+    atomicMin( reinterpret_cast<long long*>( st + 3 ), k );
+    atomicMax( reinterpret_cast<long long*>( st + 4 ), k );
+  }
+
+  __device__ __forceinline__ void histFill2( double* buf, const Tally& t, int kind, int cat, double x, double w,
+                                             bool weighted )
+  {
+    const TallyHist& h = t.h[kind];
+    histFill( buf, h, 0, x, w, weighted );
+    if ( t.breakdown )
+      histFill( buf, h, 1 + cat, x, w, weighted );
+  }
+
+  // tallyRecord (NCMMC_StdTallies.cc:430-660) for one neutron.
+  __device__ void tallyNeutron( double* buf, const Tally& t, double e, const double* u, double w, int nscat,
+                                int ninel, double e0, const double* d0 )
+  {
+    // init_dethistidvect, NCMMC_StdTallies.cc:288-308
+    const int cat = nscat > 1 ? ( ninel ? 4 : 3 ) : ( nscat == 1 ? ( ninel ? 2 : 1 ) : 0 );
+    if ( t.h[T_THETA].enabled | t.h[T_MU].enabled | t.h[T_Q].enabled ) {
+      // the reference's roundings (NCMMC_StdTallies.cc:530-560): unscattered
+      // neutrons sit at mu = 1 up to the last bits, on the last bin's edge
+      double mu;
+      if ( t.fixed_dir && t.d0z == 1.0 )
+        mu = u[2];
+      else if ( t.fixed_dir )
+        mu = __dadd_rn( __dadd_rn( __dmul_rn( t.d0x, u[0] ), __dmul_rn( t.d0y, u[1] ) ), __dmul_rn( t.d0z, u[2] ) );
+      else
+        mu = __dadd_rn( __dadd_rn( __dmul_rn( d0[0], u[0] ), __dmul_rn( d0[1], u[1] ) ), __dmul_rn( d0[2], u[2] ) );
+      mu = clampd( mu, -1.0, 1.0 );
+      if ( t.h[T_MU].enabled )
+        histFill2( buf, t, T_MU, cat, mu, w, true );
+      if ( t.h[T_Q].enabled ) {
+        const double ei = t.fixed_e ? t.e0 : e0;
+        const double q2 = __dmul_rn( __dadd_rn( __dadd_rn( __dmul_rn( __dmul_rn( sqrt( __dmul_rn( e, ei ) ), mu ), -2.0 ),
+                                                           ei ), e ), kEkin2Ksq );
+        histFill2( buf, t, T_Q, cat, sqrt( maxd( 0.0, q2 ) ), w, true );
+      }
+      if ( t.h[T_THETA].enabled )
+        histFill2( buf, t, T_THETA, cat, acos( mu ) * kToDeg, w, true );
+    }
+    if ( t.h[T_E].enabled )
+      histFill2( buf, t, T_E, cat, e, w, true );
+    if ( t.h[T_DE].enabled )
+      histFill2( buf, t, T_DE, cat, ( t.fixed_e ? t.e0 : e0 ) - e, w, true );
+    if ( t.h[T_L].enabled )
+      histFill2( buf, t, T_L, cat, sqrt( kWl2Ekin ) * sqrt( 1.0 / maxd( 4.9406564584124654e-324, e ) ), w, true );
+    if ( t.h[T_NSCAT].enabled )
+      histFill2( buf, t, T_NSCAT, cat, (double)nscat, w, true );
+    if ( t.h[T_NSCAT_UW].enabled )
+      histFill2( buf, t, T_NSCAT_UW, cat, (double)nscat, w, false );
+    if ( t.h[T_W].enabled )
+      histFill2( buf, t, T_W, cat, w, w, false );
+  }
+
+  // Block-local copy of the tally buffer in shared memory (when it fits):
+  // the min/max keys start at the empty values, the sums at zero.
+  __device__ void tallyInitShared( double* sh, const Tally& t )
+  {
+    for ( int64_t i = threadIdx.x; i < t.nbuf; i += blockDim.x )
+      sh[i] = 0.0;
+    __syncthreads();
+    for ( int k = 0; k < T_N; ++k ) {
+      if ( !t.h[k].enabled )
+        continue;
+      for ( int g = threadIdx.x; g < kGroups; g += blockDim.x ) {
+        long long* st = reinterpret_cast<long long*>( sh + t.h[k].soff + g * kStats );
+        st[3] = 0x7FFFFFFFFFFFFFFFLL;
+        st[4] = (long long)0x8000000000000000ULL;
+      }
+    }
+    __syncthreads();
+  }
+
+  __device__ void tallyFlushShared( const double* sh, const Tally& t )
+  {
+    __syncthreads();
+    for ( int k = 0; k < T_N; ++k ) {
+      if ( !t.h[k].enabled )
+        continue;
+      const TallyHist& h = t.h[k];
+      const int64_t nb = (int64_t)kGroups * ( h.nbins + 2 ) * 2;
+      for ( int64_t i = threadIdx.x; i < nb; i += blockDim.x ) {
+        const double v = sh[h.off + i];
+        if ( v != 0.0 )
+          atomicAdd( t.buf + h.off + i, v );
+      }
+      for ( int i = threadIdx.x; i < kGroups * kStats; i += blockDim.x ) {
+        const int j = i % kStats;
+        const double v = sh[h.soff + i];
+        if ( j < 3 ) {
+          if ( v != 0.0 )
+            atomicAdd( t.buf + h.soff + i, v );
+        } else {
+          const long long kv = __double_as_longlong( v );
+          long long* dst = reinterpret_cast<long long*>( t.buf + h.soff + i );
+          if ( j == 3 && kv != 0x7FFFFFFFFFFFFFFFLL )
+            atomicMin( dst, kv );
+          if ( j == 4 && kv != (long long)0x8000000000000000ULL )
+            atomicMax( dst, kv );
+        }
+      }
+    }
+  }
+
+  // Warp-aggregated append: slot of this lane among the lanes with 'want'.
+  __device__ __forceinline__ unsigned long long appendSlot( unsigned long long* counter, bool want )
+  {
+    const unsigned active = __activemask();
+    const unsigned mask = __ballot_sync( active, want );
+    unsigned long long base = 0;
+    const int lane = threadIdx.x & 31;
+    if ( mask ) {
+      const int leader = __ffs( mask ) - 1;
+      if ( lane == leader )
+        base = atomicAdd( counter, (unsigned long long)__popc( mask ) );
+      base = __shfl_sync( active, base, leader );
+    }
+    return base + __popc( mask & ( ( 1u << lane ) - 1u ) );
+  }
+
+  // Block sums of the tallied / missed counts, added to the counters once.
+  struct BlockSums {
+    unsigned long long n;
+    double w;
+  };
+
+  // ---- kernels --------------------------------------------------------------------
+
+  // Source neutrons first_id .. first_id+count-1: fillBasket of the source
+  // (NCMMC_Source.cc) and BasketSrcFiller::propagateToVolume
+  // (NCMMC_BasketSrcFiller.hh:120-178): neutrons that miss the volume are
+  // tallied with nscat = -1 (NCMMC_Baskets.cc:81) unless ignoremiss, and
+  // counted; the rest are moved onto the volume and appended to population a.
+  __global__ void __launch_bounds__(256)
+  k_mmc_emit( const Source src, const Geom g, const Engine eng, const Tally t, Pop a, uint64_t base,
+              uint64_t first_id, uint64_t count, Counters* c )
+  {
+    // (misses are few: they are tallied straight into global memory)
+    __shared__ BlockSums miss;
+    if ( threadIdx.x == 0 ) { miss.n = 0; miss.w = 0.0; }
+    __syncthreads();
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for ( uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride ) {
+      const uint64_t id = first_id + i;
+      ncgb_rng rng;
+      ncgb_rng_init( &rng, eng.seed, (uint32_t)id, 0u, kStreamSource );
+      double p[3] = { src.x, src.y, src.z };
+      double u[3] = { src.ux, src.uy, src.uz };
+      if ( src.kind == SRC_CIRCULAR && src.r > 0.0 ) {
+        // uniform point in the unit disk (polar form of randPointInUnitCircle)
+        const double rad = sqrt( rand01( rng ) ), phi = 2.0 * rand01( rng );
+        const double a0 = rad * cospi( phi ), b0 = rad * sinpi( phi );
+        p[0] += src.ax * a0 + src.bx * b0;
+        p[1] += src.ay * a0 + src.by * b0;
+        p[2] += src.az * a0 + src.bz * b0;
+      } else if ( src.kind == SRC_ISOTROPIC ) {
+        randIsotropic( rng, u );
+        if ( src.r != 0.0 ) {
+          p[0] -= u[0] * src.r;
+          p[1] -= u[1] * src.r;
+          p[2] -= u[2] * src.r;
+        }
+      }
+      const double e = sourceEnergy( src, rng );
+      bool keep = true;
+      if ( src.might_be_outside ) {
+        const double d = distEntry( g, p, u );
+        if ( d < 0.0 ) {
+          keep = false;
+          atomicAdd( &miss.n, 1ull );
+          atomicAdd( &miss.w, 1.0 );
+          if ( !eng.ignore_miss ) {
+            tallyNeutron( t.buf, t, e, u, 1.0, -1, 0, e, u );
+            atomicAdd( &c->tallied, 1ull );
+            atomicAdd( &c->tallied_w, 1.0 );
+          }
+        } else {
+          p[0] += d * u[0];
+          p[1] += d * u[1];
+          p[2] += d * u[2];
+        }
+      }
+      const unsigned long long slot = appendSlot( &c->n_a, keep );
+      if ( keep ) {
+        const uint64_t j = base + slot;
+        a.pos[3 * j] = p[0]; a.pos[3 * j + 1] = p[1]; a.pos[3 * j + 2] = p[2];
+        a.dir[3 * j] = u[0]; a.dir[3 * j + 1] = u[1]; a.dir[3 * j + 2] = u[2];
+        a.e[j] = e;
+        a.w[j] = 1.0;
+        a.xs[j] = -1.0;
+        a.nscat[j] = 0;
+        a.ninel[j] = 0;
+        a.id[j] = (uint32_t)id;
+        a.e0[j] = e;
+        a.d0[3 * j] = u[0]; a.d0[3 * j + 1] = u[1]; a.d0[3 * j + 2] = u[2];
+        a.st[j] = kNoScatter;
+      }
+    }
+    __syncthreads();
+    if ( threadIdx.x == 0 && miss.n ) {
+      atomicAdd( &c->miss, miss.n );
+      atomicAdd( &c->miss_w, miss.w );
+    }
+  }
+
+  // One engine step over population a (StdSimEngine::processBasket,
+  // NCMMC_SimEngine.cc:170-440).
+  template<bool Fast>
+  __global__ void __launch_bounds__(256)
+  k_mmc_transport( const __grid_constant__ ncgb_material_view m, const Geom g, const Engine eng, const Tally t,
+                   const Pop a, uint64_t n_a, const Pop b, uint32_t step, Counters* c, int smem )
+  {
+    extern __shared__ double sh[];
+    __shared__ BlockSums tal;
+    double* tb = smem ? sh : t.buf;
+    if ( smem )
+      tallyInitShared( sh, t );
+    if ( threadIdx.x == 0 ) { tal.n = 0; tal.w = 0.0; }
+    __syncthreads();
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for ( uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_a; i += stride ) {
+      double p[3] = { a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2] };
+      double u[3];
+      double e = a.e[i], w = a.w[i], xs = a.xs[i];
+      int nscat = a.nscat[i], ninel = a.ninel[i];
+      const int pst = a.st[i];
+      if ( pst == kNoScatter ) {
+        u[0] = a.dir[3 * i]; u[1] = a.dir[3 * i + 1]; u[2] = a.dir[3 * i + 2];
+      } else if ( pst == NCGB_ST_OK ) {
+        // the scatter of the previous step (NCMMC_SimEngine.cc:390-410)
+        const double en = a.e_new[i];
+        u[0] = a.dir_new[3 * i]; u[1] = a.dir_new[3 * i + 1]; u[2] = a.dir_new[3 * i + 2];
+        ++nscat;
+        if ( en != e ) {
+          ++ninel;
+          xs = -1.0;   // the cross-section might have changed
+        }
+        e = en;
+      } else {
+        // the reference aborts the run here; the host reports the failure
+        atomicAdd( &c->nfail, 1ull );
+        continue;
+      }
+      const double dexit = distExit( g, p, u );
+      const bool dinf = !finited( dexit );
+      // absorption (evalManyXSIsotropic of AbsOOV) and scattering (the
+      // cached value unless new or changed) macroscopic cross-sections
+      const double xabs = eng.has_abs ? eng.macro * absXS( eng.abs_c, e ) : 0.0;
+      if ( !eng.has_scat || eng.nscatlimit == 0 || ( eng.nscatlimit > 0 && nscat >= eng.nscatlimit ) ) {
+        xs = 0.0;
+      } else if ( nscat <= 0 || xs < 0.0 ) {
+        double x = 0.0;
+        if ( contains( m.dom_elow, m.dom_ehigh, e ) ) {
+          ncgb_rng dummy;
+          ncgb_rng_init( &dummy, 0, 0, 0, 0 );
+          x = xsAndPick<false, Fast>( m, e, dummy ).xs;
+        }
+        xs = eng.macro * x;
+      }
+      // calcProbTransm (NCMMC_Utils.cc:46-88): 0 for an infinite path
+      const double xsc = fmin( kDblMax, xs );
+      const double ptransm = ( g.unbounded && dinf ) ? 0.0 : ( xsc != 0.0 ? exp( -xsc * dexit ) : 1.0 );
+      // sampleRandDists (NCMMC_Utils.cc:153-176)
+      ncgb_rng rng;
+      ncgb_rng_init( &rng, eng.seed, a.id[i], step, kStreamEngine );
+      const double r = rand01( rng );
+      double ds;
+      if ( xs == 0.0 )
+        ds = infd();
+      else if ( dinf )
+        ds = log( r ) / ( -xs );
+      else
+        ds = ( -1.0 / xs ) * log( 1.0 + r * expm1( -xs * dexit ) );
+      // the part that scatters: roulette, attenuation, move to the point
+      bool keep = false;
+      double wk = 0.0;
+      if ( w != 0.0 && finited( ds ) && xs > 0.0 ) {
+        double rf = 1.0;
+        keep = true;
+        if ( nscat >= eng.nscatthr && w < eng.wthr ) {
+          if ( rand01( rng ) > eng.psurv )
+            keep = false;
+          else
+            rf = eng.boost;
+        }
+        if ( keep ) {
+          const double wr = exp( -xabs * ds );
+          keep = wr > 0.0;
+          wk = w * rf * wr * ( 1.0 - ptransm );
+        }
+      }
+      const unsigned long long slot = appendSlot( &c->n_b, keep );
+      if ( keep ) {
+        const uint64_t j = slot;
+        b.pos[3 * j] = p[0] + ds * u[0];
+        b.pos[3 * j + 1] = p[1] + ds * u[1];
+        b.pos[3 * j + 2] = p[2] + ds * u[2];
+        b.dir[3 * j] = u[0]; b.dir[3 * j + 1] = u[1]; b.dir[3 * j + 2] = u[2];
+        b.e[j] = e;
+        b.w[j] = wk;
+        b.xs[j] = xs;
+        b.nscat[j] = nscat;
+        b.ninel[j] = ninel;
+        b.id[j] = a.id[i];
+        b.e0[j] = a.e0[i];
+        b.d0[3 * j] = a.d0[3 * i]; b.d0[3 * j + 1] = a.d0[3 * i + 1]; b.d0[3 * j + 2] = a.d0[3 * i + 2];
+      }
+      // the transmitted part, at the exit (propagateAndAttenuate, then the
+      // scatter-process transmission), is tallied
+      double pabs;
+      if ( eng.has_abs ) {
+        const double xa = fmin( kDblMax, xabs );
+        pabs = ( g.unbounded && dinf ) ? 0.0 : ( xa != 0.0 ? exp( -xa * dexit ) : 1.0 );
+      } else {
+        pabs = ( g.unbounded && dinf ) ? 0.0 : 1.0;
+      }
+      const double wt = w * pabs * ptransm;
+      const double d0[3] = { a.d0[3 * i], a.d0[3 * i + 1], a.d0[3 * i + 2] };
+      tallyNeutron( tb, t, e, u, wt, nscat, ninel, a.e0[i], d0 );
+      atomicAdd( &tal.n, 1ull );
+      atomicAdd( &tal.w, wt );
+    }
+    if ( smem )
+      tallyFlushShared( sh, t );
+    __syncthreads();
+    if ( threadIdx.x == 0 && tal.n ) {
+      atomicAdd( &c->tallied, tal.n );
+      atomicAdd( &c->tallied_w, tal.w );
+    }
+  }
+
+  int gridFor( uint64_t n, int block, int cap )
+  {
+    const uint64_t g = ( n + block - 1 ) / block;
+    return (int)( g < (uint64_t)cap ? ( g ? g : 1 ) : cap );
+  }
+}
+
+namespace ncgb {
+  namespace mmc {
+
+    cudaError_t launchEmit( const Source& src, const Geom& g, const Engine& eng, const Tally& t, Pop a,
+                            uint64_t base, uint64_t first_id, uint64_t count, Counters* c, int numSMs,
+                            cudaStream_t s )
+    {
+      if ( count == 0 )
+        return cudaSuccess;
+      k_mmc_emit<<<gridFor( count, 256, numSMs * 8 ), 256, 0, s>>>( src, g, eng, t, a, base, first_id, count, c );
+      return cudaGetLastError();
+    }
+
+    cudaError_t launchTransport( const ncgb_material_view& m, const Geom& g, const Engine& eng, const Tally& t,
+                                 Pop a, uint64_t n_a, Pop b, uint32_t step, Counters* c, int numSMs,
+                                 cudaStream_t s )
+    {
+      if ( n_a == 0 )
+        return cudaSuccess;
+      // block-local tallies in shared memory when they fit
+      const std::size_t sbytes = (std::size_t)t.nbuf * sizeof(double);
+      const bool smem = sbytes <= 48 * 1024;
+      const int grid = gridFor( n_a, 256, numSMs * 4 );
+      if ( eng.fast )
+        k_mmc_transport<true><<<grid, 256, smem ? sbytes : 0, s>>>( m, g, eng, t, a, n_a, b, step, c, smem ? 1 : 0 );
+      else
+        k_mmc_transport<false><<<grid, 256, smem ? sbytes : 0, s>>>( m, g, eng, t, a, n_a, b, step, c, smem ? 1 : 0 );
+      return cudaGetLastError();
+    }
+  }
+}

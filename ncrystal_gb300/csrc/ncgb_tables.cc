@@ -467,6 +467,9 @@ namespace ncgb {
     auto mt = std::make_shared<MaterialTables>();
     mt->m_cfg = b.str("cfg");
     mt->m_temperature = b.has("temperature") ? b.f64s("temperature") : -1.0;
+    mt->m_numdens = b.has("info.numdens") ? b.f64s("info.numdens") : -1.0;
+    mt->m_info_temperature = b.has("info.temperature") ? b.f64s("info.temperature") : -1.0;
+    mt->m_bragg_threshold = b.has("info.bragg_threshold") ? b.f64s("info.bragg_threshold") : -1.0;
     ncgb_material_view& v = mt->m_rel;
     std::memset( &v, 0, sizeof(v) );
     const int64_t ncomp = b.i64s("ncomp");

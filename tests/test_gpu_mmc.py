@@ -1,0 +1,133 @@
+"""Device MiniMC against the reference's own MiniMC (tests/golden/mmc_*.npz,
+made by tests/golden/make_mmc_golden.py with the reference library): the same
+queries through this library's ncrystal_jsonquery, compared statistically
+(two-sample chi-square of every tally histogram and breakdown, normalised per
+source neutron; Bonferroni over the comparisons of a fixture), plus the
+metadata counts, scenario decoding and reproducibility."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import ncrystal_gb300.minimc as M
+from conftest import bundle_path
+from mmc_stats import GROUPS, chi2_compare, hist_from_result
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+FILES = sorted(f for f in glob.glob(os.path.join(GOLDEN, "mmc_*.npz")) if not f.endswith("mmc_scenarios.npz"))
+
+_cache = {}
+
+
+def _run(entries):
+    key = tuple(entries)
+    if key not in _cache:
+        bundle_path(entries[2])
+        q = list(entries[2:])
+        if len(q) == 4:
+            _cache[key] = M.run(q[0], geomcfg=q[1], srccfg=q[2], enginecfg=q[3])
+        else:
+            _cache[key] = M.run(q[0], scenario=q[1], enginecfg=q[2])
+    return _cache[key]
+
+
+@pytest.mark.parametrize("path", FILES, ids=[os.path.basename(p)[:-4] for p in FILES])
+def test_mmc_tallies_match_reference(path):
+    g = np.load(path)
+    entries = str(g["query"]).split("\x07")
+    res = _run(entries)
+    n_ref = g["meta.provided"][0]
+    n_gpu = res["output"]["metadata"]["provided"]["count"]
+    assert n_gpu == n_ref
+    tallies = sorted({k.split(".")[0] for k in g.files if k.endswith(".total.content")})
+    assert sorted(res["output"]["tally"].keys()) == tallies
+    comps = []
+    for t in tallies:
+        for part in ["total"] + GROUPS:
+            kc = "%s.%s.content" % (t, part)
+            if kc not in g.files:
+                continue
+            c, e, rng = hist_from_result(res, t, part)
+            rr = g["%s.%s.range" % (t, part)]
+            assert (rng[0], rng[1], rng[2]) == pytest.approx((rr[0], rr[1], rr[2]), rel=1e-12), (t, part)
+            x, ndf, p, worst = chi2_compare(g[kc], g["%s.%s.errorsq" % (t, part)], n_ref, c, e, n_gpu)
+            assert len(worst) == 0, (t, part, worst)
+            comps.append((p, t, part, x, ndf))
+    assert comps
+    pmin = min(c[0] for c in comps)
+    msg = "; ".join("%s/%s chi2=%.1f ndf=%d p=%.2e" % (t, part, x, ndf, p) for p, t, part, x, ndf in sorted(comps)[:4])
+    assert pmin > 1e-3 / len(comps), msg
+    # metadata: misses (binomial) and the tallied weight per source neutron
+    mr = g["meta.miss"]
+    mg = res["output"]["metadata"]["miss"]
+    pm = mr[0] / n_ref
+    sig = max(np.sqrt(2 * pm * (1 - pm) / n_ref), 1e-12)
+    assert abs(mg["count"] / n_gpu - pm) < 5 * sig + 1e-12
+    tr = g["meta.tallied"]
+    tg = res["output"]["metadata"]["tallied"]
+    assert abs(tg["weight"] / n_gpu - tr[1] / n_ref) < 2e-3
+    assert abs(tg["count"] / n_gpu - tr[0] / n_ref) < 0.01 * tr[0] / n_ref
+
+
+def test_mmc_scenarios_decode_like_reference():
+    rows = np.load(os.path.join(GOLDEN, "mmc_scenarios.npz"))["rows"]
+    for cfg, scen, geom, src in rows:
+        bundle_path(str(cfg))
+        d = M.decode_scenario(str(cfg), str(scen))
+        assert d["geomcfg"] == str(geom), (cfg, scen, d)
+        assert d["srccfg"] == str(src), (cfg, scen, d)
+
+
+def test_mmc_reproducible_and_seeded():
+    cfg = "Al_sg225.ncmat;temp=293K"
+    bundle_path(cfg)
+    q = dict(geomcfg="sphere;r=0.01", srccfg="circular;wl=3;z=-0.01;r=0.01;n=2e5", enginecfg="seed=5;tally=theta,nscat")
+    a = M.run(cfg, **q)
+    b = M.run(cfg, **q)
+    ca, _, _ = hist_from_result(a, "theta", "total")
+    cb, _, _ = hist_from_result(b, "theta", "total")
+    # the same histories (random streams keyed by source index and step); sums
+    # may differ in the last bits through the order of atomic additions
+    np.testing.assert_allclose(ca, cb, rtol=1e-9, atol=1e-9)
+    assert a["output"]["metadata"]["tallied"]["count"] == b["output"]["metadata"]["tallied"]["count"]
+    q["enginecfg"] = "seed=6;tally=theta,nscat"
+    c = M.run(cfg, **q)
+    cc, _, _ = hist_from_result(c, "theta", "total")
+    assert not np.array_equal(ca, cc)
+
+
+def test_mmc_mixed_mode_matches_exact_statistically():
+    import ncrystal_gb300 as NC
+    cfg = "Polyethylene_CH2.ncmat;temp=293K"
+    bundle_path(cfg)
+    runs = {}
+    for mode in ("exact", "mixed"):
+        sc = NC.createScatter(cfg, seed=3 if mode == "exact" else 4)
+        sc.set_mode(mode)
+        runs[mode] = sc.minimc_run("sphere;r=0.01", "constant;ekin=0.0253;z=-0.01;n=4e6", "tally=theta,e")
+    for t in ("theta", "e"):
+        c1, e1, _ = hist_from_result(runs["exact"], t, "total")
+        c2, e2, _ = hist_from_result(runs["mixed"], t, "total")
+        x, ndf, p, worst = chi2_compare(c1, e1, 4e6, c2, e2, 4e6)
+        assert len(worst) == 0 and p > 1e-4, (t, x, ndf, p)
+
+
+def test_mmc_no_scattering_material_transmits():
+    """absorption only / nscatlimit=0: every neutron leaves unscattered, with
+    the analytic transmission exp(-sigma_abs n d) through the sphere's centre."""
+    cfg = "Polyethylene_CH2.ncmat;temp=293K"
+    bundle_path(cfg)
+    res = M.run(cfg, geomcfg="sphere;r=0.01", srccfg="constant;ekin=0.0253;z=-0.01;n=1e5",
+                enginecfg="nscatlimit=0;tally=theta,nscat")
+    c, _, _ = hist_from_result(res, "theta", "total")
+    w = res["output"]["metadata"]["tallied"]["weight"] / 1e5
+    assert c[1] / 1e5 == pytest.approx(w, rel=1e-12)    # all at theta = 0
+    import ncrystal_gb300 as NC
+    ab = NC.createAbsorption(cfg)
+    sabs = float(ab.crossSectionIsotropic(0.0253))
+    from ncrystal_gb300.bundle.reader import read_bundle
+    nd = float(read_bundle(bundle_path(cfg))["info.numdens"][0])   # atoms/Aa^3
+    assert w == pytest.approx(np.exp(-sabs * nd * 100.0 * 0.02), rel=1e-6)
