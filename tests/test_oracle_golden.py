@@ -11,7 +11,7 @@ from conftest import KAT_AL_BRAGG, KAT_NI, bundle_path
 from oracle.pyoracle import HostMaterial
 
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                if not os.path.basename(p).startswith(("dir_", "abs_")))
+                if not os.path.basename(p).startswith(("dir_", "abs_", "mmc_")))
 WL2EKIN = 0.081804209605330899
 
 
