@@ -871,10 +871,16 @@ namespace {
       h.xmin = lo[k];
       h.xmax = hi[k];
       h.inv_delta = nb[k] / ( hi[k] - lo[k] );
-      h.off = off;
-      off += (int64_t)kGroups * ( nb[k] + 2 ) * 2;
       h.soff = off;
       off += kGroups * kStats;
+    }
+    t.nstat = off;
+    for ( int k = 0; k < T_N; ++k ) {
+      TallyHist& h = t.h[k];
+      if ( !h.enabled )
+        continue;
+      h.off = off;
+      off += (int64_t)kGroups * ( h.nbins + 2 ) * 2;
     }
     t.nbuf = off;
     return t;

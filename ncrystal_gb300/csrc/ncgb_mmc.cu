@@ -4,6 +4,7 @@
 // engine (ncgb_mmc.cc) between two transport steps.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <cstdlib>
 
 #include "ncgb_device.cuh"
 #include "ncgb_mmc.hh"
@@ -193,46 +194,118 @@ namespace {
     return k < 0 ? ( k ^ 0x7FFFFFFFFFFFFFFFLL ) : k;
   }
 
-  // Hist1D::fill (NCHists.hh:303-345, :376-400; RunningStats1D :613-650) into
-  // group g of histogram h.
-  __device__ __forceinline__ void histFill( double* buf, const TallyHist& h, int g, double x, double w, bool weighted )
+  constexpr unsigned kFull = 0xffffffffu;
+
+  // Bin of x (HistBinData1D::valueToBin with under/overflow recording,
+  // NCHists.hh:376-400): 0 underflow, 1..nbins, nbins+1 overflow; x == xmax
+  // goes to the last bin, and values that round up to nbins bins above xmin
+  // to the overflow, as in the reference.
+  __device__ __forceinline__ int binOf( const TallyHist& h, double x )
   {
-    if ( weighted && !( w > 0.0 ) )
-      return;
-    const double wt = weighted ? w : 1.0;
-    int bin;
     if ( x < h.xmin )
-      bin = 0;
-    else if ( x >= h.xmax )
-      bin = ( x == h.xmax ) ? h.nbins : h.nbins + 1;
-    else {
-      const double f = h.inv_delta * ( x - h.xmin );
-      bin = 1 + ( f >= (double)h.nbins ? h.nbins : (int)f );
-    }
-    double* b = buf + h.off + ( (int64_t)g * ( h.nbins + 2 ) + bin ) * 2;
-    atomicAdd( b, wt );
-    atomicAdd( b + 1, wt * wt );
-    double* st = buf + h.soff + g * kStats;
-    atomicAdd( st, wt );
-    atomicAdd( st + 1, wt * x );
-    atomicAdd( st + 2, wt * x * x );
-    const long long k = orderKey( x );
-    atomicMin( reinterpret_cast<long long*>( st + 3 ), k );
-    atomicMax( reinterpret_cast<long long*>( st + 4 ), k );
+      return 0;
+    if ( x >= h.xmax )
+      return ( x == h.xmax ) ? h.nbins : h.nbins + 1;
+    const double f = h.inv_delta * ( x - h.xmin );
+    return 1 + ( f >= (double)h.nbins ? h.nbins : (int)f );
   }
 
-  __device__ __forceinline__ void histFill2( double* buf, const Tally& t, int kind, int cat, double x, double w,
-                                             bool weighted )
+  // Warp-aggregated bin update: lanes filling the same (group, bin) sum
+  // their weights through the warp's scratch, and the lowest of them adds the
+  // sums with one atomic pair.
+  // Called by all 32 lanes.
+  __device__ __forceinline__ void addBins( double* buf, double* scr, const TallyHist& h, int g, int bin, double wt,
+                                           bool f )
+  {
+    const int lane = threadIdx.x & 31;
+    const unsigned key = f ? (unsigned)( g * ( h.nbins + 2 ) + bin ) : 0xffffffffu;
+    const unsigned peers = __match_any_sync( kFull, key );
+    double* b = buf + h.off + ( f ? (int64_t)key * 2 : 0 );
+    if ( __all_sync( kFull, __popc( peers ) == 1 ) ) {
+      if ( f ) {
+        atomicAdd( b, wt );
+        atomicAdd( b + 1, wt * wt );
+      }
+      return;
+    }
+    scr[lane] = f ? wt : 0.0;
+    scr[32 + lane] = f ? wt * wt : 0.0;
+    __syncwarp();
+    if ( f && __ffs( peers ) - 1 == lane ) {
+      double c = 0.0, c2 = 0.0;
+      unsigned m = peers;
+      while ( m ) {
+        const int j = __ffs( m ) - 1;
+        m &= m - 1;
+        c += scr[j];
+        c2 += scr[32 + j];
+      }
+      atomicAdd( b, c );
+      atomicAdd( b + 1, c2 );
+    }
+    __syncwarp();
+  }
+
+  // Warp reduction of one group's running statistics (RunningStats1D,
+  // NCHists.hh:613-650): sums of w, w x, w x^2 (FP64) and the extreme keys,
+  // added by lane 0.  Called by all 32 lanes; f selects the contributing ones.
+  __device__ __forceinline__ void addStats( double* st, double x, double wt, bool f )
+  {
+    double s0 = f ? wt : 0.0, s1 = f ? wt * x : 0.0, s2 = f ? wt * x * x : 0.0;
+    const long long k = orderKey( x );
+    long long kmin = f ? k : 0x7FFFFFFFFFFFFFFFLL, kmax = f ? k : (long long)0x8000000000000000ULL;
+#pragma unroll
+    for ( int o = 16; o > 0; o >>= 1 ) {
+      s0 += __shfl_xor_sync( kFull, s0, o );
+      s1 += __shfl_xor_sync( kFull, s1, o );
+      s2 += __shfl_xor_sync( kFull, s2, o );
+      const long long a = __shfl_xor_sync( kFull, kmin, o ), b = __shfl_xor_sync( kFull, kmax, o );
+      kmin = a < kmin ? a : kmin;
+      kmax = b > kmax ? b : kmax;
+    }
+    if ( ( threadIdx.x & 31 ) == 0 ) {
+      atomicAdd( st, s0 );
+      atomicAdd( st + 1, s1 );
+      atomicAdd( st + 2, s2 );
+      atomicMin( reinterpret_cast<long long*>( st + 3 ), kmin );
+      atomicMax( reinterpret_cast<long long*>( st + 4 ), kmax );
+    }
+  }
+
+  // Hist1D::fill (NCHists.hh:303-345, :525-530) of histogram h for the warp:
+  // the total and, with breakdowns, the group of each lane's category.
+  // Weighted fills skip weights <= 0; unweighted fills count 1.
+  // Where a kernel's tally updates go: statistics (always block-local in
+  // shared memory) and bins (shared memory or the global buffer); both are
+  // indexed with the global buffer's offsets.
+  struct TallyDst {
+    double* stats;
+    double* bins;
+  };
+
+  __device__ void histFillWarp( const TallyDst& d, double* scr, const Tally& t, int kind, int cat, double x,
+                                double w, bool weighted, bool on )
   {
     const TallyHist& h = t.h[kind];
-    histFill( buf, h, 0, x, w, weighted );
-    if ( t.breakdown )
-      histFill( buf, h, 1 + cat, x, w, weighted );
+    const bool f = on && ( !weighted || w > 0.0 );
+    if ( !__any_sync( kFull, f ) )
+      return;
+    const double wt = weighted ? w : 1.0;
+    const int bin = f ? binOf( h, x ) : 0;
+    addBins( d.bins, scr, h, 0, bin, wt, f );
+    addStats( d.stats + h.soff, x, wt, f );
+    if ( t.breakdown ) {
+      addBins( d.bins, scr, h, 1 + cat, bin, wt, f );
+      for ( int c = 0; c < kGroups - 1; ++c )
+        if ( __any_sync( kFull, f && cat == c ) )
+          addStats( d.stats + h.soff + ( 1 + c ) * kStats, x, wt, f && cat == c );
+    }
   }
 
-  // tallyRecord (NCMMC_StdTallies.cc:430-660) for one neutron.
-  __device__ void tallyNeutron( double* buf, const Tally& t, double e, const double* u, double w, int nscat,
-                                int ninel, double e0, const double* d0 )
+  // tallyRecord (NCMMC_StdTallies.cc:430-660) for the warp's neutrons ('on'
+  // lanes).  Called by all 32 lanes.
+  __device__ void tallyWarp( const TallyDst& buf, double* scr, const Tally& t, bool on, double e, const double* u, double w,
+                             int nscat, int ninel, double e0, const double* d0 )
   {
     // init_dethistidvect, NCMMC_StdTallies.cc:288-308
     const int cat = nscat > 1 ? ( ninel ? 4 : 3 ) : ( nscat == 1 ? ( ninel ? 2 : 1 ) : 0 );
@@ -248,78 +321,71 @@ namespace {
         mu = __dadd_rn( __dadd_rn( __dmul_rn( d0[0], u[0] ), __dmul_rn( d0[1], u[1] ) ), __dmul_rn( d0[2], u[2] ) );
       mu = clampd( mu, -1.0, 1.0 );
       if ( t.h[T_MU].enabled )
-        histFill2( buf, t, T_MU, cat, mu, w, true );
+        histFillWarp( buf, scr, t, T_MU, cat, mu, w, true, on );
       if ( t.h[T_Q].enabled ) {
         const double ei = t.fixed_e ? t.e0 : e0;
         const double q2 = __dmul_rn( __dadd_rn( __dadd_rn( __dmul_rn( __dmul_rn( sqrt( __dmul_rn( e, ei ) ), mu ), -2.0 ),
                                                            ei ), e ), kEkin2Ksq );
-        histFill2( buf, t, T_Q, cat, sqrt( maxd( 0.0, q2 ) ), w, true );
+        histFillWarp( buf, scr, t, T_Q, cat, sqrt( maxd( 0.0, q2 ) ), w, true, on );
       }
       if ( t.h[T_THETA].enabled )
-        histFill2( buf, t, T_THETA, cat, acos( mu ) * kToDeg, w, true );
+        histFillWarp( buf, scr, t, T_THETA, cat, acos( mu ) * kToDeg, w, true, on );
     }
     if ( t.h[T_E].enabled )
-      histFill2( buf, t, T_E, cat, e, w, true );
+      histFillWarp( buf, scr, t, T_E, cat, e, w, true, on );
     if ( t.h[T_DE].enabled )
-      histFill2( buf, t, T_DE, cat, ( t.fixed_e ? t.e0 : e0 ) - e, w, true );
+      histFillWarp( buf, scr, t, T_DE, cat, ( t.fixed_e ? t.e0 : e0 ) - e, w, true, on );
     if ( t.h[T_L].enabled )
-      histFill2( buf, t, T_L, cat, sqrt( kWl2Ekin ) * sqrt( 1.0 / maxd( 4.9406564584124654e-324, e ) ), w, true );
+      histFillWarp( buf, scr, t, T_L, cat, sqrt( kWl2Ekin ) * sqrt( 1.0 / maxd( 4.9406564584124654e-324, e ) ), w,
+                    true, on );
     if ( t.h[T_NSCAT].enabled )
-      histFill2( buf, t, T_NSCAT, cat, (double)nscat, w, true );
+      histFillWarp( buf, scr, t, T_NSCAT, cat, (double)nscat, w, true, on );
     if ( t.h[T_NSCAT_UW].enabled )
-      histFill2( buf, t, T_NSCAT_UW, cat, (double)nscat, w, false );
+      histFillWarp( buf, scr, t, T_NSCAT_UW, cat, (double)nscat, w, false, on );
     if ( t.h[T_W].enabled )
-      histFill2( buf, t, T_W, cat, w, w, false );
+      histFillWarp( buf, scr, t, T_W, cat, w, w, false, on );
   }
 
-  // Block-local copy of the tally buffer in shared memory (when it fits):
-  // the min/max keys start at the empty values, the sums at zero.
-  __device__ void tallyInitShared( double* sh, const Tally& t )
+  // Block-local tallies in shared memory: the statistics always, the bins
+  // too when 'bins' is set (sh then mirrors the whole buffer).  Min/max keys
+  // start at the empty values, sums at zero.
+  __device__ void tallyInitShared( double* sh, const Tally& t, bool bins )
   {
-    for ( int64_t i = threadIdx.x; i < t.nbuf; i += blockDim.x )
-      sh[i] = 0.0;
-    __syncthreads();
-    for ( int k = 0; k < T_N; ++k ) {
-      if ( !t.h[k].enabled )
-        continue;
-      for ( int g = threadIdx.x; g < kGroups; g += blockDim.x ) {
-        long long* st = reinterpret_cast<long long*>( sh + t.h[k].soff + g * kStats );
-        st[3] = 0x7FFFFFFFFFFFFFFFLL;
-        st[4] = (long long)0x8000000000000000ULL;
-      }
+    const int64_t n = bins ? t.nbuf : t.nstat;
+    for ( int64_t i = threadIdx.x; i < n; i += blockDim.x ) {
+      const int j = (int)( i % kStats );
+      long long v = 0;
+      if ( i < t.nstat && j == 3 ) v = 0x7FFFFFFFFFFFFFFFLL;
+      if ( i < t.nstat && j == 4 ) v = (long long)0x8000000000000000ULL;
+      sh[i] = __longlong_as_double( v );
     }
     __syncthreads();
   }
 
-  __device__ void tallyFlushShared( const double* sh, const Tally& t )
+  __device__ void tallyFlushShared( const double* sh, const Tally& t, bool bins )
   {
     __syncthreads();
-    for ( int k = 0; k < T_N; ++k ) {
-      if ( !t.h[k].enabled )
-        continue;
-      const TallyHist& h = t.h[k];
-      const int64_t nb = (int64_t)kGroups * ( h.nbins + 2 ) * 2;
-      for ( int64_t i = threadIdx.x; i < nb; i += blockDim.x ) {
-        const double v = sh[h.off + i];
+    for ( int64_t i = threadIdx.x; i < t.nstat; i += blockDim.x ) {
+      const int j = (int)( i % kStats );
+      const double v = sh[i];
+      if ( j < 3 ) {
         if ( v != 0.0 )
-          atomicAdd( t.buf + h.off + i, v );
-      }
-      for ( int i = threadIdx.x; i < kGroups * kStats; i += blockDim.x ) {
-        const int j = i % kStats;
-        const double v = sh[h.soff + i];
-        if ( j < 3 ) {
-          if ( v != 0.0 )
-            atomicAdd( t.buf + h.soff + i, v );
-        } else {
-          const long long kv = __double_as_longlong( v );
-          long long* dst = reinterpret_cast<long long*>( t.buf + h.soff + i );
-          if ( j == 3 && kv != 0x7FFFFFFFFFFFFFFFLL )
-            atomicMin( dst, kv );
-          if ( j == 4 && kv != (long long)0x8000000000000000ULL )
-            atomicMax( dst, kv );
-        }
+          atomicAdd( t.buf + i, v );
+      } else {
+        const long long kv = __double_as_longlong( v );
+        long long* dst = reinterpret_cast<long long*>( t.buf + i );
+        if ( j == 3 && kv != 0x7FFFFFFFFFFFFFFFLL )
+          atomicMin( dst, kv );
+        if ( j == 4 && kv != (long long)0x8000000000000000ULL )
+          atomicMax( dst, kv );
       }
     }
+    if ( bins )
+      for ( int64_t i = t.nstat + threadIdx.x; i < t.nbuf; i += blockDim.x ) {
+        const double v = sh[i];
+        if ( v != 0.0 )
+          atomicAdd( t.buf + i, v );
+      }
   }
 
   // Warp-aggregated append: slot of this lane among the lanes with 'want'.
@@ -338,67 +404,92 @@ namespace {
     return base + __popc( mask & ( ( 1u << lane ) - 1u ) );
   }
 
-  // Block sums of the tallied / missed counts, added to the counters once.
+  // Warp sums of the tallied (or missed) counts, added to block totals in
+  // shared memory.  Called by all 32 lanes.
   struct BlockSums {
     unsigned long long n;
     double w;
   };
 
-  // ---- kernels --------------------------------------------------------------------
+  __device__ __forceinline__ void addCount( BlockSums* bs, bool on, double w )
+  {
+    const unsigned m = __ballot_sync( kFull, on );
+    double s = on ? w : 0.0;
+#pragma unroll
+    for ( int o = 16; o > 0; o >>= 1 )
+      s += __shfl_xor_sync( kFull, s, o );
+    if ( m && ( threadIdx.x & 31 ) == 0 ) {
+      atomicAdd( &bs->n, (unsigned long long)__popc( m ) );
+      atomicAdd( &bs->w, s );
+    }
+  }
+
+  constexpr int kBlock = 256;
+  constexpr int kWarps = kBlock / 32;
 
   // Source neutrons first_id .. first_id+count-1: fillBasket of the source
   // (NCMMC_Source.cc) and BasketSrcFiller::propagateToVolume
   // (NCMMC_BasketSrcFiller.hh:120-178): neutrons that miss the volume are
   // tallied with nscat = -1 (NCMMC_Baskets.cc:81) unless ignoremiss, and
   // counted; the rest are moved onto the volume and appended to population a.
-  __global__ void __launch_bounds__(256)
+  // Warp-uniform loop (all lanes iterate together for the warp collectives).
+  __global__ void __launch_bounds__(kBlock)
   k_mmc_emit( const Source src, const Geom g, const Engine eng, const Tally t, Pop a, uint64_t base,
-              uint64_t first_id, uint64_t count, Counters* c )
+              uint64_t first_id, uint64_t count, Counters* c, int bins_smem )
   {
-    // (misses are few: they are tallied straight into global memory)
-    __shared__ BlockSums miss;
-    if ( threadIdx.x == 0 ) { miss.n = 0; miss.w = 0.0; }
+    extern __shared__ double sh[];
+    __shared__ BlockSums miss, tal;
+    __shared__ double scratch[kWarps][64];
+    double* scr = scratch[threadIdx.x >> 5];
+    const TallyDst tb{ sh, bins_smem ? sh : t.buf };
+    tallyInitShared( sh, t, bins_smem );
+    if ( threadIdx.x == 0 ) { miss.n = 0; miss.w = 0.0; tal.n = 0; tal.w = 0.0; }
     __syncthreads();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for ( uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride ) {
+    for ( uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < count; i0 += stride ) {
+      const uint64_t i = i0 + threadIdx.x;
+      const bool on = i < count;
       const uint64_t id = first_id + i;
       ncgb_rng rng;
       ncgb_rng_init( &rng, eng.seed, (uint32_t)id, 0u, kStreamSource );
       double p[3] = { src.x, src.y, src.z };
       double u[3] = { src.ux, src.uy, src.uz };
-      if ( src.kind == SRC_CIRCULAR && src.r > 0.0 ) {
-        // uniform point in the unit disk (polar form of randPointInUnitCircle)
-        const double rad = sqrt( rand01( rng ) ), phi = 2.0 * rand01( rng );
-        const double a0 = rad * cospi( phi ), b0 = rad * sinpi( phi );
-        p[0] += src.ax * a0 + src.bx * b0;
-        p[1] += src.ay * a0 + src.by * b0;
-        p[2] += src.az * a0 + src.bz * b0;
-      } else if ( src.kind == SRC_ISOTROPIC ) {
-        randIsotropic( rng, u );
-        if ( src.r != 0.0 ) {
-          p[0] -= u[0] * src.r;
-          p[1] -= u[1] * src.r;
-          p[2] -= u[2] * src.r;
+      double e = 0.0;
+      if ( on ) {
+        if ( src.kind == SRC_CIRCULAR && src.r > 0.0 ) {
+          // uniform point in the unit disk (polar form of randPointInUnitCircle)
+          const double rad = sqrt( rand01( rng ) ), phi = 2.0 * rand01( rng );
+          const double a0 = rad * cospi( phi ), b0 = rad * sinpi( phi );
+          p[0] += src.ax * a0 + src.bx * b0;
+          p[1] += src.ay * a0 + src.by * b0;
+          p[2] += src.az * a0 + src.bz * b0;
+        } else if ( src.kind == SRC_ISOTROPIC ) {
+          randIsotropic( rng, u );
+          if ( src.r != 0.0 ) {
+            p[0] -= u[0] * src.r;
+            p[1] -= u[1] * src.r;
+            p[2] -= u[2] * src.r;
+          }
         }
+        e = sourceEnergy( src, rng );
       }
-      const double e = sourceEnergy( src, rng );
-      bool keep = true;
-      if ( src.might_be_outside ) {
+      bool keep = on, missed = false;
+      if ( on && src.might_be_outside ) {
         const double d = distEntry( g, p, u );
         if ( d < 0.0 ) {
           keep = false;
-          atomicAdd( &miss.n, 1ull );
-          atomicAdd( &miss.w, 1.0 );
-          if ( !eng.ignore_miss ) {
-            tallyNeutron( t.buf, t, e, u, 1.0, -1, 0, e, u );
-            atomicAdd( &c->tallied, 1ull );
-            atomicAdd( &c->tallied_w, 1.0 );
-          }
+          missed = true;
         } else {
           p[0] += d * u[0];
           p[1] += d * u[1];
           p[2] += d * u[2];
         }
+      }
+      addCount( &miss, missed, 1.0 );
+      const bool tally_miss = missed && !eng.ignore_miss;
+      if ( __any_sync( kFull, tally_miss ) ) {
+        tallyWarp( tb, scr, t, tally_miss, e, u, 1.0, -1, 0, e, u );
+        addCount( &tal, tally_miss, 1.0 );
       }
       const unsigned long long slot = appendSlot( &c->n_a, keep );
       if ( keep ) {
@@ -416,98 +507,127 @@ namespace {
         a.st[j] = kNoScatter;
       }
     }
+    tallyFlushShared( sh, t, bins_smem );
     __syncthreads();
-    if ( threadIdx.x == 0 && miss.n ) {
-      atomicAdd( &c->miss, miss.n );
-      atomicAdd( &c->miss_w, miss.w );
+    if ( threadIdx.x == 0 ) {
+      if ( miss.n ) {
+        atomicAdd( &c->miss, miss.n );
+        atomicAdd( &c->miss_w, miss.w );
+      }
+      if ( tal.n ) {
+        atomicAdd( &c->tallied, tal.n );
+        atomicAdd( &c->tallied_w, tal.w );
+      }
     }
   }
 
   // One engine step over population a (StdSimEngine::processBasket,
-  // NCMMC_SimEngine.cc:170-440).
+  // NCMMC_SimEngine.cc:170-440).  Warp-uniform loop, as k_mmc_emit.
   template<bool Fast>
-  __global__ void __launch_bounds__(256)
+  __global__ void __launch_bounds__(kBlock)
   k_mmc_transport( const __grid_constant__ ncgb_material_view m, const Geom g, const Engine eng, const Tally t,
-                   const Pop a, uint64_t n_a, const Pop b, uint32_t step, Counters* c, int smem )
+                   const Pop a, uint64_t n_a, const Pop b, uint32_t step, Counters* c, int bins_smem )
   {
     extern __shared__ double sh[];
     __shared__ BlockSums tal;
-    double* tb = smem ? sh : t.buf;
-    if ( smem )
-      tallyInitShared( sh, t );
+    __shared__ double scratch[kWarps][64];
+    double* scr = scratch[threadIdx.x >> 5];
+    const TallyDst tb{ sh, bins_smem ? sh : t.buf };
+    tallyInitShared( sh, t, bins_smem );
     if ( threadIdx.x == 0 ) { tal.n = 0; tal.w = 0.0; }
     __syncthreads();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for ( uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_a; i += stride ) {
-      double p[3] = { a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2] };
-      double u[3];
-      double e = a.e[i], w = a.w[i], xs = a.xs[i];
-      int nscat = a.nscat[i], ninel = a.ninel[i];
-      const int pst = a.st[i];
-      if ( pst == kNoScatter ) {
-        u[0] = a.dir[3 * i]; u[1] = a.dir[3 * i + 1]; u[2] = a.dir[3 * i + 2];
-      } else if ( pst == NCGB_ST_OK ) {
-        // the scatter of the previous step (NCMMC_SimEngine.cc:390-410)
-        const double en = a.e_new[i];
-        u[0] = a.dir_new[3 * i]; u[1] = a.dir_new[3 * i + 1]; u[2] = a.dir_new[3 * i + 2];
-        ++nscat;
-        if ( en != e ) {
-          ++ninel;
-          xs = -1.0;   // the cross-section might have changed
+    for ( uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n_a; i0 += stride ) {
+      const uint64_t i = i0 + threadIdx.x;
+      bool on = i < n_a;
+      double p[3] = { 0.0, 0.0, 0.0 }, u[3] = { 0.0, 0.0, 1.0 }, d0[3] = { 0.0, 0.0, 1.0 };
+      double e = 0.0, w = 0.0, xs = 0.0, e0 = 0.0;
+      int nscat = 0, ninel = 0;
+      uint32_t id = 0;
+      if ( on ) {
+        p[0] = a.pos[3 * i]; p[1] = a.pos[3 * i + 1]; p[2] = a.pos[3 * i + 2];
+        e = a.e[i]; w = a.w[i]; xs = a.xs[i];
+        nscat = a.nscat[i]; ninel = a.ninel[i];
+        id = a.id[i];
+        e0 = a.e0[i];
+        d0[0] = a.d0[3 * i]; d0[1] = a.d0[3 * i + 1]; d0[2] = a.d0[3 * i + 2];
+        const int pst = a.st[i];
+        if ( pst == kNoScatter ) {
+          u[0] = a.dir[3 * i]; u[1] = a.dir[3 * i + 1]; u[2] = a.dir[3 * i + 2];
+        } else if ( pst == NCGB_ST_OK ) {
+          // the scatter of the previous step (NCMMC_SimEngine.cc:390-410)
+          const double en = a.e_new[i];
+          u[0] = a.dir_new[3 * i]; u[1] = a.dir_new[3 * i + 1]; u[2] = a.dir_new[3 * i + 2];
+          ++nscat;
+          if ( en != e ) {
+            ++ninel;
+            xs = -1.0;   // the cross-section might have changed
+          }
+          e = en;
+        } else {
+          // the reference aborts the run here; the host reports the failure
+          atomicAdd( &c->nfail, 1ull );
+          on = false;
         }
-        e = en;
-      } else {
-        // the reference aborts the run here; the host reports the failure
-        atomicAdd( &c->nfail, 1ull );
-        continue;
       }
-      const double dexit = distExit( g, p, u );
-      const bool dinf = !finited( dexit );
-      // absorption (evalManyXSIsotropic of AbsOOV) and scattering (the
-      // cached value unless new or changed) macroscopic cross-sections
-      const double xabs = eng.has_abs ? eng.macro * absXS( eng.abs_c, e ) : 0.0;
-      if ( !eng.has_scat || eng.nscatlimit == 0 || ( eng.nscatlimit > 0 && nscat >= eng.nscatlimit ) ) {
-        xs = 0.0;
-      } else if ( nscat <= 0 || xs < 0.0 ) {
-        double x = 0.0;
-        if ( contains( m.dom_elow, m.dom_ehigh, e ) ) {
-          ncgb_rng dummy;
-          ncgb_rng_init( &dummy, 0, 0, 0, 0 );
-          x = xsAndPick<false, Fast>( m, e, dummy ).xs;
-        }
-        xs = eng.macro * x;
-      }
-      // calcProbTransm (NCMMC_Utils.cc:46-88): 0 for an infinite path
-      const double xsc = fmin( kDblMax, xs );
-      const double ptransm = ( g.unbounded && dinf ) ? 0.0 : ( xsc != 0.0 ? exp( -xsc * dexit ) : 1.0 );
-      // sampleRandDists (NCMMC_Utils.cc:153-176)
-      ncgb_rng rng;
-      ncgb_rng_init( &rng, eng.seed, a.id[i], step, kStreamEngine );
-      const double r = rand01( rng );
-      double ds;
-      if ( xs == 0.0 )
-        ds = infd();
-      else if ( dinf )
-        ds = log( r ) / ( -xs );
-      else
-        ds = ( -1.0 / xs ) * log( 1.0 + r * expm1( -xs * dexit ) );
-      // the part that scatters: roulette, attenuation, move to the point
       bool keep = false;
-      double wk = 0.0;
-      if ( w != 0.0 && finited( ds ) && xs > 0.0 ) {
-        double rf = 1.0;
-        keep = true;
-        if ( nscat >= eng.nscatthr && w < eng.wthr ) {
-          if ( rand01( rng ) > eng.psurv )
-            keep = false;
-          else
-            rf = eng.boost;
+      double wk = 0.0, wt = 0.0, ds = 0.0;
+      if ( on ) {
+        const double dexit = distExit( g, p, u );
+        const bool dinf = !finited( dexit );
+        // absorption (evalManyXSIsotropic of AbsOOV) and scattering (the
+        // cached value unless new or changed) macroscopic cross-sections
+        const double xabs = eng.has_abs ? eng.macro * absXS( eng.abs_c, e ) : 0.0;
+        if ( !eng.has_scat || eng.nscatlimit == 0 || ( eng.nscatlimit > 0 && nscat >= eng.nscatlimit ) ) {
+          xs = 0.0;
+        } else if ( nscat <= 0 || xs < 0.0 ) {
+          double x = 0.0;
+          if ( contains( m.dom_elow, m.dom_ehigh, e ) ) {
+            ncgb_rng dummy;
+            ncgb_rng_init( &dummy, 0, 0, 0, 0 );
+            x = xsAndPick<false, Fast>( m, e, dummy ).xs;
+          }
+          xs = eng.macro * x;
         }
-        if ( keep ) {
-          const double wr = exp( -xabs * ds );
-          keep = wr > 0.0;
-          wk = w * rf * wr * ( 1.0 - ptransm );
+        // calcProbTransm (NCMMC_Utils.cc:46-88): 0 for an infinite path
+        const double xsc = fmin( kDblMax, xs );
+        const double ptransm = ( g.unbounded && dinf ) ? 0.0 : ( xsc != 0.0 ? exp( -xsc * dexit ) : 1.0 );
+        // sampleRandDists (NCMMC_Utils.cc:153-176)
+        ncgb_rng rng;
+        ncgb_rng_init( &rng, eng.seed, id, step, kStreamEngine );
+        const double r = rand01( rng );
+        if ( xs == 0.0 )
+          ds = infd();
+        else if ( dinf )
+          ds = log( r ) / ( -xs );
+        else
+          ds = ( -1.0 / xs ) * log( 1.0 + r * expm1( -xs * dexit ) );
+        // the part that scatters: roulette, attenuation, move to the point
+        if ( w != 0.0 && finited( ds ) && xs > 0.0 ) {
+          double rf = 1.0;
+          keep = true;
+          if ( nscat >= eng.nscatthr && w < eng.wthr ) {
+            if ( rand01( rng ) > eng.psurv )
+              keep = false;
+            else
+              rf = eng.boost;
+          }
+          if ( keep ) {
+            const double wr = exp( -xabs * ds );
+            keep = wr > 0.0;
+            wk = w * rf * wr * ( 1.0 - ptransm );
+          }
         }
+        // the transmitted part, at the exit (propagateAndAttenuate, then the
+        // scatter-process transmission), is tallied
+        double pabs;
+        if ( eng.has_abs ) {
+          const double xa = fmin( kDblMax, xabs );
+          pabs = ( g.unbounded && dinf ) ? 0.0 : ( xa != 0.0 ? exp( -xa * dexit ) : 1.0 );
+        } else {
+          pabs = ( g.unbounded && dinf ) ? 0.0 : 1.0;
+        }
+        wt = w * pabs * ptransm;
       }
       const unsigned long long slot = appendSlot( &c->n_b, keep );
       if ( keep ) {
@@ -521,27 +641,14 @@ namespace {
         b.xs[j] = xs;
         b.nscat[j] = nscat;
         b.ninel[j] = ninel;
-        b.id[j] = a.id[i];
-        b.e0[j] = a.e0[i];
-        b.d0[3 * j] = a.d0[3 * i]; b.d0[3 * j + 1] = a.d0[3 * i + 1]; b.d0[3 * j + 2] = a.d0[3 * i + 2];
+        b.id[j] = id;
+        b.e0[j] = e0;
+        b.d0[3 * j] = d0[0]; b.d0[3 * j + 1] = d0[1]; b.d0[3 * j + 2] = d0[2];
       }
-      // the transmitted part, at the exit (propagateAndAttenuate, then the
-      // scatter-process transmission), is tallied
-      double pabs;
-      if ( eng.has_abs ) {
-        const double xa = fmin( kDblMax, xabs );
-        pabs = ( g.unbounded && dinf ) ? 0.0 : ( xa != 0.0 ? exp( -xa * dexit ) : 1.0 );
-      } else {
-        pabs = ( g.unbounded && dinf ) ? 0.0 : 1.0;
-      }
-      const double wt = w * pabs * ptransm;
-      const double d0[3] = { a.d0[3 * i], a.d0[3 * i + 1], a.d0[3 * i + 2] };
-      tallyNeutron( tb, t, e, u, wt, nscat, ninel, a.e0[i], d0 );
-      atomicAdd( &tal.n, 1ull );
-      atomicAdd( &tal.w, wt );
+      tallyWarp( tb, scr, t, on, e, u, wt, nscat, ninel, e0, d0 );
+      addCount( &tal, on, wt );
     }
-    if ( smem )
-      tallyFlushShared( sh, t );
+    tallyFlushShared( sh, t, bins_smem );
     __syncthreads();
     if ( threadIdx.x == 0 && tal.n ) {
       atomicAdd( &c->tallied, tal.n );
@@ -559,13 +666,46 @@ namespace {
 namespace ncgb {
   namespace mmc {
 
+    // Bins in shared memory when the whole buffer fits in the budget
+    // (NCGB_MMC_SMEM_KB, default 96 KB: two 256-thread blocks per SM for the
+    // five default-sized tallies); the statistics always.
+    static std::size_t smemBudget()
+    {
+      static std::size_t b = [] {
+        const char* v = std::getenv( "NCGB_MMC_SMEM_KB" );
+        const long kb = v ? std::atol( v ) : 96;
+        return (std::size_t)( kb > 0 && kb <= 220 ? kb : 96 ) * 1024;
+      }();
+      return b;
+    }
+
+    template<class K>
+    static cudaError_t allowSmem( K kernel, std::size_t bytes )
+    {
+      if ( bytes <= 48 * 1024 )
+        return cudaSuccess;
+      return cudaFuncSetAttribute( kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes );
+    }
+
+    static std::size_t tallySmem( const Tally& t, bool& bins )
+    {
+      bins = (std::size_t)t.nbuf * sizeof(double) <= smemBudget();
+      return (std::size_t)( bins ? t.nbuf : t.nstat ) * sizeof(double);
+    }
+
     cudaError_t launchEmit( const Source& src, const Geom& g, const Engine& eng, const Tally& t, Pop a,
                             uint64_t base, uint64_t first_id, uint64_t count, Counters* c, int numSMs,
                             cudaStream_t s )
     {
       if ( count == 0 )
         return cudaSuccess;
-      k_mmc_emit<<<gridFor( count, 256, numSMs * 8 ), 256, 0, s>>>( src, g, eng, t, a, base, first_id, count, c );
+      bool bins = false;
+      const std::size_t sbytes = tallySmem( t, bins );
+      cudaError_t e = allowSmem( k_mmc_emit, sbytes );
+      if ( e != cudaSuccess )
+        return e;
+      k_mmc_emit<<<gridFor( count, kBlock, numSMs * 4 ), kBlock, sbytes, s>>>( src, g, eng, t, a, base, first_id,
+                                                                             count, c, bins ? 1 : 0 );
       return cudaGetLastError();
     }
 
@@ -575,15 +715,20 @@ namespace ncgb {
     {
       if ( n_a == 0 )
         return cudaSuccess;
-      // block-local tallies in shared memory when they fit
-      const std::size_t sbytes = (std::size_t)t.nbuf * sizeof(double);
-      const bool smem = sbytes <= 48 * 1024;
-      const int grid = gridFor( n_a, 256, numSMs * 4 );
-      if ( eng.fast )
-        k_mmc_transport<true><<<grid, 256, smem ? sbytes : 0, s>>>( m, g, eng, t, a, n_a, b, step, c, smem ? 1 : 0 );
-      else
-        k_mmc_transport<false><<<grid, 256, smem ? sbytes : 0, s>>>( m, g, eng, t, a, n_a, b, step, c, smem ? 1 : 0 );
-      return cudaGetLastError();
+      bool bins = false;
+      const std::size_t sbytes = tallySmem( t, bins );
+      const int grid = gridFor( n_a, kBlock, numSMs * 4 );
+      cudaError_t e;
+      if ( eng.fast ) {
+        e = allowSmem( k_mmc_transport<true>, sbytes );
+        if ( e == cudaSuccess )
+          k_mmc_transport<true><<<grid, kBlock, sbytes, s>>>( m, g, eng, t, a, n_a, b, step, c, bins ? 1 : 0 );
+      } else {
+        e = allowSmem( k_mmc_transport<false>, sbytes );
+        if ( e == cudaSuccess )
+          k_mmc_transport<false><<<grid, kBlock, sbytes, s>>>( m, g, eng, t, a, n_a, b, step, c, bins ? 1 : 0 );
+      }
+      return e != cudaSuccess ? e : cudaGetLastError();
     }
   }
 }

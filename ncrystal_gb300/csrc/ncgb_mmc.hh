@@ -67,10 +67,12 @@ namespace ncgb {
 
     // Tallies (NCMMC_StdTallies.cc).  Histogram k has 6 groups (total and
     // the five breakdowns NOSCAT, SINGLESCAT_ELAS, SINGLESCAT_INELAS,
-    // MULTISCAT_PUREELAS, MULTISCAT_OTHER) of nbins+2 bins (underflow first,
-    // overflow last), each bin [content, error^2]; then per group the running
-    // statistics [sum w, sum w x, sum w x^2, min key, max key] (keys: doubles
-    // mapped to order-preserving int64).
+    // MULTISCAT_PUREELAS, MULTISCAT_OTHER), each with running statistics
+    // [sum w, sum w x, sum w x^2, min key, max key] (keys: doubles mapped to
+    // order-preserving int64) and nbins+2 bins (underflow first, overflow
+    // last) of [content, error^2].  The buffer holds all statistics first
+    // (nstat doubles), then all bins, so that kernels can keep the statistics
+    // in shared memory even when the bins do not fit there.
     enum TallyKind : int32_t { T_THETA = 0, T_MU, T_NSCAT, T_NSCAT_UW, T_W, T_E, T_L, T_DE, T_Q, T_N };
     constexpr int kGroups = 6;
     constexpr int kStats = 5;
@@ -79,7 +81,7 @@ namespace ncgb {
       int32_t enabled, nbins;
       double xmin, xmax, inv_delta;
       int64_t off;             // first double of this histogram's bins in the tally buffer
-      int64_t soff;            // first double of its statistics
+      int64_t soff;            // first double of its statistics (< nstat)
     };
 
     struct Tally {
@@ -89,6 +91,7 @@ namespace ncgb {
       int32_t fixed_e;         // use e0 as the incoming energy
       int32_t pad;
       double d0x, d0y, d0z, e0;
+      int64_t nstat;           // doubles of statistics at the start of the buffer
       int64_t nbuf;            // doubles in the tally buffer
       double* buf;             // device
     };
