@@ -26,8 +26,12 @@ throughout (the reference's results to rounding).
   e2e    -- the same through the C ABI with host (pinned) arrays, copies
             inside the timed region
 
+minimc: the reference's MiniMC run on the device (1e7 histories per step,
+polyethylene sphere, pencil beam), metric histories/s, CPU baseline the
+oracle's MiniMC engine.
+
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-       [--workload pe|al2o3_large|al_small|crystal_batch|mixed_batch]
+       [--workload pe|al2o3_large|al_small|crystal_batch|mixed_batch|minimc]
        [--mode mixed|exact] [--sampler auto|plain|learned]
 Under torchrun (N>1) each rank runs an independent replica on its own GPU
 (the path has no cross-neutron exchange: replicas only) and rank 0 prints the
@@ -89,7 +93,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="pe",
-                    choices=["pe", "al2o3_large", "al_small", "crystal_batch", "mixed_batch"])
+                    choices=["pe", "al2o3_large", "al_small", "crystal_batch", "mixed_batch", "minimc"])
     ap.add_argument("--sampler", default="auto", choices=["auto", "plain", "learned"],
                     help="S(alpha,beta) beta sampling: plain percentile inversion, or the learned proposal "
                          "(trained on the GPU before timing; the plain sampler is timed beside it). "
@@ -570,8 +574,200 @@ def run_gb300(args):
     return 0
 
 
+# ---- MiniMC workload -------------------------------------------------------------------
+# The reference's MiniMC on a polyethylene sphere (r = 1 cm) under a pencil
+# beam of 0.0253 eV neutrons, 1e7 histories per step, tallies theta, mu, e,
+# nscat, w with breakdowns (the query of tests/golden/mmc_pe_sphere.npz).
+MMC_METRIC = "MiniMC neutron histories/s on 1 GB300 (polyethylene sphere r=1cm, pencil beam 0.0253 eV)"
+MMC_UNIT = "histories/s"
+MMC_GEOM = "sphere;r=0.01"
+MMC_ENGINE = "seed=11;tally=theta,mu,e,nscat,w"
+MMC_N = 10000000
+MMC_ENERGY = 0.0253
+# algorithmic bytes: a transported neutron reads its state (position,
+# direction, pending scatter result, energy, weight, cached xs, counters,
+# stream key, initial energy and direction: 128 B) and, when it goes on to a
+# collision, writes it to the next population (116 B); a collision reads
+# energy, direction and stream key (36 B) and writes E', direction, status (36 B)
+MMC_BYTES_READ, MMC_BYTES_WRITE, MMC_BYTES_SCATTER = 128, 116, 72
+
+
+def mmc_src(n):
+    return "constant;ekin=%g;z=-0.01;n=%d" % (MMC_ENERGY, n)
+
+
+def mmc_cpu_baseline(seconds, threads=None):
+    """The oracle's CPU MiniMC engine (oracle/ncgb_oracle_mmc.c, pinned to the
+    reference's MiniMC by tests/test_oracle_mmc.py) on this host's cores, on
+    a bounded number of histories of the same query."""
+    import ncrystal_gb300._build as B
+    import ncrystal_gb300.minimc as M
+    import ncrystal_gb300.workloads as W
+    from ncrystal_gb300.bundle.reader import read_bundle
+    from oracle import pyoracle as P
+    threads = threads or os.cpu_count() or 1
+    path = os.path.join(B.BUNDLES, B.bundle_file_name(W.PE293))
+    geom = M.decode_cfgstr(MMC_GEOM, "geom")["decoded"]
+    src = M.decode_cfgstr(mmc_src(1000), "src")["decoded"]
+    src["energy_ev"] = MMC_ENERGY
+    eng = M.decode_cfgstr(MMC_ENGINE, "engine")["decoded"]
+    bins = {"theta": (180, 0.0, 180.0), "mu": (200, -1.0, 1.0), "e": (200, 0.0, 0.5), "nscat": (22, -1.5, 20.5),
+            "w": (200, 0.0, 1.0)}
+    m = P.HostMaterial(path)
+    c, nstat, nbuf = P.mmc_config(m, read_bundle(path), geom, src, eng, bins, seed=11)
+    t0 = time.perf_counter()
+    P.mmc_run(m, c, nbuf, 0, 2000, threads=1)
+    rate1 = 2000 / max(time.perf_counter() - t0, 1e-6)
+    n = int(min(MMC_N, max(threads * 1000, rate1 * threads * seconds)))
+    t0 = time.perf_counter()
+    _, cnt = P.mmc_run(m, c, nbuf, 0, n, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": MMC_UNIT, "cores": threads, "kind": "port",
+            "sample": "%d histories of the same query (%.3g neutron-steps), %d threads, %.1f s"
+                      % (n, cnt[5], threads, dt)}
+
+
+def run_minimc_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import __graft_entry__
+    __graft_entry__.build()
+    vals, base = [], None
+    per_step = max(1.0, 60.0 / max(1, args.steps + args.warmup))
+    for i in range(args.warmup + args.steps):
+        b = mmc_cpu_baseline(min(per_step, args.cpu_seconds))
+        if i >= args.warmup:
+            vals.append(b["value"])
+            base = b
+    v = statistics.median(vals)
+    base["value"] = v
+    line = {"metric": MMC_METRIC, "value": v, "unit": MMC_UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "minimc", "cfg": "Polyethylene_CH2.ncmat;temp=293K", "geomcfg": MMC_GEOM,
+                       "srccfg": mmc_src(MMC_N), "enginecfg": MMC_ENGINE, "parallelism": "replicas1"},
+            "impl": "reference", "cpu_baseline": base,
+            "e2e": {"value": v, "unit": MMC_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_minimc(args):
+    """value: histories per second of device time (CUDA events around the
+    engine's step loop on its stream); e2e: the same runs through the C ABI
+    call (ncgb_mmc_run: cfg strings in, the results document out), wall
+    clock.  Each step is one complete MiniMC run of 1e7 histories; the tally
+    histograms stay in shared memory / L2, the population (2 x 8.4M neutrons,
+    ~2.8 GB) is far larger than L2."""
+    import torch
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__
+    if rank == 0 or world == 1:
+        __graft_entry__.build()
+    if dist:
+        dist.barrier()
+        __graft_entry__.build()
+    import ncrystal_gb300 as NC
+    import ncrystal_gb300.workloads as W
+    dev = torch.device("cuda", local)
+    sc = NC.createScatter(W.PE293, seed=11 + rank)
+    sc.set_mode(args.mode)
+    src = mmc_src(MMC_N)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        sc.minimc_run(MMC_GEOM, src, MMC_ENGINE)
+    # kernel shares (phase timing on; one untimed run)
+    NC.phase_times()
+    NC.phase_timing(True)
+    res = sc.minimc_run(MMC_GEOM, src, MMC_ENGINE)
+    NC.phase_timing(False)
+    ms_pick, ms_sab, nbatches, _ = NC.phase_times()
+    devmd = res["output"]["metadata"]["device"]
+    barrier()
+    secs = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            r = sc.minimc_run(MMC_GEOM, src, MMC_ENGINE)
+            secs.append(r["output"]["metadata"]["device"]["seconds"])
+        barrier()
+    dev_s = max_over_ranks(sum(secs), dist, dev)
+    value = world * MMC_N * args.steps / dev_s
+    # e2e: the C ABI call, wall clock (cfg strings in, JSON document out)
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(e2e_steps):
+        r = sc.minimc_run(MMC_GEOM, src, MMC_ENGINE)
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    nbuf = sum(6 * (t["total"]["bindata"]["nbins"] + 2) * 2 + 30 for t in r["output"]["tally"].values())
+    e2e = {"value": world * MMC_N * e2e_steps / e2e_s, "unit": MMC_UNIT, "steps": e2e_steps,
+           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": nbuf * 8 + 64,
+           "api": "ncgb_mmc_run (C ABI; cfg strings in, results JSON out)"}
+    # roofline of the dominant kernel (algorithmic bytes per launch over the
+    # launch's CUDA-event time)
+    peak, peak_kind = measured_peaks()
+    nst = devmd["neutron_steps"]
+    launches = max(1, devmd["transport_launches"])
+    t_tr = devmd["transport_ms"] / launches / 1e3
+    nscat = nst - MMC_N
+    bytes_tr = (MMC_BYTES_READ * nst + MMC_BYTES_WRITE * nscat) / launches
+    nb = max(1, nbatches)
+    t_pick, t_sab = ms_pick / nb / 1e3, ms_sab / nb / 1e3
+    bytes_sc = MMC_BYTES_SCATTER * nscat / nb
+    tot = t_tr + t_pick + t_sab
+    kernels = {
+        "k_mmc_transport": {"ms_per_launch": t_tr * 1e3, "launches": launches, "bytes_per_launch": bytes_tr,
+                            "achieved_gbs": bytes_tr / t_tr / 1e9 if t_tr else None,
+                            "share": t_tr / tot if tot else None},
+        "k_pick": {"ms_per_launch": t_pick * 1e3, "launches": nb, "bytes_per_launch": bytes_sc,
+                   "share": t_pick / tot if tot else None},
+        "k_sab": {"ms_per_launch": t_sab * 1e3, "launches": nb, "share": t_sab / tot if tot else None},
+    }
+    achieved = kernels["k_mmc_transport"]["achieved_gbs"]
+    if rank == 0:
+        base = mmc_cpu_baseline(args.cpu_seconds)
+        line = {
+            "metric": MMC_METRIC, "value": value, "unit": MMC_UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.mode == "exact" else "f64+f32",
+            "data": "synthetic",
+            "config": {"workload": "minimc", "cfg": W.PE293, "geomcfg": MMC_GEOM, "srccfg": src,
+                       "enginecfg": MMC_ENGINE, "mode": args.mode, "parallelism": "replicas%d" % world,
+                       "neutron_steps_per_run": nst, "engine_steps_per_run": devmd["steps"],
+                       "l2": "population 2 x 2^23 neutrons (~2.8 GB) > L2; tallies block-local in shared memory"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
+                         "traffic": profiled_traffic("k_mmc_transport", "minimc"), "kernel": "k_mmc_transport",
+                         "kernels": kernels,
+                         "note": "latency / FP64 bound (warp reductions of the tally statistics), not HBM bound"},
+            "cpu_baseline": base,
+            "e2e": e2e,
+            "clocks": clk.summary(),
+            "gpu_launches": args.steps * (launches + 2 * nb + 1),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "minimc":
+        return run_minimc_reference(args) if args.impl == "reference" else run_minimc(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

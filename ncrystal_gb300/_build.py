@@ -112,12 +112,12 @@ def build_library(force=False, verbose=False):
 def build_oracle(force=False):
     """Compile the CPU oracle (test infrastructure)."""
     os.makedirs(ORACLE_BUILD, exist_ok=True)
-    src = os.path.join(ORACLE, "ncgb_oracle.c")
+    srcs = [os.path.join(ORACLE, "ncgb_oracle.c"), os.path.join(ORACLE, "ncgb_oracle_mmc.c")]
     out = oracle_path()
-    deps = [src, os.path.join(INC, "ncgb_philox.h"), os.path.join(INC, "ncgb_tables.h")]
+    deps = srcs + [os.path.join(INC, "ncgb_philox.h"), os.path.join(INC, "ncgb_tables.h")]
     if force or not _newer(out, deps):
-        _run(["gcc", "-std=c99", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-I" + INC,
-              "-o", out, src, "-lm"])
+        _run(["gcc", "-std=gnu99", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-I" + INC,
+              "-o", out] + srcs + ["-lm"])
     return out
 
 

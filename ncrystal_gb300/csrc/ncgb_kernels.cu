@@ -549,6 +549,8 @@ namespace ncgb {
 
   int scatterLaunchesPerBatch() { return 2; }
 
+  bool phaseTiming() { return g_timing; }
+
   void setPhaseTiming( bool on )
   {
     std::lock_guard<std::mutex> lock( g_evmtx );

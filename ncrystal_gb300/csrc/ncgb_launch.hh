@@ -83,6 +83,7 @@ namespace ncgb {
   cudaError_t launchXS( const ncgb_material_view& m, const Batch& b, uint64_t repeat, cudaStream_t s );
   int scatterLaunchesPerBatch();
   void setPhaseTiming( bool on );
+  bool phaseTiming();
   int takePhaseTimes( double* ms_pick, double* ms_sab, unsigned long* nbatches );
 }
 

@@ -1067,7 +1067,14 @@ namespace {
     Counters c;
     uint64_t steps = 0;
     double seconds = 0;
+    // with phase timing on (ncgb_phase_timing): transport kernel time and
+    // launches (the scatter kernels' times go to ncgb_phase_times)
+    double transport_ms = 0;
+    uint64_t transport_launches = 0;
+    uint64_t neutron_steps = 0;     // transported neutrons summed over steps
   };
+
+  void formTotals( const Tally& t, std::vector<double>& buf );
 
   // The step loop (StdSimEngine::step / SimMgr, NCMMC_SimEngine.cc:151-165).
   RunResult runEngine( const HandleInfo& hi, const GeomCfg& gc, const SrcCfg& sc, const EngineCfg& ec, Tally t,
@@ -1138,6 +1145,14 @@ namespace {
     Pop A = pa.pop, B = pb.pop;
     uint64_t nA = 0, emitted = 0;
     uint32_t step = 0;
+    const bool timing = ncgb::phaseTiming();
+    cudaEvent_t te0 = nullptr, te1 = nullptr;
+    if ( timing ) {
+      cudaEventCreate( &te0 );
+      cudaEventCreate( &te1 );
+    }
+    double transport_ms = 0;
+    uint64_t transport_launches = 0, neutron_steps = 0;
     const uint32_t kMaxSteps = 100000000u;
     for ( ;; ) {
       if ( emitted < sc.n && nA < cap ) {
@@ -1155,9 +1170,20 @@ namespace {
         continue;
       }
       checkCuda( cudaMemsetAsync( &dc->n_b, 0, sizeof(unsigned long long), st ), "memset" );
+      if ( timing )
+        cudaEventRecord( te0, st );
       checkCuda( launchTransport( hi.view, gc.g, eng, t, A, nA, B, step, dc, nsm, st ), "k_mmc_transport" );
+      if ( timing )
+        cudaEventRecord( te1, st );
       checkCuda( cudaMemcpyAsync( hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost, st ), "D2H" );
       checkCuda( cudaStreamSynchronize( st ), "k_mmc_transport" );
+      if ( timing ) {
+        float ms = 0;
+        cudaEventElapsedTime( &ms, te0, te1 );
+        transport_ms += ms;
+        ++transport_launches;
+      }
+      neutron_steps += nA;
       if ( hc->nfail )
         throw MmcError( "CalcError", "MiniMC: " + std::to_string( hc->nfail ) + " scatter(s) failed (a rejection"
                         " loop reached its limit of attempts)" );
@@ -1197,9 +1223,17 @@ namespace {
     cudaEventElapsedTime( &ms, ev0, ev1 );
     cudaEventDestroy( ev0 );
     cudaEventDestroy( ev1 );
+    formTotals( t, r.tally );
     r.c = *hc;
     r.steps = step;
     r.seconds = ms * 1e-3;
+    r.transport_ms = transport_ms;
+    r.transport_launches = transport_launches;
+    r.neutron_steps = neutron_steps;
+    if ( timing ) {
+      cudaEventDestroy( te0 );
+      cudaEventDestroy( te1 );
+    }
     return r;
   }
 
@@ -1216,6 +1250,44 @@ namespace {
     double v;
     std::memcpy( &v, &k, 8 );
     return v;
+  }
+
+  // With breakdowns the kernels fill only the five category groups; the
+  // total group (0) is formed here: bins and sums added, extremes combined.
+  void formTotals( const Tally& t, std::vector<double>& buf )
+  {
+    if ( !t.breakdown )
+      return;
+    for ( int k = 0; k < T_N; ++k ) {
+      const TallyHist& h = t.h[k];
+      if ( !h.enabled )
+        continue;
+      const int64_t nb2 = (int64_t)( h.nbins + 2 ) * 2;
+      double* b0 = buf.data() + h.off;
+      for ( int64_t i = 0; i < nb2; ++i ) {
+        double v = 0.0;
+        for ( int g = 1; g < kGroups; ++g )
+          v += b0[g * nb2 + i];
+        b0[i] = v;
+      }
+      double* s0 = buf.data() + h.soff;
+      long long mn = 0x7FFFFFFFFFFFFFFFLL, mx = (long long)0x8000000000000000ULL;
+      for ( int j = 0; j < 3; ++j ) {
+        double v = 0.0;
+        for ( int g = 1; g < kGroups; ++g )
+          v += s0[g * kStats + j];
+        s0[j] = v;
+      }
+      for ( int g = 1; g < kGroups; ++g ) {
+        long long a, b;
+        std::memcpy( &a, &s0[g * kStats + 3], 8 );
+        std::memcpy( &b, &s0[g * kStats + 4], 8 );
+        mn = std::min( mn, a );
+        mx = std::max( mx, b );
+      }
+      std::memcpy( &s0[3], &mn, 8 );
+      std::memcpy( &s0[4], &mx, 8 );
+    }
   }
 
   void histJSON( std::ostream& os, const Tally& t, const std::vector<double>& buf, int k, int g, const char* title )
@@ -1285,6 +1357,9 @@ namespace {
        << "},\"miss\":{\"count\":" << r.c.miss << ",\"weight\":" << jsonNum( r.c.miss_w )
        << "},\"tallied\":{\"count\":" << r.c.tallied << ",\"weight\":" << jsonNum( r.c.tallied_w )
        << "},\"device\":{\"steps\":" << r.steps << ",\"seconds\":" << jsonNum( r.seconds )
+       << ",\"neutron_steps\":" << r.neutron_steps << ",\"transport_ms\":"
+       << ( r.transport_launches ? jsonNum( r.transport_ms ) : std::string( "null" ) )
+       << ",\"transport_launches\":" << r.transport_launches
        << ",\"mode\":" << ( hi.mode == NCGB_MODE_MIXED ? "\"mixed\"" : "\"exact\"" ) << "}}}}";
     return os.str();
   }

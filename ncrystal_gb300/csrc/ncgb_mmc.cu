@@ -210,40 +210,16 @@ namespace {
     return 1 + ( f >= (double)h.nbins ? h.nbins : (int)f );
   }
 
-  // Warp-aggregated bin update: lanes filling the same (group, bin) sum
-  // their weights through the warp's scratch, and the lowest of them adds the
-  // sums with one atomic pair.
-  // Called by all 32 lanes.
-  __device__ __forceinline__ void addBins( double* buf, double* scr, const TallyHist& h, int g, int bin, double wt,
-                                           bool f )
+  // Bin update: one shared-memory (or global) atomic pair per lane.  Lanes
+  // of a warp that hit the same bin serialise in the atomic unit, which is
+  // cheaper than aggregating them on the narrow FP64 pipe first.
+  __device__ __forceinline__ void addBins( double* buf, const TallyHist& h, int g, int bin, double wt, bool f )
   {
-    const int lane = threadIdx.x & 31;
-    const unsigned key = f ? (unsigned)( g * ( h.nbins + 2 ) + bin ) : 0xffffffffu;
-    const unsigned peers = __match_any_sync( kFull, key );
-    double* b = buf + h.off + ( f ? (int64_t)key * 2 : 0 );
-    if ( __all_sync( kFull, __popc( peers ) == 1 ) ) {
-      if ( f ) {
-        atomicAdd( b, wt );
-        atomicAdd( b + 1, wt * wt );
-      }
-      return;
+    if ( f ) {
+      double* b = buf + h.off + ( (int64_t)g * ( h.nbins + 2 ) + bin ) * 2;
+      atomicAdd( b, wt );
+      atomicAdd( b + 1, wt * wt );
     }
-    scr[lane] = f ? wt : 0.0;
-    scr[32 + lane] = f ? wt * wt : 0.0;
-    __syncwarp();
-    if ( f && __ffs( peers ) - 1 == lane ) {
-      double c = 0.0, c2 = 0.0;
-      unsigned m = peers;
-      while ( m ) {
-        const int j = __ffs( m ) - 1;
-        m &= m - 1;
-        c += scr[j];
-        c2 += scr[32 + j];
-      }
-      atomicAdd( b, c );
-      atomicAdd( b + 1, c2 );
-    }
-    __syncwarp();
   }
 
   // Warp reduction of one group's running statistics (RunningStats1D,
@@ -283,8 +259,10 @@ namespace {
     double* bins;
   };
 
-  __device__ void histFillWarp( const TallyDst& d, double* scr, const Tally& t, int kind, int cat, double x,
-                                double w, bool weighted, bool on )
+  // With breakdowns only the five category groups are filled: the host
+  // forms the total as their sum (bins, sums) and extremes.
+  __device__ void histFillWarp( const TallyDst& d, const Tally& t, int kind, int cat, double x, double w,
+                                bool weighted, bool on )
   {
     const TallyHist& h = t.h[kind];
     const bool f = on && ( !weighted || w > 0.0 );
@@ -292,19 +270,21 @@ namespace {
       return;
     const double wt = weighted ? w : 1.0;
     const int bin = f ? binOf( h, x ) : 0;
-    addBins( d.bins, scr, h, 0, bin, wt, f );
-    addStats( d.stats + h.soff, x, wt, f );
-    if ( t.breakdown ) {
-      addBins( d.bins, scr, h, 1 + cat, bin, wt, f );
-      for ( int c = 0; c < kGroups - 1; ++c )
-        if ( __any_sync( kFull, f && cat == c ) )
-          addStats( d.stats + h.soff + ( 1 + c ) * kStats, x, wt, f && cat == c );
+    if ( !t.breakdown ) {
+      addBins( d.bins, h, 0, bin, wt, f );
+      addStats( d.stats + h.soff, x, wt, f );
+      return;
     }
+    addBins( d.bins, h, 1 + cat, bin, wt, f );
+    for ( int c = 0; c < kGroups - 1; ++c )
+      if ( __any_sync( kFull, f && cat == c ) )
+        addStats( d.stats + h.soff + ( 1 + c ) * kStats, x, wt, f && cat == c );
   }
 
   // tallyRecord (NCMMC_StdTallies.cc:430-660) for the warp's neutrons ('on'
   // lanes).  Called by all 32 lanes.
-  __device__ void tallyWarp( const TallyDst& buf, double* scr, const Tally& t, bool on, double e, const double* u, double w,
+  template<bool Fast>
+  __device__ void tallyWarp( const TallyDst& buf, const Tally& t, bool on, double e, const double* u, double w,
                              int nscat, int ninel, double e0, const double* d0 )
   {
     // init_dethistidvect, NCMMC_StdTallies.cc:288-308
@@ -321,29 +301,30 @@ namespace {
         mu = __dadd_rn( __dadd_rn( __dmul_rn( d0[0], u[0] ), __dmul_rn( d0[1], u[1] ) ), __dmul_rn( d0[2], u[2] ) );
       mu = clampd( mu, -1.0, 1.0 );
       if ( t.h[T_MU].enabled )
-        histFillWarp( buf, scr, t, T_MU, cat, mu, w, true, on );
+        histFillWarp( buf, t, T_MU, cat, mu, w, true, on );
       if ( t.h[T_Q].enabled ) {
         const double ei = t.fixed_e ? t.e0 : e0;
         const double q2 = __dmul_rn( __dadd_rn( __dadd_rn( __dmul_rn( __dmul_rn( sqrt( __dmul_rn( e, ei ) ), mu ), -2.0 ),
                                                            ei ), e ), kEkin2Ksq );
-        histFillWarp( buf, scr, t, T_Q, cat, sqrt( maxd( 0.0, q2 ) ), w, true, on );
+        histFillWarp( buf, t, T_Q, cat, sqrt( maxd( 0.0, q2 ) ), w, true, on );
       }
       if ( t.h[T_THETA].enabled )
-        histFillWarp( buf, scr, t, T_THETA, cat, acos( mu ) * kToDeg, w, true, on );
+        histFillWarp( buf, t, T_THETA, cat, Fast ? (double)( acosf( (float)mu ) * (float)kToDeg ) : acos( mu ) * kToDeg,
+                      w, true, on );
     }
     if ( t.h[T_E].enabled )
-      histFillWarp( buf, scr, t, T_E, cat, e, w, true, on );
+      histFillWarp( buf, t, T_E, cat, e, w, true, on );
     if ( t.h[T_DE].enabled )
-      histFillWarp( buf, scr, t, T_DE, cat, ( t.fixed_e ? t.e0 : e0 ) - e, w, true, on );
+      histFillWarp( buf, t, T_DE, cat, ( t.fixed_e ? t.e0 : e0 ) - e, w, true, on );
     if ( t.h[T_L].enabled )
-      histFillWarp( buf, scr, t, T_L, cat, sqrt( kWl2Ekin ) * sqrt( 1.0 / maxd( 4.9406564584124654e-324, e ) ), w,
+      histFillWarp( buf, t, T_L, cat, sqrt( kWl2Ekin ) * sqrt( 1.0 / maxd( 4.9406564584124654e-324, e ) ), w,
                     true, on );
     if ( t.h[T_NSCAT].enabled )
-      histFillWarp( buf, scr, t, T_NSCAT, cat, (double)nscat, w, true, on );
+      histFillWarp( buf, t, T_NSCAT, cat, (double)nscat, w, true, on );
     if ( t.h[T_NSCAT_UW].enabled )
-      histFillWarp( buf, scr, t, T_NSCAT_UW, cat, (double)nscat, w, false, on );
+      histFillWarp( buf, t, T_NSCAT_UW, cat, (double)nscat, w, false, on );
     if ( t.h[T_W].enabled )
-      histFillWarp( buf, scr, t, T_W, cat, w, w, false, on );
+      histFillWarp( buf, t, T_W, cat, w, w, false, on );
   }
 
   // Block-local tallies in shared memory: the statistics always, the bins
@@ -425,7 +406,6 @@ namespace {
   }
 
   constexpr int kBlock = 256;
-  constexpr int kWarps = kBlock / 32;
 
   // Source neutrons first_id .. first_id+count-1: fillBasket of the source
   // (NCMMC_Source.cc) and BasketSrcFiller::propagateToVolume
@@ -439,8 +419,6 @@ namespace {
   {
     extern __shared__ double sh[];
     __shared__ BlockSums miss, tal;
-    __shared__ double scratch[kWarps][64];
-    double* scr = scratch[threadIdx.x >> 5];
     const TallyDst tb{ sh, bins_smem ? sh : t.buf };
     tallyInitShared( sh, t, bins_smem );
     if ( threadIdx.x == 0 ) { miss.n = 0; miss.w = 0.0; tal.n = 0; tal.w = 0.0; }
@@ -488,7 +466,7 @@ namespace {
       addCount( &miss, missed, 1.0 );
       const bool tally_miss = missed && !eng.ignore_miss;
       if ( __any_sync( kFull, tally_miss ) ) {
-        tallyWarp( tb, scr, t, tally_miss, e, u, 1.0, -1, 0, e, u );
+        tallyWarp<false>( tb, t, tally_miss, e, u, 1.0, -1, 0, e, u );
         addCount( &tal, tally_miss, 1.0 );
       }
       const unsigned long long slot = appendSlot( &c->n_a, keep );
@@ -530,8 +508,6 @@ namespace {
   {
     extern __shared__ double sh[];
     __shared__ BlockSums tal;
-    __shared__ double scratch[kWarps][64];
-    double* scr = scratch[threadIdx.x >> 5];
     const TallyDst tb{ sh, bins_smem ? sh : t.buf };
     tallyInitShared( sh, t, bins_smem );
     if ( threadIdx.x == 0 ) { tal.n = 0; tal.w = 0.0; }
@@ -589,17 +565,24 @@ namespace {
           }
           xs = eng.macro * x;
         }
-        // calcProbTransm (NCMMC_Utils.cc:46-88): 0 for an infinite path
+        // calcProbTransm (NCMMC_Utils.cc:46-88): 0 for an infinite path.
+        // The mixed mode takes the attenuation factors and the sampled
+        // distance in FP32 (relative 1e-7 of a weight or a path length).
         const double xsc = fmin( kDblMax, xs );
-        const double ptransm = ( g.unbounded && dinf ) ? 0.0 : ( xsc != 0.0 ? exp( -xsc * dexit ) : 1.0 );
-        // sampleRandDists (NCMMC_Utils.cc:153-176)
+        const double ptransm = ( g.unbounded && dinf ) ? 0.0
+                             : ( xsc != 0.0 ? ( Fast ? (double)expf( (float)( -xsc * dexit ) ) : exp( -xsc * dexit ) )
+                                            : 1.0 );
+        // sampleRandDists (NCMMC_Utils.cc:153-176); log(1 + r expm1(-t)) as
+        // log1p in the mixed mode, accurate for thin paths
         ncgb_rng rng;
         ncgb_rng_init( &rng, eng.seed, id, step, kStreamEngine );
         const double r = rand01( rng );
         if ( xs == 0.0 )
           ds = infd();
         else if ( dinf )
-          ds = log( r ) / ( -xs );
+          ds = ( Fast ? (double)logf( (float)r ) : log( r ) ) / ( -xs );
+        else if ( Fast )
+          ds = ( -1.0 / xs ) * (double)log1pf( (float)r * expm1f( (float)( -xs * dexit ) ) );
         else
           ds = ( -1.0 / xs ) * log( 1.0 + r * expm1( -xs * dexit ) );
         // the part that scatters: roulette, attenuation, move to the point
@@ -613,7 +596,7 @@ namespace {
               rf = eng.boost;
           }
           if ( keep ) {
-            const double wr = exp( -xabs * ds );
+            const double wr = Fast ? (double)expf( (float)( -xabs * ds ) ) : exp( -xabs * ds );
             keep = wr > 0.0;
             wk = w * rf * wr * ( 1.0 - ptransm );
           }
@@ -623,7 +606,8 @@ namespace {
         double pabs;
         if ( eng.has_abs ) {
           const double xa = fmin( kDblMax, xabs );
-          pabs = ( g.unbounded && dinf ) ? 0.0 : ( xa != 0.0 ? exp( -xa * dexit ) : 1.0 );
+          pabs = ( g.unbounded && dinf ) ? 0.0
+               : ( xa != 0.0 ? ( Fast ? (double)expf( (float)( -xa * dexit ) ) : exp( -xa * dexit ) ) : 1.0 );
         } else {
           pabs = ( g.unbounded && dinf ) ? 0.0 : 1.0;
         }
@@ -645,7 +629,7 @@ namespace {
         b.e0[j] = e0;
         b.d0[3 * j] = d0[0]; b.d0[3 * j + 1] = d0[1]; b.d0[3 * j + 2] = d0[2];
       }
-      tallyWarp( tb, scr, t, on, e, u, wt, nscat, ninel, e0, d0 );
+      tallyWarp<Fast>( tb, t, on, e, u, wt, nscat, ninel, e0, d0 );
       addCount( &tal, on, wt );
     }
     tallyFlushShared( sh, t, bins_smem );

@@ -1235,6 +1235,23 @@ int64_t ncgb_oracle_scatter_dir_many( const ncgb_material_view* m, const double*
   return nbad;
 }
 
+/* One neutron of ncgb_oracle_scatter_dir_many with the caller's stream
+ * (the CPU MiniMC engine, oracle/ncgb_oracle_mmc.c). */
+int ncgb_oracle_scatter_dir( const ncgb_material_view* m, ncgb_rng* rng, double ekin, const double* in,
+                             double* ef, double* out )
+{
+  double mu = 1.0;
+  if ( !ora_contains( m->dom_elow, m->dom_ehigh, ekin ) ) {
+    *ef = ekin;
+    out[0] = in[0]; out[1] = in[1]; out[2] = in[2];
+    return ORA_OK;
+  }
+  int st = ncgb_oracle_scatter( m, rng, ekin, ef, &mu );
+  if ( st == ORA_OK )
+    st = ora_rand_dir_given_mu( rng, mu, in, out );
+  return st;
+}
+
 /* AbsOOV::crossSectionIsotropic, NCAbsOOV.cc:40-44: c/sqrt(E), infinite at E = 0. */
 void ncgb_oracle_abs_xs_many( const ncgb_material_view* m, const double* ekin, int64_t n, double* out )
 {

@@ -245,3 +245,180 @@ def reference_abs_xs(cfg, ekin):
     if L.refpin_abs_xs(cfg.encode(), _P(e), len(e), _P(out)):
         raise RuntimeError("reference could not create absorption for %r" % cfg)
     return out
+
+
+# ---- CPU MiniMC engine (oracle/ncgb_oracle_mmc.c) --------------------------------------
+
+MMC_TALLIES = ["theta", "mu", "nscat", "nscat_uw", "w", "e", "l", "de", "q"]
+MMC_GROUPS = ["NOSCAT", "SINGLESCAT_ELAS", "SINGLESCAT_INELAS", "MULTISCAT_PUREELAS", "MULTISCAT_OTHER"]
+
+
+class OraMmcCfg(C.Structure):
+    _fields_ = [("geom", C.c_int32), ("unbounded", C.c_int32), ("r", C.c_double), ("dx", C.c_double),
+                ("dy", C.c_double), ("dz", C.c_double),
+                ("src", C.c_int32), ("might_be_outside", C.c_int32),
+                ("sx", C.c_double), ("sy", C.c_double), ("sz", C.c_double), ("sux", C.c_double),
+                ("suy", C.c_double), ("suz", C.c_double), ("sr", C.c_double), ("energy", C.c_double),
+                ("ax", C.c_double), ("ay", C.c_double), ("az", C.c_double), ("bx", C.c_double),
+                ("by", C.c_double), ("bz", C.c_double),
+                ("macro", C.c_double), ("abs_c", C.c_double), ("psurv", C.c_double), ("wthr", C.c_double),
+                ("nscatthr", C.c_int32), ("nscatlimit", C.c_int32), ("has_abs", C.c_int32), ("has_scat", C.c_int32),
+                ("ignore_miss", C.c_int32), ("breakdown", C.c_int32),
+                ("seed", C.c_uint64), ("scatter_seed", C.c_uint64), ("scatter_stream", C.c_uint32), ("pad", C.c_uint32),
+                ("fixed_dir", C.c_int32), ("fixed_e", C.c_int32),
+                ("d0x", C.c_double), ("d0y", C.c_double), ("d0z", C.c_double), ("e0", C.c_double),
+                ("enabled", C.c_int32 * 9), ("nbins", C.c_int32 * 9), ("xmin", C.c_double * 9),
+                ("xmax", C.c_double * 9), ("off", C.c_int64 * 9), ("soff", C.c_int64 * 9)]
+
+
+def mmc_config(material, bundle, geom, src, engine, binnings, seed=1, scatter_seed=2, scatter_stream=0):
+    """The engine's configuration from a run's decoded input (the 'decoded'
+    dicts of a MiniMC results document: geometry, source with a fixed energy
+    in eV under 'energy_ev', engine) and the tally binnings
+    {name: (nbins, xmin, xmax)}; bundle: the material's bundle records
+    (info.numdens, abs_c)."""
+    c = OraMmcCfg()
+    kinds = {"sphere": 0, "box": 1, "slab": 2, "cyl": 3}
+    c.geom = kinds[geom["name"]]
+    c.r = geom.get("r", 0.0)
+    c.dx = geom.get("dx", 0.0)
+    c.dy = geom.get("dy", 0.0)
+    c.dz = geom.get("dz", 0.0)
+    c.unbounded = int(c.geom == 2 or (c.geom == 3 and c.dy == 0.0))
+    sk = {"constant": 0, "circular": 1, "isotropic": 2}[src["name"]]
+    c.src = sk
+    c.sx, c.sy, c.sz = src.get("x", 0.0), src.get("y", 0.0), src.get("z", 0.0)
+    c.sux, c.suy, c.suz = src.get("ux", 0.0), src.get("uy", 0.0), src.get("uz", 1.0)
+    c.sr = src.get("r", 0.0)
+    c.energy = src["energy_ev"]
+    def inside(x, y, z):
+        if c.geom == 0:
+            return x * x + y * y + z * z <= c.r * c.r
+        if c.geom == 1:
+            return abs(x) <= c.dx and abs(y) <= c.dy and abs(z) <= c.dz
+        if c.geom == 2:
+            return abs(z) <= c.dz
+        return x * x + z * z <= c.r * c.r and (c.dy == 0.0 or abs(y) <= c.dy)
+    c.might_be_outside = int((sk == 1 and c.sr > 0) or not inside(c.sx, c.sy, c.sz))
+    if sk == 1 and c.sr > 0:
+        d = np.array([c.sux, c.suy, c.suz])
+        a = np.array([1.0, 0.0, 0.0])
+        if a @ d > 0.8:
+            a = np.array([0.0, 1.0, 0.0])
+        if a @ d > 0.8:
+            a = np.array([0.0, 0.0, 1.0])
+        va = np.cross(d, a); va /= np.linalg.norm(va)
+        vb = np.cross(d, va); vb /= np.linalg.norm(vb)
+        c.ax, c.ay, c.az = va * c.sr
+        c.bx, c.by, c.bz = vb * c.sr
+    nd = float(bundle["info.numdens"][0])
+    c.macro = 100.0 * nd
+    absc = float(bundle["abs_c"][0]) if "abs_c" in bundle else 0.0
+    c.has_abs = int(bool(engine.get("absorption", True)) and absc > 0.0 and c.macro > 0.0)
+    c.abs_c = absc if c.has_abs else 0.0
+    c.has_scat = int(c.macro > 0.0 and int(bundle["ncomp"][0]) > 0)
+    rl = engine.get("roulette", {"psurvival": 0.1, "weight_threshold": 0.01, "nscat_threshold": 2})
+    c.psurv, c.wthr, c.nscatthr = rl["psurvival"], rl["weight_threshold"], rl["nscat_threshold"]
+    c.nscatlimit = -1 if engine.get("nscatlimit") is None else int(engine["nscatlimit"])
+    c.ignore_miss = int(bool(engine.get("ignoremiss", False)))
+    c.breakdown = int(bool(engine.get("tallybreakdown", True)))
+    c.seed, c.scatter_seed, c.scatter_stream = seed, scatter_seed, scatter_stream
+    src_src = engine.get("tallyref", "truth") == "src"
+    if sk in (0, 1):
+        c.fixed_dir = 1
+        c.d0x, c.d0y, c.d0z = c.sux, c.suy, c.suz
+    c.fixed_e = 1
+    c.e0 = c.energy
+    del src_src
+    off = 0
+    for k, name in enumerate(MMC_TALLIES):
+        if name in binnings:
+            c.enabled[k] = 1
+            c.soff[k] = off
+            off += 6 * 5
+    nstat = off
+    for k, name in enumerate(MMC_TALLIES):
+        if name in binnings:
+            nb, lo, hi = binnings[name]
+            c.nbins[k], c.xmin[k], c.xmax[k] = int(nb), lo, hi
+            c.off[k] = off
+            off += 6 * (int(nb) + 2) * 2
+    return c, nstat, off
+
+
+def mmc_empty_buffer(c, nbuf):
+    buf = np.zeros(nbuf, dtype=np.float64)
+    k = buf.view(np.int64)
+    for t in range(9):
+        if c.enabled[t]:
+            for g in range(6):
+                k[c.soff[t] + g * 5 + 3] = np.iinfo(np.int64).max
+                k[c.soff[t] + g * 5 + 4] = np.iinfo(np.int64).min
+    return buf
+
+
+def mmc_run(material, c, nbuf, first_id, count, threads=1):
+    """Histories [first_id, first_id+count) on `threads` host threads.
+    Returns (tally buffer, counts[tallied, tallied_w, miss, miss_w, nfail, steps])."""
+    from concurrent.futures import ThreadPoolExecutor
+    L = oracle_lib()
+    if not hasattr(L, "_mmc_ready"):
+        L.ncgb_oracle_mmc_run.restype = C.c_int
+        L.ncgb_oracle_mmc_run.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p]
+        L._mmc_ready = True
+    parts = max(1, min(threads, count))
+    edges = np.linspace(first_id, first_id + count, parts + 1).astype(np.uint64)
+    bufs = [mmc_empty_buffer(c, nbuf) for _ in range(parts)]
+    cnts = [np.zeros(6) for _ in range(parts)]
+
+    def work(i):
+        L.ncgb_oracle_mmc_run(material.view, C.byref(c), int(edges[i]), int(edges[i + 1] - edges[i]),
+                              _P(bufs[i]), _P(cnts[i]))
+
+    with ThreadPoolExecutor(max_workers=parts) as ex:
+        list(ex.map(work, range(parts)))
+    out = mmc_empty_buffer(c, nbuf)
+    ko = out.view(np.int64)
+    for b in bufs:
+        kb = b.view(np.int64)
+        for t in range(9):
+            if not c.enabled[t]:
+                continue
+            for g in range(6):
+                s0 = c.soff[t] + g * 5
+                out[s0:s0 + 3] += b[s0:s0 + 3]
+                ko[s0 + 3] = min(ko[s0 + 3], kb[s0 + 3])
+                ko[s0 + 4] = max(ko[s0 + 4], kb[s0 + 4])
+        nstat_end = min(c.off[t] for t in range(9) if c.enabled[t])
+        out[nstat_end:] += b[nstat_end:]
+    return out, np.sum(cnts, axis=0)
+
+
+def mmc_hist(c, buf, name, part="total"):
+    """(content, errorsq) with under/overflow of one tally group."""
+    k = MMC_TALLIES.index(name)
+    g = 0 if part == "total" else 1 + MMC_GROUPS.index(part)
+    nb = c.nbins[k]
+    b = buf[c.off[k] + g * (nb + 2) * 2: c.off[k] + (g + 1) * (nb + 2) * 2].reshape(-1, 2)
+    return b[:, 0].copy(), b[:, 1].copy()
+
+
+def reference_mmc(entries):
+    """The reference library's own MiniMC (ncrystal_jsonquery of
+    oracle/_ref/libNCrystal.so, where the NCrystal sources were built) for a
+    query ["mmc", "run", ...]; None when that library is absent."""
+    import json
+    import ncrystal_gb300._build as B
+    path = os.path.join(B.REF_OUT, "libNCrystal.so")
+    if not os.path.exists(path):
+        return None
+    L = C.CDLL(path)
+    L.ncrystal_jsonquery.restype = C.c_void_p
+    L.ncrystal_jsonquery.argtypes = [C.c_char_p]
+    L.ncrystal_dealloc_string.argtypes = [C.c_void_p]
+    raw = L.ncrystal_jsonquery("\x07".join(entries).encode())
+    if not raw:
+        raise RuntimeError("reference MiniMC query failed: %r" % (entries,))
+    txt = C.cast(raw, C.c_char_p).value.decode()
+    L.ncrystal_dealloc_string(raw)
+    return json.loads(txt)
