@@ -861,6 +861,19 @@ namespace {
     autob( T_L, 200, 0.0, 10.0, false );
     autob( T_DE, 200, -1.0, 1.0, false );
     autob( T_Q, 200, 0.0, 10.0, false );
+    // statistics shifts: the tally values of an unscattered source neutron
+    // (device arithmetic for l matches this expression bit for bit)
+    {
+      const double e0 = src.fixed_e ? src.e_fixed : ( src.mean_e ? src.e_mean : 0.0 );
+      for ( int k = 0; k < T_N; ++k )
+        t.shift[k] = 0.0;
+      if ( src.fixed_dir )
+        t.shift[T_MU] = 1.0;
+      if ( e0 > 0.0 ) {
+        t.shift[T_E] = e0;
+        t.shift[T_L] = std::sqrt( kWl2Ekin ) * std::sqrt( 1.0 / e0 );
+      }
+    }
     int64_t off = 0;
     for ( int k = 0; k < T_N; ++k ) {
       TallyHist& h = t.h[k];
@@ -1298,8 +1311,10 @@ namespace {
     os << "{\"datatype\":\"NCrystalHist1D_v1\",\"title\":" << jsonStr( title ) << ",\"stats\":{\"integral\":"
        << jsonNum( stt[0] );
     if ( stt[0] > 0.0 ) {
-      const double mean = stt[1] / stt[0];
-      const double rms = std::sqrt( std::max( 0.0, stt[2] / stt[0] - mean * mean ) );
+      // sums of w (x - shift) and w (x - shift)^2
+      const double m1 = stt[1] / stt[0];
+      const double mean = t.shift[k] + m1;
+      const double rms = std::sqrt( std::max( 0.0, stt[2] / stt[0] - m1 * m1 ) );
       os << ",\"rms\":" << jsonNum( rms ) << ",\"mean\":" << jsonNum( mean ) << ",\"minfilled\":"
          << jsonNum( fromKey( stt[3] ) ) << ",\"maxfilled\":" << jsonNum( fromKey( stt[4] ) );
     } else {

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdlib>
+#include <algorithm>
+#include <cmath>
 
 #include "ncgb_device.cuh"
 #include "ncgb_mmc.hh"
@@ -210,24 +212,42 @@ namespace {
     return 1 + ( f >= (double)h.nbins ? h.nbins : (int)f );
   }
 
-  // Bin update: one shared-memory (or global) atomic pair per lane.  Lanes
-  // of a warp that hit the same bin serialise in the atomic unit, which is
-  // cheaper than aggregating them on the narrow FP64 pipe first.
-  __device__ __forceinline__ void addBins( double* buf, const TallyHist& h, int g, int bin, double wt, bool f )
+  // Where a kernel's tally updates go: the warp's private statistics
+  // (shared memory) and the block's bins, in shared memory as 64-bit
+  // fixed-point integers (native integer atomics; FP64 atomics on shared
+  // memory are compare-and-swap loops that contending lanes retry on the
+  // narrow FP64 pipe) or, when they do not fit, the global FP64 buffer.
+  // Indices are the global buffer's offsets (bins: minus nstat in shared
+  // memory).
+  struct TallyDst {
+    double* stats;
+    unsigned long long* ubins;
+    double* gbins;
+  };
+
+  __device__ __forceinline__ void addBins( const TallyDst& d, const Tally& t, const TallyHist& h, int g, int bin,
+                                           double wt, bool f )
   {
-    if ( f ) {
-      double* b = buf + h.off + ( (int64_t)g * ( h.nbins + 2 ) + bin ) * 2;
-      atomicAdd( b, wt );
-      atomicAdd( b + 1, wt * wt );
+    if ( !f )
+      return;
+    const int64_t i = h.off + ( (int64_t)g * ( h.nbins + 2 ) + bin ) * 2;
+    if ( d.ubins ) {
+      unsigned long long* b = d.ubins + ( i - t.nstat );
+      atomicAdd( b, __double2ull_rn( wt * t.cscale ) );
+      atomicAdd( b + 1, __double2ull_rn( wt * wt * t.escale ) );
+    } else {
+      atomicAdd( d.gbins + i, wt );
+      atomicAdd( d.gbins + i + 1, wt * wt );
     }
   }
 
   // Warp reduction of one group's running statistics (RunningStats1D,
   // NCHists.hh:613-650): sums of w, w x, w x^2 (FP64) and the extreme keys,
-  // added by lane 0.  Called by all 32 lanes; f selects the contributing ones.
-  __device__ __forceinline__ void addStats( double* st, double x, double wt, bool f )
+  // added by lane 0 to the warp's private slots.  Called by all 32 lanes; f
+  // selects the contributing ones.
+  __device__ __forceinline__ void addStats( double* st, double x, double xs, double wt, bool f )
   {
-    double s0 = f ? wt : 0.0, s1 = f ? wt * x : 0.0, s2 = f ? wt * x * x : 0.0;
+    double s0 = f ? wt : 0.0, s1 = f ? wt * xs : 0.0, s2 = f ? wt * xs * xs : 0.0;
     const long long k = orderKey( x );
     long long kmin = f ? k : 0x7FFFFFFFFFFFFFFFLL, kmax = f ? k : (long long)0x8000000000000000ULL;
 #pragma unroll
@@ -240,24 +260,92 @@ namespace {
       kmax = b > kmax ? b : kmax;
     }
     if ( ( threadIdx.x & 31 ) == 0 ) {
-      atomicAdd( st, s0 );
-      atomicAdd( st + 1, s1 );
-      atomicAdd( st + 2, s2 );
-      atomicMin( reinterpret_cast<long long*>( st + 3 ), kmin );
-      atomicMax( reinterpret_cast<long long*>( st + 4 ), kmax );
+      // the warp's private slots: one writer, no atomics
+      st[0] += s0;
+      st[1] += s1;
+      st[2] += s2;
+      long long* sk = reinterpret_cast<long long*>( st );
+      if ( kmin < sk[3] ) sk[3] = kmin;
+      if ( kmax > sk[4] ) sk[4] = kmax;
     }
+    __syncwarp();
   }
 
   // Hist1D::fill (NCHists.hh:303-345, :525-530) of histogram h for the warp:
   // the total and, with breakdowns, the group of each lane's category.
   // Weighted fills skip weights <= 0; unweighted fills count 1.
-  // Where a kernel's tally updates go: statistics (always block-local in
-  // shared memory) and bins (shared memory or the global buffer); both are
-  // indexed with the global buffer's offsets.
-  struct TallyDst {
-    double* stats;
-    double* bins;
-  };
+  // One reduce-scatter step over the warp: lanes whose 'bit' is clear keep
+  // the lower half of v, the others the upper half, each adding its
+  // partner's copy of the kept half (n values in, n/2 out, n/2 adds).
+  template<int N, class T, class Op>
+  __device__ __forceinline__ void rsStep( T* v, int bit, Op op )
+  {
+    const bool upper = ( threadIdx.x >> bit ) & 1;
+#pragma unroll
+    for ( int j = 0; j < N / 2; ++j ) {
+      const T send = upper ? v[j] : v[j + N / 2];
+      const T keep = upper ? v[j + N / 2] : v[j];
+      v[j] = op( keep, __shfl_xor_sync( kFull, send, 1 << bit ) );
+    }
+  }
+
+  // Statistics of the five category groups in one warp reduce-scatter:
+  // 15 sums (w, w x, w x^2 per category; 16 slots) end up one per lane pair
+  // (lane l holds slot l >> 1) after 8+4+2+1+1 additions per lane, instead of
+  // a 5-step butterfly of 3 sums for every category present; the extreme
+  // keys (10 values, 2 x 8 slots) likewise on the integer pipe.  The lane
+  // holding a slot adds it to the warp's private statistics.  Called by all
+  // 32 lanes.
+  __device__ __forceinline__ void addStatsCats( double* st, double x, double xs, double wt, bool f, int cat )
+  {
+    double v[16];
+#pragma unroll
+    for ( int c = 0; c < 5; ++c ) {
+      const bool mine = f && cat == c;
+      v[3 * c] = mine ? wt : 0.0;
+      v[3 * c + 1] = mine ? wt * xs : 0.0;
+      v[3 * c + 2] = mine ? wt * xs * xs : 0.0;
+    }
+    v[15] = 0.0;
+    auto add = []( double a, double b ) { return a + b; };
+    rsStep<16>( v, 4, add );
+    rsStep<8>( v, 3, add );
+    rsStep<4>( v, 2, add );
+    rsStep<2>( v, 1, add );
+    v[0] += __shfl_xor_sync( kFull, v[0], 1 );
+    const int lane = threadIdx.x & 31;
+    const int slot = lane >> 1;
+    if ( ( lane & 1 ) == 0 && slot < 15 && v[0] != 0.0 )
+      st[( 1 + slot / 3 ) * kStats + slot % 3] += v[0];
+    // extremes: 8 slots of minima (5 used) and 8 of maxima
+    const long long k = orderKey( x );
+    long long mn[8], mx[8];
+#pragma unroll
+    for ( int c = 0; c < 8; ++c ) {
+      const bool mine = f && cat == c;
+      mn[c] = mine ? k : 0x7FFFFFFFFFFFFFFFLL;
+      mx[c] = mine ? k : (long long)0x8000000000000000ULL;
+    }
+    auto lo = []( long long a, long long b ) { return a < b ? a : b; };
+    auto hi = []( long long a, long long b ) { return a > b ? a : b; };
+    rsStep<8>( mn, 4, lo );
+    rsStep<8>( mx, 4, hi );
+    rsStep<4>( mn, 3, lo );
+    rsStep<4>( mx, 3, hi );
+    rsStep<2>( mn, 2, lo );
+    rsStep<2>( mx, 2, hi );
+    mn[0] = lo( mn[0], __shfl_xor_sync( kFull, mn[0], 2 ) );
+    mx[0] = hi( mx[0], __shfl_xor_sync( kFull, mx[0], 2 ) );
+    mn[0] = lo( mn[0], __shfl_xor_sync( kFull, mn[0], 1 ) );
+    mx[0] = hi( mx[0], __shfl_xor_sync( kFull, mx[0], 1 ) );
+    const int ks = lane >> 2;
+    if ( ( lane & 3 ) == 0 && ks < 5 ) {
+      long long* sk = reinterpret_cast<long long*>( st + ( 1 + ks ) * kStats );
+      if ( mn[0] < sk[3] ) sk[3] = mn[0];
+      if ( mx[0] > sk[4] ) sk[4] = mx[0];
+    }
+    __syncwarp();
+  }
 
   // With breakdowns only the five category groups are filled: the host
   // forms the total as their sum (bins, sums) and extremes.
@@ -270,15 +358,14 @@ namespace {
       return;
     const double wt = weighted ? w : 1.0;
     const int bin = f ? binOf( h, x ) : 0;
+    const double xs = x - t.shift[kind];
     if ( !t.breakdown ) {
-      addBins( d.bins, h, 0, bin, wt, f );
-      addStats( d.stats + h.soff, x, wt, f );
+      addBins( d, t, h, 0, bin, wt, f );
+      addStats( d.stats + h.soff, x, xs, wt, f );
       return;
     }
-    addBins( d.bins, h, 1 + cat, bin, wt, f );
-    for ( int c = 0; c < kGroups - 1; ++c )
-      if ( __any_sync( kFull, f && cat == c ) )
-        addStats( d.stats + h.soff + ( 1 + c ) * kStats, x, wt, f && cat == c );
+    addBins( d, t, h, 1 + cat, bin, wt, f );
+    addStatsCats( d.stats + h.soff, x, xs, wt, f, cat );
   }
 
   // tallyRecord (NCMMC_StdTallies.cc:430-660) for the warp's neutrons ('on'
@@ -327,20 +414,31 @@ namespace {
       histFillWarp( buf, t, T_W, cat, w, w, false, on );
   }
 
-  // Block-local tallies in shared memory: the statistics always, the bins
-  // too when 'bins' is set (sh then mirrors the whole buffer).  Min/max keys
-  // start at the empty values, sums at zero.
-  __device__ void tallyInitShared( double* sh, const Tally& t, bool bins )
+  constexpr int kBlock = 256;
+  constexpr int kWarps = kBlock / 32;
+
+  // Block-local tallies in shared memory: kWarps private copies of the
+  // statistics, then (when 'bins') the bins as fixed-point integers.  Min/max
+  // keys start at the empty values, everything else at zero.
+  __device__ TallyDst tallyInitShared( double* sh, const Tally& t, bool bins )
   {
-    const int64_t n = bins ? t.nbuf : t.nstat;
+    const int64_t ns = (int64_t)kWarps * t.nstat;
+    const int64_t n = ns + ( bins ? t.nbuf - t.nstat : 0 );
     for ( int64_t i = threadIdx.x; i < n; i += blockDim.x ) {
-      const int j = (int)( i % kStats );
       long long v = 0;
-      if ( i < t.nstat && j == 3 ) v = 0x7FFFFFFFFFFFFFFFLL;
-      if ( i < t.nstat && j == 4 ) v = (long long)0x8000000000000000ULL;
+      if ( i < ns ) {
+        const int j = (int)( ( i % t.nstat ) % kStats );
+        if ( j == 3 ) v = 0x7FFFFFFFFFFFFFFFLL;
+        if ( j == 4 ) v = (long long)0x8000000000000000ULL;
+      }
       sh[i] = __longlong_as_double( v );
     }
     __syncthreads();
+    TallyDst d;
+    d.stats = sh + ( threadIdx.x >> 5 ) * t.nstat;
+    d.ubins = bins ? reinterpret_cast<unsigned long long*>( sh + ns ) : nullptr;
+    d.gbins = t.buf;
+    return d;
   }
 
   __device__ void tallyFlushShared( const double* sh, const Tally& t, bool bins )
@@ -348,12 +446,18 @@ namespace {
     __syncthreads();
     for ( int64_t i = threadIdx.x; i < t.nstat; i += blockDim.x ) {
       const int j = (int)( i % kStats );
-      const double v = sh[i];
       if ( j < 3 ) {
+        double v = 0.0;
+        for ( int w = 0; w < kWarps; ++w )
+          v += sh[w * t.nstat + i];
         if ( v != 0.0 )
           atomicAdd( t.buf + i, v );
       } else {
-        const long long kv = __double_as_longlong( v );
+        long long kv = j == 3 ? 0x7FFFFFFFFFFFFFFFLL : (long long)0x8000000000000000ULL;
+        for ( int w = 0; w < kWarps; ++w ) {
+          const long long x = __double_as_longlong( sh[w * t.nstat + i] );
+          kv = j == 3 ? ( x < kv ? x : kv ) : ( x > kv ? x : kv );
+        }
         long long* dst = reinterpret_cast<long long*>( t.buf + i );
         if ( j == 3 && kv != 0x7FFFFFFFFFFFFFFFLL )
           atomicMin( dst, kv );
@@ -361,12 +465,15 @@ namespace {
           atomicMax( dst, kv );
       }
     }
-    if ( bins )
-      for ( int64_t i = t.nstat + threadIdx.x; i < t.nbuf; i += blockDim.x ) {
-        const double v = sh[i];
-        if ( v != 0.0 )
-          atomicAdd( t.buf + i, v );
+    if ( bins ) {
+      const unsigned long long* ub = reinterpret_cast<const unsigned long long*>( sh + (int64_t)kWarps * t.nstat );
+      const double ic = 1.0 / t.cscale, ie = 1.0 / t.escale;
+      for ( int64_t i = threadIdx.x; i < t.nbuf - t.nstat; i += blockDim.x ) {
+        const unsigned long long v = ub[i];
+        if ( v )
+          atomicAdd( t.buf + t.nstat + i, (double)v * ( ( i & 1 ) ? ie : ic ) );
       }
+    }
   }
 
   // Warp-aggregated append: slot of this lane among the lanes with 'want'.
@@ -405,8 +512,6 @@ namespace {
     }
   }
 
-  constexpr int kBlock = 256;
-
   // Source neutrons first_id .. first_id+count-1: fillBasket of the source
   // (NCMMC_Source.cc) and BasketSrcFiller::propagateToVolume
   // (NCMMC_BasketSrcFiller.hh:120-178): neutrons that miss the volume are
@@ -419,8 +524,7 @@ namespace {
   {
     extern __shared__ double sh[];
     __shared__ BlockSums miss, tal;
-    const TallyDst tb{ sh, bins_smem ? sh : t.buf };
-    tallyInitShared( sh, t, bins_smem );
+    const TallyDst tb = tallyInitShared( sh, t, bins_smem );
     if ( threadIdx.x == 0 ) { miss.n = 0; miss.w = 0.0; tal.n = 0; tal.w = 0.0; }
     __syncthreads();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -508,8 +612,7 @@ namespace {
   {
     extern __shared__ double sh[];
     __shared__ BlockSums tal;
-    const TallyDst tb{ sh, bins_smem ? sh : t.buf };
-    tallyInitShared( sh, t, bins_smem );
+    const TallyDst tb = tallyInitShared( sh, t, bins_smem );
     if ( threadIdx.x == 0 ) { tal.n = 0; tal.w = 0.0; }
     __syncthreads();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -673,9 +776,27 @@ namespace ncgb {
 
     static std::size_t tallySmem( const Tally& t, bool& bins )
     {
-      bins = (std::size_t)t.nbuf * sizeof(double) <= smemBudget();
-      return (std::size_t)( bins ? t.nbuf : t.nstat ) * sizeof(double);
+      const std::size_t st = (std::size_t)kWarps * t.nstat * sizeof(double);
+      const std::size_t bb = (std::size_t)( t.nbuf - t.nstat ) * sizeof(double);
+      bins = st + bb <= smemBudget();
+      return st + ( bins ? bb : 0 );
     }
+
+    // Fixed-point scales of the shared-memory bins for a launch of 'grid'
+    // blocks over n neutrons whose tally weights are at most wmax: the
+    // largest powers of two (<= 2^60) that keep a block's sums below 2^62.
+    static Tally withScales( Tally t, uint64_t n, int grid, double wmax )
+    {
+      const double per_block = (double)kBlock * (double)( ( n + (uint64_t)grid * kBlock - 1 ) / ( (uint64_t)grid * kBlock ) );
+      const double wm = wmax > 1.0 ? wmax : 1.0;
+      t.cscale = std::ldexp( 1.0, std::min( 60, (int)std::floor( 62.0 - std::log2( per_block * wm ) ) ) );
+      t.escale = std::ldexp( 1.0, std::min( 60, (int)std::floor( 62.0 - std::log2( per_block * wm * wm ) ) ) );
+      return t;
+    }
+
+    // Largest tally weight: 1 from the source; roulette survivors below the
+    // threshold are boosted by 1/psurvival, and weights only fall otherwise.
+    static double maxWeight( const Engine& eng ) { return std::max( 1.0, eng.wthr * eng.boost ); }
 
     cudaError_t launchEmit( const Source& src, const Geom& g, const Engine& eng, const Tally& t, Pop a,
                             uint64_t base, uint64_t first_id, uint64_t count, Counters* c, int numSMs,
@@ -688,8 +809,9 @@ namespace ncgb {
       cudaError_t e = allowSmem( k_mmc_emit, sbytes );
       if ( e != cudaSuccess )
         return e;
-      k_mmc_emit<<<gridFor( count, kBlock, numSMs * 4 ), kBlock, sbytes, s>>>( src, g, eng, t, a, base, first_id,
-                                                                             count, c, bins ? 1 : 0 );
+      const int grid = gridFor( count, kBlock, numSMs * 4 );
+      k_mmc_emit<<<grid, kBlock, sbytes, s>>>( src, g, eng, withScales( t, count, grid, 1.0 ), a, base, first_id,
+                                               count, c, bins ? 1 : 0 );
       return cudaGetLastError();
     }
 
@@ -702,15 +824,16 @@ namespace ncgb {
       bool bins = false;
       const std::size_t sbytes = tallySmem( t, bins );
       const int grid = gridFor( n_a, kBlock, numSMs * 4 );
+      const Tally ts = withScales( t, n_a, grid, maxWeight( eng ) );
       cudaError_t e;
       if ( eng.fast ) {
         e = allowSmem( k_mmc_transport<true>, sbytes );
         if ( e == cudaSuccess )
-          k_mmc_transport<true><<<grid, kBlock, sbytes, s>>>( m, g, eng, t, a, n_a, b, step, c, bins ? 1 : 0 );
+          k_mmc_transport<true><<<grid, kBlock, sbytes, s>>>( m, g, eng, ts, a, n_a, b, step, c, bins ? 1 : 0 );
       } else {
         e = allowSmem( k_mmc_transport<false>, sbytes );
         if ( e == cudaSuccess )
-          k_mmc_transport<false><<<grid, kBlock, sbytes, s>>>( m, g, eng, t, a, n_a, b, step, c, bins ? 1 : 0 );
+          k_mmc_transport<false><<<grid, kBlock, sbytes, s>>>( m, g, eng, ts, a, n_a, b, step, c, bins ? 1 : 0 );
       }
       return e != cudaSuccess ? e : cudaGetLastError();
     }

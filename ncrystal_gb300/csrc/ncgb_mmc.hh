@@ -94,6 +94,13 @@ namespace ncgb {
       int64_t nstat;           // doubles of statistics at the start of the buffer
       int64_t nbuf;            // doubles in the tally buffer
       double* buf;             // device
+      // per launch: fixed-point scales (powers of two) of the block-local
+      // bins in shared memory, for contents and errors^2
+      double cscale, escale;
+      // per tally: the statistics accumulate sums of w (x - shift) and
+      // w (x - shift)^2, shift = the value of an unscattered source neutron
+      // where that is fixed (delta-like groups keep their rms at ~0)
+      double shift[T_N];
     };
 
     // Population of neutrons (structure of arrays; directions [n][3]).

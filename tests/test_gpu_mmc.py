@@ -56,6 +56,24 @@ def test_mmc_tallies_match_reference(path):
             x, ndf, p, worst = chi2_compare(g[kc], g["%s.%s.errorsq" % (t, part)], n_ref, c, e, n_gpu)
             assert len(worst) == 0, (t, part, worst)
             comps.append((p, t, part, x, ndf))
+            # running statistics: integral = sum of the bins, extremes around
+            # the mean, and the mean within 6 standard errors of the reference's
+            st = res["output"]["tally"][t]["total" if part == "total" else "breakdown"]
+            st = (st if part == "total" else st[part])["stats"]
+            rs = g["%s.%s.stats" % (t, part)]   # integral, mean, rms, min, max
+            assert st["integral"] == pytest.approx(c.sum(), rel=1e-9, abs=1e-12)
+            if st["integral"] > 0 and rs[0] > 0:
+                tol = 1e-12 * max(abs(st["minfilled"]), abs(st["maxfilled"]), 1e-300)
+                assert st["minfilled"] - tol <= st["mean"] <= st["maxfilled"] + tol
+                assert st["rms"] >= 0.0
+                neff = min(c.sum() ** 2 / max(e.sum(), 1e-300), g[kc].sum() ** 2 / max(g["%s.%s.errorsq" % (t, part)].sum(), 1e-300))
+                if neff > 100 and rs[2] > 0:
+                    assert abs(st["mean"] - rs[1]) < 6 * rs[2] / np.sqrt(neff) + 1e-9 * abs(rs[1]), (t, part, st, rs)
+                    if rs[2] < 1e-6 * abs(rs[1]):
+                        # a delta-like group: rms at the rounding floor on both sides
+                        assert st["rms"] < 1e-6 * abs(st["mean"]), (t, part, st, rs)
+                    else:
+                        assert st["rms"] == pytest.approx(rs[2], rel=0.05), (t, part, st, rs)
     assert comps
     pmin = min(c[0] for c in comps)
     msg = "; ".join("%s/%s chi2=%.1f ndf=%d p=%.2e" % (t, part, x, ndf, p) for p, t, part, x, ndf in sorted(comps)[:4])
