@@ -117,14 +117,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel, workload_name):
-    """DRAM bytes per launch from the committed ncu summary, if any
-    (profiles/<kernel>_<workload>.md, line 'dram_bytes_per_launch: X')."""
+def profiled_traffic(kernel, workload_name, key="dram_bytes_per_launch"):
+    """DRAM bytes from the committed ncu summary, if any
+    (profiles/<kernel>_<workload>.md, line '<key>: X'): per launch, or per
+    unit of work with another key."""
     p = os.path.join(ROOT, "profiles", "%s_%s.md" % (kernel, workload_name))
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.strip().startswith("dram_bytes_per_launch:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -736,6 +737,10 @@ def run_minimc(args):
         "k_sab": {"ms_per_launch": t_sab * 1e3, "launches": nb, "share": t_sab / tot if tot else None},
     }
     achieved = kernels["k_mmc_transport"]["achieved_gbs"]
+    # DRAM traffic per launch: the ncu capture's bytes per transported
+    # neutron (profiles/k_mmc_transport_minimc.md) times this run's average
+    per_neutron = profiled_traffic("k_mmc_transport", "minimc", "dram_bytes_per_neutron_step")
+    traffic = per_neutron * nst / launches if per_neutron else None
     if rank == 0:
         base = mmc_cpu_baseline(args.cpu_seconds)
         line = {
@@ -749,7 +754,7 @@ def run_minimc(args):
                        "l2": "population 2 x 2^23 neutrons (~2.8 GB) > L2; tallies block-local in shared memory"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
-                         "traffic": profiled_traffic("k_mmc_transport", "minimc"), "kernel": "k_mmc_transport",
+                         "traffic": traffic, "kernel": "k_mmc_transport",
                          "kernels": kernels,
                          "note": "latency / FP64 bound (warp reductions of the tally statistics), not HBM bound"},
             "cpu_baseline": base,
