@@ -348,6 +348,17 @@ int ncgb_tables_build_proposal( void* tables, int comp, const float* knots, cons
 int ncgb_tables_set_proposal( void* tables, int comp, const void* hdr, const void* slot, const void* cell,
                               const void* seg, unsigned long nseg );
 
+/* Device-side derivation of the S(alpha,beta) sampling tables (the
+ * per-energy-point samplers of SABIntegrator::analyseEnergyPoint,
+ * NCSABIntegrator.cc:283-309, :352-559): compares component 'comp' of a bundle
+ * derived on the host and on the current CUDA device.  Integer arrays must
+ * agree exactly (n_int_mismatch); doubles differ only where CUDA's log/exp
+ * differ from the host's in the last place (n_double_diff, max_rel_diff).
+ * Times in ms.  Material loading uses the device builder when the environment
+ * sets NCGB_TABLES_BUILD=device. */
+int ncgb_sab_derive_compare( const char* bundle_path, int comp, double* max_rel_diff, long long* n_double_diff,
+                             long long* n_int_mismatch, double* ms_host, double* ms_device );
+
 /* Phase timing for benchmarks: while enabled, every scatter batch records
  * CUDA events on its stream before and after its two kernels (the pick /
  * cross-section pass and the S(alpha,beta) pass).  ncgb_phase_times waits for

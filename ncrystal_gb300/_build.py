@@ -76,7 +76,10 @@ def build_library(force=False, verbose=False):
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(BUILD, exist_ok=True)
-    cu = ["ncgb_kernels.cu", "ncgb_noalloc.cu", "ncgb_mlp.cu", "ncgb_mmc.cu"]
+    cu = ["ncgb_kernels.cu", "ncgb_noalloc.cu", "ncgb_mlp.cu", "ncgb_mmc.cu", "ncgb_sabderive.cu"]
+    # the device table builder shares its arithmetic with the host builder
+    # (g++ -ffp-contract=off): no contraction into FMAs there either
+    cu_flags = {"ncgb_sabderive.cu": ["-fmad=false"]}
     cc = ["ncgb_capi.cc", "ncgb_tables.cc", "ncgb_bundle.cc", "ncgb_hostapi.cc", "ncgb_proposal.cc",
           "ncgb_mmc.cc"]
     hdrs = _headers()
@@ -87,8 +90,8 @@ def build_library(force=False, verbose=False):
         obj = os.path.join(BUILD, f + ".o")
         objs.append(obj)
         if force or not _newer(obj, [src] + hdrs):
-            jobs.append([nvcc] + ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-                                         "-I" + INC, "-I" + CSRC, "-c", src, "-o", obj])
+            jobs.append([nvcc] + ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC"]
+                        + cu_flags.get(f, []) + ["-I" + INC, "-I" + CSRC, "-c", src, "-o", obj])
     for f in cc:
         src = os.path.join(CSRC, f)
         obj = os.path.join(BUILD, f + ".o")

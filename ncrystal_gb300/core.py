@@ -155,6 +155,8 @@ def lib():
         "ncgb_phase_timing": (None, [_C.c_int]),
         "ncgb_phase_times": (_C.c_int, [_dblp, _dblp, _C.POINTER(_C.c_ulong), _C.POINTER(_C.c_ulong)]),
         "ncgb_device_bytes": (_C.c_ulong, [H]),
+        "ncgb_sab_derive_compare": (_C.c_int, [_C.c_char_p, _C.c_int, _dblp, _C.POINTER(_C.c_longlong),
+                                               _C.POINTER(_C.c_longlong), _dblp, _dblp]),
         "ncrystal_jsonquery": (_C.c_void_p, [_C.c_char_p]),
         "ncrystal_dealloc_string": (None, [_C.c_void_p]),
         "ncgb_mmc_run": (_C.c_void_p, [H, _C.c_char_p, _C.c_char_p, _C.c_char_p]),
@@ -703,6 +705,20 @@ def createScatter(cfgstr, seed=None):
     if not h.internal:
         raise NCException("could not create scatter for %r" % cfgstr)
     return Scatter(h, cfgstr)
+
+
+def sab_derive_compare(bundle_path, comp):
+    """Host- and device-derived S(alpha,beta) sampling tables of one
+    component compared (ncgb_sab_derive_compare): dict with max_rel_diff,
+    n_double_diff, n_int_mismatch, ms_host, ms_device."""
+    L = lib()
+    mr, ms_h, ms_d = _C.c_double(), _C.c_double(), _C.c_double()
+    nd, ni = _C.c_longlong(), _C.c_longlong()
+    if L.ncgb_sab_derive_compare(bundle_path.encode(), int(comp), _C.byref(mr), _C.byref(nd), _C.byref(ni),
+                                 _C.byref(ms_h), _C.byref(ms_d)):
+        raise NCCalcError(L.ncgb_tables_lasterror().decode())
+    return {"max_rel_diff": mr.value, "n_double_diff": nd.value, "n_int_mismatch": ni.value,
+            "ms_host": ms_h.value, "ms_device": ms_d.value}
 
 
 def createProcess(cfgstr):

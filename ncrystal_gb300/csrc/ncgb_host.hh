@@ -83,6 +83,9 @@ namespace ncgb {
     std::vector<ncgb_alpha_info> info;  // same offsets as bx (one unused slot per sampler)
   };
   SABDerived deriveSAB( const SABInput& );
+  // The same on the current CUDA device (ncgb_sabderive.cu); used by build()
+  // when NCGB_TABLES_BUILD=device.
+  SABDerived deriveSABDevice( const SABInput& );
 
   // Free-gas cross-section shape (NCFreeGasUtils.cc:64-84):
   double freeGasXSShapeASq( double a_squared );

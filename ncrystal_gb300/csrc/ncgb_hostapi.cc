@@ -5,9 +5,13 @@
 #include "ncgb_proposal.hh"
 #include "ncrystal_gb300.h"
 
+#include <algorithm>
+#include <chrono>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 namespace {
   struct HostTables {
@@ -191,6 +195,114 @@ int ncgb_tables_scalar( void* handle, int comp, const char* name, double* out )
   if ( n == "type" ) { *out = v.comp[comp].type; return 0; }
   if ( n == "ncomp" ) { *out = v.ncomp; return 0; }
   return 1;
+}
+
+}
+
+// ---- device-side S(alpha,beta) derivation: comparison with the host builder ----------
+namespace {
+  template<class T>
+  void cmpInt( const std::vector<T>& a, const std::vector<T>& b, long long& bad )
+  {
+    if ( a.size() != b.size() ) { bad += 1 + (long long)std::max( a.size(), b.size() ); return; }
+    for ( std::size_t i = 0; i < a.size(); ++i )
+      if ( a[i] != b[i] ) ++bad;
+  }
+
+  void cmpDbl( double a, double b, double& maxrel, long long& ndiff )
+  {
+    if ( a == b || ( std::isnan( a ) && std::isnan( b ) ) )
+      return;
+    ++ndiff;
+    const double d = std::fabs( a - b ), s = std::max( std::fabs( a ), std::fabs( b ) );
+    const double r = s > 0 ? d / s : d;
+    if ( !( r <= maxrel ) )
+      maxrel = ( std::isinf( a ) || std::isinf( b ) ) ? INFINITY : std::max( maxrel, r );
+  }
+
+  void cmpDbl( const std::vector<double>& a, const std::vector<double>& b, double& maxrel, long long& ndiff,
+               long long& bad )
+  {
+    if ( a.size() != b.size() ) { bad += 1; return; }
+    for ( std::size_t i = 0; i < a.size(); ++i )
+      cmpDbl( a[i], b[i], maxrel, ndiff );
+  }
+}
+
+extern "C" {
+
+/* Derives the sampling tables of S(alpha,beta) component 'comp' of a bundle
+ * with the host builder and with the device builder, and compares them:
+ * integer arrays (sampler kinds, offsets, beta counts and offsets) must be
+ * identical (n_int_mismatch counts differences); doubles are reported as the
+ * number that differ and their largest relative difference.  Also returns
+ * both derivation times (milliseconds, wall clock; the device's includes its
+ * copies).  Returns 0, or 1 with ncgb_tables_lasterror set. */
+int ncgb_sab_derive_compare( const char* bundle_path, int comp, double* max_rel_diff, long long* n_double_diff,
+                             long long* n_int_mismatch, double* ms_host, double* ms_device )
+{
+  try {
+    auto b = ncgb::Bundle::load( bundle_path );
+    const std::string p = "c" + std::to_string( comp ) + ".";
+    if ( !b.has( p + "sab" ) )
+      throw ncgb::Error( "component " + std::to_string( comp ) + " is not an S(alpha,beta) component" );
+    ncgb::SABInput in;
+    in.alpha = b.f64( p + "alpha" );
+    in.beta = b.f64( p + "beta" );
+    in.sab = b.f64( p + "sab" );
+    in.egrid = b.f64( p + "egrid" );
+    in.kT = b.f64s( p + "sab_kT" );
+    in.sigma_bound = b.f64s( p + "sigma_bound" );
+    in.ext_sigma_free = b.f64s( p + "ext_sigma_free" );
+    in.ext_ca = b.f64s( p + "ext_ca" );
+    auto t0 = std::chrono::steady_clock::now();
+    ncgb::SABDerived h = ncgb::deriveSAB( in );
+    auto t1 = std::chrono::steady_clock::now();
+    ncgb::SABDerived d = ncgb::deriveSABDevice( in );
+    auto t2 = std::chrono::steady_clock::now();
+    if ( ms_host ) *ms_host = std::chrono::duration<double, std::milli>( t1 - t0 ).count();
+    if ( ms_device ) *ms_device = std::chrono::duration<double, std::milli>( t2 - t1 ).count();
+    long long bad = 0, ndiff = 0;
+    double maxrel = 0.0;
+    cmpInt( h.kind, d.kind, bad );
+    cmpInt( h.ibetaoffset, d.ibetaoffset, bad );
+    cmpInt( h.nbeta, d.nbeta, bad );
+    cmpInt( h.offset, d.offset, bad );
+    cmpDbl( h.logsab, d.logsab, maxrel, ndiff, bad );
+    cmpDbl( h.cumul, d.cumul, maxrel, ndiff, bad );
+    cmpDbl( h.xs, d.xs, maxrel, ndiff, bad );
+    cmpDbl( h.fbkep, d.fbkep, maxrel, ndiff, bad );
+    cmpDbl( h.bx, d.bx, maxrel, ndiff, bad );
+    cmpDbl( h.by, d.by, maxrel, ndiff, bad );
+    cmpDbl( h.bcdf, d.bcdf, maxrel, ndiff, bad );
+    cmpDbl( h.kext, d.kext, maxrel, ndiff );
+    cmpDbl( h.k1, d.k1, maxrel, ndiff );
+    cmpDbl( h.k2, d.k2, maxrel, ndiff );
+    if ( h.info.size() != d.info.size() ) {
+      ++bad;
+    } else {
+      for ( std::size_t i = 0; i < h.info.size(); ++i ) {
+        const ncgb_alpha_info &x = h.info[i], &y = d.info[i];
+        if ( x.front_idx != y.front_idx || x.back_idx != y.back_idx )
+          ++bad;
+        cmpDbl( x.front_alpha, y.front_alpha, maxrel, ndiff );
+        cmpDbl( x.front_sval, y.front_sval, maxrel, ndiff );
+        cmpDbl( x.front_logsval, y.front_logsval, maxrel, ndiff );
+        cmpDbl( x.back_alpha, y.back_alpha, maxrel, ndiff );
+        cmpDbl( x.back_sval, y.back_sval, maxrel, ndiff );
+        cmpDbl( x.back_logsval, y.back_logsval, maxrel, ndiff );
+        cmpDbl( x.prob_front, y.prob_front, maxrel, ndiff );
+        cmpDbl( x.prob_notback, y.prob_notback, maxrel, ndiff );
+      }
+    }
+    if ( max_rel_diff ) *max_rel_diff = maxrel;
+    if ( n_double_diff ) *n_double_diff = ndiff;
+    if ( n_int_mismatch ) *n_int_mismatch = bad;
+    return 0;
+  } catch ( std::exception& e ) {
+    t_lasterr = e.what();
+    return 1;
+  }
 }
 
 }

@@ -1,0 +1,409 @@
+// Device-side derivation of the S(alpha,beta) sampling tables
+// (SABIntegrator::analyseEnergyPoint per energy-grid point,
+// NCSABIntegrator.cc:283-309, :352-559; PointwiseDist, NCPointwiseDist.cc:28-74).
+//
+// The host builder (ncgb_tables.cc: deriveSAB) walks the energy grid and, at
+// each point, the beta rows one after the other.  Here:
+//   k_logcumul   one thread per beta row: log S and the cumulative alpha
+//                integrals (NCSABIntegrator.cc:119-138),
+//   k_betarows   one thread per (energy point, beta row): the row's active
+//                alpha range (activeGridRanges, NCSABUtils.cc:460-536, by
+//                binary search: the host's sweep converges to the same
+//                indices), kinematic limits and tailed breakdown
+//                (NCSABUtils.cc:538-633),
+//   k_epoints    one thread per energy point: the ordered part (skipped rows,
+//                the kinematic end point, the Neumaier sum of the beta
+//                weights, the normalised beta distribution).
+// Compiled with -fmad=false and sharing its per-row code with the host
+// (ncgb_sabderive.hh), so the two agree bit for bit except where CUDA's log and
+// exp differ from the host's in the last place.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ncgb_host.hh"
+#include "ncgb_sabderive.hh"
+
+namespace {
+
+  using namespace ncgb::sabd;
+
+  __global__ void k_logcumul( const double* alpha, const double* sab, int na, int nb, double* logsab, double* cumul )
+  {
+    const int ib = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( ib >= nb )
+      return;
+    const size_t g0 = (size_t)ib * na;
+    for ( int ai = 0; ai < na; ++ai ) {
+      const double e = sab[g0 + ai];
+      logsab[g0 + ai] = e > 0.0 ? log( e ) : -INFINITY;
+    }
+    double c = 0.0;
+    cumul[g0] = 0.0;
+    for ( int ai = 0; ai + 1 < na; ++ai ) {
+      c += integrateAlphaIntervalFast( alpha[ai], sab[g0 + ai], alpha[ai + 1], sab[g0 + ai + 1], logsab[g0 + ai],
+                                       logsab[g0 + ai + 1] );
+      cumul[g0 + ai + 1] = c;
+    }
+  }
+
+  // Per (energy point, beta row): whether the row is in the active range, and
+  // its cross-section and alpha sampler.
+  struct BetaRow {
+    double xs;
+    int32_t inrange, pad;
+    ncgb_alpha_info info;
+  };
+
+  __device__ int lastLE( const double* a, int n, double x )
+  {
+    // largest i with a[i] <= x, or 0
+    int lo = 0, hi = n;   // first index with a[i] > x in [lo, hi]
+    while ( lo < hi ) {
+      const int mid = ( lo + hi ) >> 1;
+      if ( a[mid] <= x ) lo = mid + 1; else hi = mid;
+    }
+    return lo > 0 ? lo - 1 : 0;
+  }
+
+  __device__ int firstGE( const double* a, int n, double x )
+  {
+    int lo = 0, hi = n;   // first index with a[i] >= x
+    while ( lo < hi ) {
+      const int mid = ( lo + hi ) >> 1;
+      if ( a[mid] < x ) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+  }
+
+  __global__ void k_betarows( const double* alpha, const double* beta, const double* sab, const double* logsab,
+                              const double* cumul, int na, int nb, const double* egrid, double kT, BetaRow* rows )
+  {
+    const int ie = blockIdx.y;
+    const int ib = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( ib >= nb )
+      return;
+    const double x = egrid[ie] / kT;
+    const double b = beta[ib];
+    // activeGridRanges (NCSABUtils.cc:474-533)
+    double alow = -1.0, aupp = -2.0;
+    if ( b > -x ) {
+      const ALim al = alphaLimits( x, b );
+      alow = al.lo;
+      aupp = al.hi;
+    }
+    const bool inr = !( alpha[na - 1] <= alow || alpha[0] >= aupp || aupp < alow );
+    int iLow = na, iUpp = na;
+    if ( inr ) {
+      iLow = lastLE( alpha, na, alow );
+      iUpp = firstGE( alpha, na, aupp );
+      if ( iUpp > na - 1 )
+        iUpp = na - 1;
+    }
+    // the row in analyseEnergyPoint (NCSABIntegrator.cc:437-486)
+    const ALim al = alphaLimits( x, b );
+    double xs = 0.0;
+    TailedBreakdown tb;
+    if ( iUpp > iLow && al.hi > al.lo ) {
+      const size_t slice = (size_t)na * ib;
+      tb = tailedBreakdown( alpha, (unsigned)na, sab + slice, logsab + slice, cumul + slice, al.lo, al.hi,
+                            (unsigned)iLow, (unsigned)iUpp );
+      xs = tb.xs_front + tb.xs_back + tb.xs_middle;
+    }
+    BetaRow r;
+    memset( &r, 0, sizeof(r) );
+    r.xs = xs;
+    r.inrange = inr;
+    if ( xs > 0.0 ) {
+      r.info.front_alpha = tb.front.alpha;
+      r.info.front_sval = tb.front.sval;
+      r.info.front_logsval = tb.front.logsval;
+      r.info.back_alpha = tb.back.alpha;
+      r.info.back_sval = tb.back.sval;
+      r.info.back_logsval = tb.back.logsval;
+      if ( tb.narrow ) {
+        r.info.prob_front = 1.0;
+      } else {
+        r.info.prob_front = tb.xs_front / xs;
+        r.info.prob_notback = 1.0 - tb.xs_back / xs;
+        r.info.front_idx = tb.imiddle_low;
+        r.info.back_idx = tb.imiddle_upp;
+      }
+    } else {
+      r.info.prob_front = 2.0;
+      r.info.front_alpha = al.lo;
+      r.info.back_alpha = al.hi;
+    }
+    rows[(size_t)ie * nb + ib] = r;
+  }
+
+  // The ordered part of analyseEnergyPoint (NCSABIntegrator.cc:384-559) and
+  // the PointwiseDist normalisation, one thread per energy point.  Per point
+  // the outputs occupy [ie*(nb+1), ie*(nb+1)+nbeta) of bx/by/bcdf and
+  // [ie*(nb+1), ...+nbeta-1) of info.
+  __global__ void k_epoints( const double* beta, int nb, const double* egrid, int ne, double kT, double sigma_bound,
+                             const BetaRow* rows, double* bx, double* by, double* bcdf, ncgb_alpha_info* info,
+                             double* xs_out, int32_t* kind, int32_t* ibl_out, int32_t* nbeta_out, double* fbkep,
+                             int32_t* err )
+  {
+    const int ie = blockIdx.x * blockDim.x + threadIdx.x;
+    if ( ie >= ne )
+      return;
+    const double x = egrid[ie] / kT;
+    const BetaRow* rr = rows + (size_t)ie * nb;
+    const size_t o = (size_t)ie * ( nb + 1 );
+    double beta_lower_limit = -x;
+    bool starts = true;
+    if ( beta_lower_limit < beta[0] ) {
+      const double c1 = beta[0] - ( beta[1] - beta[0] ) * 1e-6;
+      const double c2 = beta[0] - fabs( beta[0] ) * 1e-13;
+      const double c3 = nextafter( beta[0], beta_lower_limit );
+      beta_lower_limit = dmin( c1, dmin( c2, c3 ) );
+      starts = false;
+    }
+    int ibeta_low = nb;
+    for ( int ib = 0; ib < nb; ++ib )
+      if ( rr[ib].inrange ) { ibeta_low = ib; break; }
+    xs_out[ie] = 0.0;
+    kind[ie] = 0;
+    ibl_out[ie] = 0;
+    nbeta_out[ie] = 0;
+    fbkep[ie] = 0.0;
+    if ( ibeta_low >= nb )
+      return;
+    if ( ibeta_low > 0 && beta_lower_limit < beta[ibeta_low - 1] ) {
+      beta_lower_limit = beta[ibeta_low - 1];
+      starts = false;
+    }
+    double prev_first = beta_lower_limit, prev_second = 0.0;
+    int n = 0;
+    bx[o] = prev_first;
+    by[o] = prev_second;
+    ++n;
+    StableSum tot;
+    bool next_ep = starts;
+    for ( int ib = ibeta_low; ib < nb; ++ib ) {
+      const double b = beta[ib];
+      if ( b == beta_lower_limit )
+        continue;
+      const double xsb = rr[ib].xs;
+      info[o + n - 1] = rr[ib].info;
+      if ( next_ep ) {
+        next_ep = false;
+        const double db_real = b - prev_first;
+        prev_first -= db_real * ( 1.0 / 3.0 );
+        bx[o] = prev_first;
+      }
+      tot.add( 0.5 * ( b - prev_first ) * ( xsb + prev_second ) );
+      prev_first = b;
+      prev_second = xsb;
+      bx[o + n] = prev_first;
+      by[o + n] = prev_second;
+      ++n;
+    }
+    double xs_total = tot.sum() * sigma_bound / ( 4 * x );
+    if ( !( xs_total >= 0.0 ) )
+      xs_total = 0.0;
+    xs_out[ie] = xs_total;
+    if ( xs_total == 0.0 )
+      return;
+    kind[ie] = 1;
+    ibl_out[ie] = ibeta_low;
+    nbeta_out[ie] = n;
+    fbkep[ie] = starts ? beta_lower_limit : 1.0;
+    // PointwiseDist (NCPointwiseDist.cc:28-74)
+    StableSum area;
+    bcdf[o] = 0.0;
+    for ( int i = 0; i < n; ++i ) {
+      const double y = by[o + i];
+      if ( y < 0.0 || isinf( y ) || ( i > 0 && bx[o + i] < bx[o + i - 1] ) )
+        atomicExch( err, 1 );
+    }
+    for ( int i = 1; i < n; ++i ) {
+      const double a = ( bx[o + i] - bx[o + i - 1] ) * 0.5 * ( by[o + i] + by[o + i - 1] );
+      if ( a < 0 )
+        atomicExch( err, 1 );
+      area.add( a );
+      bcdf[o + i] = area.sum();
+    }
+    const double tarea = area.sum();
+    if ( !( tarea > 0.0 ) ) {
+      atomicExch( err, 1 );
+      return;
+    }
+    const double nf = 1.0 / tarea;
+    for ( int i = 0; i < n; ++i ) {
+      bcdf[o + i] *= nf;
+      by[o + i] *= nf;
+    }
+    bcdf[o + n - 1] = 1.0;
+  }
+
+  // Compaction into the host builder's layout: energy point ie's nbeta beta
+  // points go to [off[ie], off[ie]+nbeta) of bx/by/bcdf, its nbeta-1 alpha
+  // samplers and one zero pad to the same range of info.
+  __global__ void k_compact( int ne, int nb, const int32_t* nbeta, const int64_t* off, const double* sbx,
+                             const double* sby, const double* sbcdf, const ncgb_alpha_info* sinfo, double* bx,
+                             double* by, double* bcdf, ncgb_alpha_info* info )
+  {
+    const int ie = blockIdx.y;
+    const int n = nbeta[ie];
+    const size_t o = (size_t)ie * ( nb + 1 );
+    const int64_t d = off[ie];
+    for ( int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x ) {
+      bx[d + i] = sbx[o + i];
+      by[d + i] = sby[o + i];
+      bcdf[d + i] = sbcdf[o + i];
+      if ( i < n - 1 ) {
+        info[d + i] = sinfo[o + i];
+      } else {
+        ncgb_alpha_info z;
+        memset( &z, 0, sizeof(z) );
+        info[d + i] = z;
+      }
+    }
+  }
+
+  void check( cudaError_t e, const char* what )
+  {
+    if ( e != cudaSuccess )
+      throw ncgb::Error( std::string( "device table derivation: " ) + what + ": " + cudaGetErrorString( e ) );
+  }
+
+  // One device allocation carved into 256-byte aligned arrays (first pass
+  // sizes it, second pass hands out pointers).
+  struct Carve {
+    char* base = nullptr;
+    size_t used = 0;
+    template<class T> T* take( size_t n )
+    {
+      T* q = reinterpret_cast<T*>( base ? base + used : nullptr );
+      used += ( n * sizeof(T) + 255 ) & ~size_t(255);
+      return q;
+    }
+  };
+
+  struct DevBlock {
+    void* p = nullptr;
+    ~DevBlock() { if ( p ) cudaFree( p ); }
+  };
+}
+
+namespace ncgb {
+
+  // deriveSAB on the current CUDA device: same outputs as the host builder.
+  SABDerived deriveSABDevice( const SABInput& in )
+  {
+    const size_t na = in.alpha.size(), nb = in.beta.size(), ne = in.egrid.size();
+    if ( na < 2 || nb < 2 || in.sab.size() != na * nb )
+      throw Error( "SAB kernel with inconsistent grid sizes" );
+    if ( ne < 2 )
+      throw Error( "SAB energy grid too small" );
+    const size_t nslot = ne * ( nb + 1 );
+    double *d_alpha, *d_beta, *d_sab, *d_egrid, *d_log, *d_cum, *d_bx, *d_by, *d_bcdf, *d_xs, *d_fbkep;
+    double *c_bx, *c_by, *c_bcdf;
+    ncgb_alpha_info *d_info, *c_info;
+    BetaRow* d_rows;
+    int32_t *d_kind, *d_ibl, *d_nbeta, *d_err;
+    int64_t* d_off;
+    DevBlock blk;
+    for ( int pass = 0; pass < 2; ++pass ) {
+      Carve c;
+      if ( pass == 1 )
+        c.base = static_cast<char*>( blk.p );
+      d_alpha = c.take<double>( na );
+      d_beta = c.take<double>( nb );
+      d_sab = c.take<double>( na * nb );
+      d_egrid = c.take<double>( ne );
+      d_log = c.take<double>( na * nb );
+      d_cum = c.take<double>( na * nb );
+      d_rows = c.take<BetaRow>( ne * nb );
+      d_bx = c.take<double>( nslot );
+      d_by = c.take<double>( nslot );
+      d_bcdf = c.take<double>( nslot );
+      d_info = c.take<ncgb_alpha_info>( nslot );
+      c_bx = c.take<double>( nslot );
+      c_by = c.take<double>( nslot );
+      c_bcdf = c.take<double>( nslot );
+      c_info = c.take<ncgb_alpha_info>( nslot );
+      d_xs = c.take<double>( ne );
+      d_fbkep = c.take<double>( ne );
+      d_kind = c.take<int32_t>( ne );
+      d_ibl = c.take<int32_t>( ne );
+      d_nbeta = c.take<int32_t>( ne );
+      d_off = c.take<int64_t>( ne );
+      d_err = c.take<int32_t>( 1 );
+      if ( pass == 0 )
+        check( cudaMalloc( &blk.p, c.used ), "cudaMalloc" );
+    }
+    check( cudaMemcpy( d_alpha, in.alpha.data(), na * 8, cudaMemcpyHostToDevice ), "H2D" );
+    check( cudaMemcpy( d_beta, in.beta.data(), nb * 8, cudaMemcpyHostToDevice ), "H2D" );
+    check( cudaMemcpy( d_sab, in.sab.data(), na * nb * 8, cudaMemcpyHostToDevice ), "H2D" );
+    check( cudaMemcpy( d_egrid, in.egrid.data(), ne * 8, cudaMemcpyHostToDevice ), "H2D" );
+    check( cudaMemset( d_err, 0, 4 ), "memset" );
+    k_logcumul<<<( (int)nb + 127 ) / 128, 128>>>( d_alpha, d_sab, (int)na, (int)nb, d_log, d_cum );
+    check( cudaGetLastError(), "k_logcumul" );
+    k_betarows<<<dim3( ( (unsigned)nb + 127 ) / 128, (unsigned)ne ), 128>>>( d_alpha, d_beta, d_sab, d_log, d_cum,
+                                                                           (int)na, (int)nb, d_egrid, in.kT, d_rows );
+    check( cudaGetLastError(), "k_betarows" );
+    k_epoints<<<( (int)ne + 63 ) / 64, 64>>>( d_beta, (int)nb, d_egrid, (int)ne, in.kT, in.sigma_bound, d_rows, d_bx,
+                                              d_by, d_bcdf, d_info, d_xs, d_kind, d_ibl, d_nbeta, d_fbkep, d_err );
+    check( cudaGetLastError(), "k_epoints" );
+    // per-point offsets (the scan over ~ne counts is done on the host)
+    std::vector<int32_t> kind( ne ), ibl( ne ), nbeta( ne );
+    check( cudaMemcpy( nbeta.data(), d_nbeta, ne * 4, cudaMemcpyDeviceToHost ), "D2H" );
+    std::vector<int64_t> offs( ne );
+    int64_t tot = 0;
+    for ( size_t ie = 0; ie < ne; ++ie ) {
+      offs[ie] = tot;
+      tot += nbeta[ie];
+    }
+    check( cudaMemcpy( d_off, offs.data(), ne * 8, cudaMemcpyHostToDevice ), "H2D" );
+    k_compact<<<dim3( ( (unsigned)nb + 128 ) / 128, (unsigned)ne ), 128>>>( (int)ne, (int)nb, d_nbeta, d_off, d_bx,
+                                                                           d_by, d_bcdf, d_info, c_bx, c_by, c_bcdf,
+                                                                           c_info );
+    check( cudaGetLastError(), "k_compact" );
+    SABDerived d;
+    d.logsab.resize( na * nb );
+    d.cumul.resize( na * nb );
+    std::vector<double> xs( ne ), fbk( ne );
+    int32_t err = 0;
+    check( cudaMemcpy( d.logsab.data(), d_log, na * nb * 8, cudaMemcpyDeviceToHost ), "D2H" );
+    check( cudaMemcpy( d.cumul.data(), d_cum, na * nb * 8, cudaMemcpyDeviceToHost ), "D2H" );
+    check( cudaMemcpy( xs.data(), d_xs, ne * 8, cudaMemcpyDeviceToHost ), "D2H" );
+    check( cudaMemcpy( fbk.data(), d_fbkep, ne * 8, cudaMemcpyDeviceToHost ), "D2H" );
+    check( cudaMemcpy( kind.data(), d_kind, ne * 4, cudaMemcpyDeviceToHost ), "D2H" );
+    check( cudaMemcpy( ibl.data(), d_ibl, ne * 4, cudaMemcpyDeviceToHost ), "D2H" );
+    check( cudaMemcpy( &err, d_err, 4, cudaMemcpyDeviceToHost ), "D2H" );
+    if ( err )
+      throw Error( "PointwiseDist: invalid beta distribution at an energy-grid point" );
+    d.bx.resize( tot );
+    d.by.resize( tot );
+    d.bcdf.resize( tot );
+    d.info.resize( tot );
+    if ( tot ) {
+      check( cudaMemcpy( d.bx.data(), c_bx, tot * 8, cudaMemcpyDeviceToHost ), "D2H" );
+      check( cudaMemcpy( d.by.data(), c_by, tot * 8, cudaMemcpyDeviceToHost ), "D2H" );
+      check( cudaMemcpy( d.bcdf.data(), c_bcdf, tot * 8, cudaMemcpyDeviceToHost ), "D2H" );
+      check( cudaMemcpy( d.info.data(), c_info, tot * sizeof(ncgb_alpha_info), cudaMemcpyDeviceToHost ), "D2H" );
+    }
+    // per-point arrays in the host builder's layout (NCSABIntegrator.cc:283-309)
+    d.xs = xs;
+    for ( size_t ie = 0; ie < ne; ++ie ) {
+      d.kind.push_back( kind[ie] );
+      d.offset.push_back( offs[ie] );
+      d.ibetaoffset.push_back( kind[ie] ? ibl[ie] : 0 );
+      d.nbeta.push_back( kind[ie] ? nbeta[ie] : 0 );
+      d.fbkep.push_back( kind[ie] ? fbk[ie] : 0.0 );
+    }
+    const double emax = in.egrid.back();
+    const double extxs_emax = in.ext_sigma_free * freeGasXSShapeASq( in.ext_ca * emax );
+    d.kext = ( d.xs.back() - extxs_emax ) * emax;
+    d.k1 = d.xs.back() * emax;
+    d.k2 = extxs_emax * emax;
+    return d;
+  }
+}
