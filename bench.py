@@ -327,10 +327,15 @@ class SingleRunner:
 
     def e2e_info(self):
         esz = 4 if self.f32 else 8
+        zcv = os.environ.get("NCGB_ZERO_COPY", "")
+        zc = (zcv != "0") if zcv else self.f32
         chunk = 1 << 22
         return {"h2d_bytes_per_step": self.n * esz, "d2h_bytes_per_step": 3 * self.n * esz,
-                "gpu_launches_per_step": 2 * ((self.n + chunk - 1) // chunk),
-                "api": "ncgb_xs_scatter_many%s (C ABI, pinned host arrays)" % ("_f32" if self.f32 else "")}
+                "gpu_launches_per_step": 2 if zc else 2 * ((self.n + chunk - 1) // chunk),
+                "api": "ncgb_xs_scatter_many%s (C ABI, pinned host arrays; %s)"
+                       % ("_f32" if self.f32 else "",
+                          "the kernels read the energies from and write the results to host memory over "
+                          "NVLink-C2C" if zc else "chunked copies on two streams")}
 
     def launches_per_step(self):
         return 2
@@ -380,8 +385,12 @@ class BatchRunner:
                                        self.h_ef.data_ptr(), self.h_mu.data_ptr())
 
     def e2e_info(self):
+        zc = os.environ.get("NCGB_ZERO_COPY", "") == "1"
         return {"h2d_bytes_per_step": self.n * 8 + self.h_off.numel() * 8, "d2h_bytes_per_step": 3 * self.n * 8,
-                "gpu_launches_per_step": 2, "api": "ncgb_batch_xs_scatter_many (C ABI, pinned host arrays)",
+                "gpu_launches_per_step": 2,
+                "api": "ncgb_batch_xs_scatter_many (C ABI, pinned host arrays; %s)"
+                       % ("kernels read and write host memory over NVLink-C2C" if zc
+                          else "chunked copies on two streams"),
                 "autotuned_shape": {"pick_block": self.shape[0], "sab_blocks_per_sm": self.shape[1]}}
 
     def launches_per_step(self):

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <initializer_list>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -470,6 +471,62 @@ namespace {
   std::atomic<bool> g_warn_genscatter_many{true};
   std::atomic<bool> g_warn_genscatter{true};
 
+  // Zero-copy host calls: over the GB300's coherent NVLink-C2C the kernels
+  // can read the energies from pinned host arrays and write the results there
+  // directly, without staging copies.  Measured (2^24 neutrons): better for
+  // FP32 I/O (corundum e2e 5.7-6.3e9 vs 5.2-5.5e9 scatters/s with copies),
+  // worse for FP64 I/O (polyethylene 2.3-3.6e9 vs 4.6-4.9e9: the
+  // S(alpha,beta) pass writes its results at scattered indices, which the
+  // link turns into many small transactions).  Default: on for the FP32
+  // calls, off otherwise; NCGB_ZERO_COPY=1 / 0 forces it on / off.
+  bool zeroCopyFor( bool f32 )
+  {
+    const char* v = std::getenv( "NCGB_ZERO_COPY" );
+    if ( v && *v )
+      return std::string( v ) != "0";
+    return f32;
+  }
+
+  // Device address of pinned, mapped host memory (cudaHostAlloc /
+  // cudaHostRegister with UVA), or null for any other pointer.
+  const void* mappedDevicePtr( const void* p )
+  {
+    if ( !p )
+      return nullptr;
+    cudaPointerAttributes a;
+    if ( cudaPointerGetAttributes( &a, p ) != cudaSuccess ) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+  }
+
+  // All the given host arrays (nulls ignored) are mapped: their device
+  // addresses, in order, into 'out'.
+  bool allMapped( std::initializer_list<const void*> ptrs, std::vector<void*>& out )
+  {
+    out.clear();
+    for ( const void* p : ptrs ) {
+      if ( !p ) { out.push_back( nullptr ); continue; }
+      const void* d = mappedDevicePtr( p );
+      if ( !d )
+        return false;
+      out.push_back( const_cast<void*>( d ) );
+    }
+    return true;
+  }
+
+  // Neutrons per chunk of the copy pipeline (NCGB_CHUNK_LOG2, default 22).
+  uint64_t copyChunk()
+  {
+    static const uint64_t c = [] {
+      const char* v = std::getenv( "NCGB_CHUNK_LOG2" );
+      const int k = v ? std::atoi( v ) : 22;
+      return uint64_t(1) << ( k >= 16 && k <= 26 ? k : 22 );
+    }();
+    return c;
+  }
+
   // Chunked H2D / kernels / D2H pipeline over two streams for the host-array
   // fused entry points.  Chunk k runs on stream k%2 with the k%2 half of the
   // staging buffers; the SAB queue and counters are shared, so the kernels of
@@ -483,7 +540,25 @@ namespace {
       return;
     DeviceMaterial& dm = *o.mat;
     Scratch& s = scratchFor( dm );
-    const uint64_t chunk = std::min<uint64_t>( n, uint64_t(1) << 22 );
+    std::vector<void*> mp;
+    if ( zeroCopyFor( sizeof(T) == 4 ) && allMapped( { ekin, xs, ef, mu }, mp ) ) {
+      // zero-copy: one batch straight over the caller's pinned arrays
+      ensure( s.d_queue, s.cap_queue, n * sizeof(ncgb::QEntry) );
+      resetNFail( s, s.stream );
+      ncgb::Batch b = makeBatch( o, s, nextCall( o ) );
+      b.ekin = mp[0];
+      b.in_f32 = b.out_f32 = ( sizeof(T) == 4 );
+      b.n_ekin = b.n_out = n;
+      b.out_xs = mp[1];
+      b.out_a = mp[2];
+      b.out_b = mp[3];
+      runBatch( dm, s, b, s.stream );
+      const unsigned long bad = readNFail( s, s.stream );
+      if ( bad )
+        throwSamplingFailure( bad );
+      return;
+    }
+    const uint64_t chunk = std::min<uint64_t>( n, copyChunk() );
     ensure( s.d_in, s.cap_in, 2 * chunk * sizeof(T) );
     ensure( s.d_a, s.cap_a, 2 * chunk * sizeof(T) );
     ensure( s.d_b, s.cap_b, 2 * chunk * sizeof(T) );
@@ -1446,8 +1521,29 @@ void ncgb_batch_xs_scatter_many( ncgb_batch_t bt, const double* ekin, const int6
     // locate materials and random streams from the global index off + o); one
     // call sequence number for the whole call.
     Scratch& s = scratchFor( *bo.mats.front() );
-    const uint64_t chunk = std::min<uint64_t>( n, uint64_t(1) << 22 );
     const std::size_t offbytes = ( bo.nmat + 1 ) * sizeof(int64_t);
+    std::vector<void*> mp;
+    if ( zeroCopyFor( false ) && allMapped( { ekin, xs, ef, mu }, mp ) ) {
+      // zero-copy: one batch straight over the caller's pinned arrays
+      ensure( s.d_in, s.cap_in, offbytes + 256 );
+      ensure( s.d_queue, s.cap_queue, n * sizeof(ncgb::QEntry) );
+      int64_t* d_off = static_cast<int64_t*>( s.d_in );
+      const uint32_t call = bo.callseq.fetch_add( 1, std::memory_order_relaxed );
+      resetNFail( s, s.stream );
+      checkCuda( cudaMemcpyAsync( d_off, offsets, offbytes, cudaMemcpyHostToDevice, s.stream ), "H2D" );
+      ncgb::Batch b = multiBatch( bo, s, static_cast<const double*>( mp[0] ), n, static_cast<double*>( mp[1] ),
+                                  static_cast<double*>( mp[2] ), static_cast<double*>( mp[3] ), nullptr );
+      b.callseq = call;
+      b.index_offset = 0;
+      checkCuda( cudaStreamWaitEvent( s.stream, s.done, 0 ), "cudaStreamWaitEvent" );
+      checkCuda( ncgb::launchScatterMulti( bo.d_slots, d_off, bo.nmat, b, bo.cfg, s.stream ), "batch kernels" );
+      checkCuda( cudaEventRecord( s.done, s.stream ), "cudaEventRecord" );
+      const unsigned long bad = readNFail( s, s.stream );
+      if ( bad )
+        throwSamplingFailure( bad );
+      return;
+    }
+    const uint64_t chunk = std::min<uint64_t>( n, copyChunk() );
     ensure( s.d_in, s.cap_in, 2 * chunk * sizeof(double) + offbytes + 256 );
     ensure( s.d_a, s.cap_a, 2 * chunk * sizeof(double) );
     ensure( s.d_b, s.cap_b, 2 * chunk * sizeof(double) );
