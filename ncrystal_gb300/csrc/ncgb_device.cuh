@@ -431,10 +431,13 @@ namespace ncgb_dev {
     const float ef = (float)ekin;
     float commul[NCGB_MAX_COMP];
     float tot = 0.0f;
-#pragma unroll
+    // a rolled loop: unrolled, every copy carried the whole switch over the
+    // component types, and the pick pass stalled on instruction fetch
+#pragma unroll 1
     for ( int i = 0; i < NCGB_MAX_COMP; ++i ) {
-      if ( i < m.ncomp )
-        tot = fmaf( m.comp[i].scale_f, compXSf( m.comp[i], ekin, ef ), tot );
+      if ( i >= m.ncomp )
+        break;
+      tot = fmaf( m.comp[i].scale_f, compXSf( m.comp[i], ekin, ef ), tot );
       commul[i] = tot;
     }
     XSPick r{ (double)tot, 0 };
@@ -465,10 +468,11 @@ namespace ncgb_dev {
       return xsAndPickF<Pick>( m, ekin, rng );
     double commul[NCGB_MAX_COMP];
     double tot = 0.0;
-#pragma unroll
+#pragma unroll 1
     for ( int i = 0; i < NCGB_MAX_COMP; ++i ) {
-      if ( i < m.ncomp )
-        tot += m.comp[i].scale * compXS<Fast>( m.comp[i], ekin );
+      if ( i >= m.ncomp )
+        break;
+      tot += m.comp[i].scale * compXS<Fast>( m.comp[i], ekin );
       commul[i] = tot;
     }
     XSPick r{ tot, 0 };
