@@ -348,6 +348,21 @@ int ncgb_tables_build_proposal( void* tables, int comp, const float* knots, cons
 int ncgb_tables_set_proposal( void* tables, int comp, const void* hdr, const void* slot, const void* cell,
                               const void* seg, unsigned long nseg );
 
+/* Creates n scatter handles (the seed of ncrystal_create_scatter_builtinrng)
+ * for materials given by cfg-strings, deriving the S(alpha,beta) samplers of
+ * all of them in one batched device derivation (a temperature grid, a set of
+ * crystals).  Materials already loaded on this device are reused.  Returns 0,
+ * or 1 with the error state set and null handles. */
+int ncgb_create_scatters( const char* const* cfgstrs, unsigned long n, unsigned long seed,
+                          ncrystal_scatter_t* out );
+
+/* Host and batched device derivation over all S(alpha,beta) components of
+ * n bundles: the comparison of ncgb_sab_derive_compare summed over them, the
+ * number of components, and the two total times in ms. */
+int ncgb_sab_derive_compare_many( const char* const* bundle_paths, unsigned long n, double* max_rel_diff,
+                                  long long* n_double_diff, long long* n_int_mismatch, long long* ncomp,
+                                  double* ms_host, double* ms_device );
+
 /* Device-side derivation of the S(alpha,beta) sampling tables (the
  * per-energy-point samplers of SABIntegrator::analyseEnergyPoint,
  * NCSABIntegrator.cc:283-309, :352-559): compares component 'comp' of a bundle

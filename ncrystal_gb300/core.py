@@ -157,6 +157,10 @@ def lib():
         "ncgb_device_bytes": (_C.c_ulong, [H]),
         "ncgb_sab_derive_compare": (_C.c_int, [_C.c_char_p, _C.c_int, _dblp, _C.POINTER(_C.c_longlong),
                                                _C.POINTER(_C.c_longlong), _dblp, _dblp]),
+        "ncgb_sab_derive_compare_many": (_C.c_int, [_C.POINTER(_C.c_char_p), _C.c_ulong, _dblp,
+                                                    _C.POINTER(_C.c_longlong), _C.POINTER(_C.c_longlong),
+                                                    _C.POINTER(_C.c_longlong), _dblp, _dblp]),
+        "ncgb_create_scatters": (_C.c_int, [_C.POINTER(_C.c_char_p), _C.c_ulong, _C.c_ulong, _C.POINTER(H)]),
         "ncrystal_jsonquery": (_C.c_void_p, [_C.c_char_p]),
         "ncrystal_dealloc_string": (None, [_C.c_void_p]),
         "ncgb_mmc_run": (_C.c_void_p, [H, _C.c_char_p, _C.c_char_p, _C.c_char_p]),
@@ -705,6 +709,42 @@ def createScatter(cfgstr, seed=None):
     if not h.internal:
         raise NCException("could not create scatter for %r" % cfgstr)
     return Scatter(h, cfgstr)
+
+
+# Philox key of handles made without a seed (ncrystal_create_scatter).
+_DEFAULT_SEED = 0x4e43727973746c21
+
+
+def createScatters(cfgstrs, seed=None):
+    """Scatter objects for many cfg-strings at once (ncgb_create_scatters):
+    the S(alpha,beta) samplers of all the materials (a temperature grid, a
+    set of crystals) are derived in one batched device derivation."""
+    L = lib()
+    cfgstrs = list(cfgstrs)
+    n = len(cfgstrs)
+    arr = (_C.c_char_p * max(n, 1))(*[c.encode() for c in cfgstrs])
+    out = (_Handle * max(n, 1))()
+    seed = _DEFAULT_SEED if seed is None else int(seed)
+    if L.ncgb_create_scatters(arr, n, seed, out):
+        _check()
+        raise NCException("could not create scatters")
+    return [Scatter(out[i], cfgstrs[i]) for i in range(n)]
+
+
+def sab_derive_compare_many(bundle_paths):
+    """ncgb_sab_derive_compare over every S(alpha,beta) component of many
+    bundles, the device side as one batched derivation: dict with
+    max_rel_diff, n_double_diff, n_int_mismatch, ncomp, ms_host, ms_device."""
+    L = lib()
+    paths = list(bundle_paths)
+    arr = (_C.c_char_p * max(len(paths), 1))(*[p.encode() for p in paths])
+    mr, ms_h, ms_d = _C.c_double(), _C.c_double(), _C.c_double()
+    nd, ni, nc = _C.c_longlong(), _C.c_longlong(), _C.c_longlong()
+    if L.ncgb_sab_derive_compare_many(arr, len(paths), _C.byref(mr), _C.byref(nd), _C.byref(ni), _C.byref(nc),
+                                      _C.byref(ms_h), _C.byref(ms_d)):
+        raise NCCalcError(L.ncgb_tables_lasterror().decode())
+    return {"max_rel_diff": mr.value, "n_double_diff": nd.value, "n_int_mismatch": ni.value,
+            "ncomp": nc.value, "ms_host": ms_h.value, "ms_device": ms_d.value}
 
 
 def sab_derive_compare(bundle_path, comp):

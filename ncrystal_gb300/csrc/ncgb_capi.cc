@@ -187,6 +187,74 @@ namespace {
                       " written by ncgb_export, which runs NCrystal's host-side material loading." );
   }
 
+  // Upload built tables as a device material of the current device and cache it.
+  std::shared_ptr<DeviceMaterial> uploadMaterial( const std::string& canon, int dev,
+                                                  std::shared_ptr<ncgb::MaterialTables> tables )
+  {
+    auto dm = std::make_shared<DeviceMaterial>();
+    dm->tables = std::move( tables );
+    dm->device = dev;
+    const std::size_t bytes = dm->tables->arenaBytes();
+    checkCuda( cudaMalloc( &dm->d_arena, std::max<std::size_t>( bytes, 256 ) ), "cudaMalloc (material tables)" );
+    checkCuda( cudaMemcpy( dm->d_arena, dm->tables->arena().data(), bytes, cudaMemcpyHostToDevice ),
+               "cudaMemcpy (material tables)" );
+    dm->view = dm->tables->relocate( dm->d_arena );
+    g_matcache[std::make_pair( canon, dev )] = dm;
+    return dm;
+  }
+
+  // Many materials at once (a temperature grid, a batch of crystals): their
+  // S(alpha,beta) samplers derived in one batched device derivation.
+  std::vector<std::shared_ptr<DeviceMaterial>> getMaterials( const std::vector<std::string>& cfgs )
+  {
+    int dev = 0;
+    checkCuda( cudaGetDevice( &dev ), "cudaGetDevice" );
+    std::lock_guard<std::mutex> lock( g_matmtx );
+    std::vector<std::shared_ptr<DeviceMaterial>> out( cfgs.size() );
+    std::vector<ncgb::Bundle> bundles;
+    std::vector<std::size_t> todo;
+    std::vector<std::string> canons;
+    for ( std::size_t i = 0; i < cfgs.size(); ++i ) {
+      const std::string canon = canonicalCfg( cfgs[i] );
+      auto it = g_matcache.find( std::make_pair( canon, dev ) );
+      if ( it != g_matcache.end() )
+        if ( auto sp = it->second.lock() ) { out[i] = sp; continue; }
+      bool dup = false;
+      for ( std::size_t j = 0; j < canons.size(); ++j )
+        if ( canons[j] == canon ) dup = true;
+      if ( dup )
+        continue;
+      auto b = ncgb::Bundle::load( findBundle( cfgs[i] ) );
+      if ( canonicalCfg( b.str("cfg") ) != canon )
+        throw TypedError( "BadInput", "material bundle " + b.path() + " holds cfg \"" + b.str("cfg") + "\", not \""
+                          + cfgs[i] + "\"" );
+      bundles.push_back( std::move( b ) );
+      todo.push_back( i );
+      canons.push_back( canon );
+    }
+    std::vector<std::map<int, ncgb::SABInput>> inputs;
+    std::vector<const ncgb::SABInput*> flat;
+    for ( auto& b : bundles )
+      inputs.push_back( ncgb::sabInputs( b ) );
+    for ( auto& m : inputs )
+      for ( auto& kv : m )
+        flat.push_back( &kv.second );
+    std::vector<ncgb::SABDerived> derived = ncgb::deriveSABDeviceMany( flat );
+    std::size_t k = 0;
+    for ( std::size_t j = 0; j < bundles.size(); ++j ) {
+      std::map<int, ncgb::SABDerived> pre;
+      for ( auto& kv : inputs[j] )
+        pre.emplace( kv.first, std::move( derived[k++] ) );
+      auto tables = ncgb::MaterialTables::build( bundles[j], &pre );
+      out[todo[j]] = uploadMaterial( canons[j], dev, std::move( tables ) );
+    }
+    // duplicates of a material built in this call
+    for ( std::size_t i = 0; i < cfgs.size(); ++i )
+      if ( !out[i] )
+        out[i] = g_matcache[std::make_pair( canonicalCfg( cfgs[i] ), dev )].lock();
+    return out;
+  }
+
   std::shared_ptr<DeviceMaterial> getMaterial( const std::string& cfg )
   {
     const std::string canon = canonicalCfg( cfg );
@@ -203,16 +271,7 @@ namespace {
     if ( canonicalCfg( bundle.str("cfg") ) != canon )
       throw TypedError( "BadInput", "material bundle " + bundle.path() + " holds cfg \"" + bundle.str("cfg")
                         + "\", not \"" + cfg + "\"" );
-    auto dm = std::make_shared<DeviceMaterial>();
-    dm->tables = ncgb::MaterialTables::build( bundle );
-    dm->device = dev;
-    const std::size_t bytes = dm->tables->arenaBytes();
-    checkCuda( cudaMalloc( &dm->d_arena, std::max<std::size_t>( bytes, 256 ) ), "cudaMalloc (material tables)" );
-    checkCuda( cudaMemcpy( dm->d_arena, dm->tables->arena().data(), bytes, cudaMemcpyHostToDevice ),
-               "cudaMemcpy (material tables)" );
-    dm->view = dm->tables->relocate( dm->d_arena );
-    g_matcache[key] = dm;
-    return dm;
+    return uploadMaterial( canon, dev, ncgb::MaterialTables::build( bundle ) );
   }
 
   // ---- handles (ncrystal.cc:104-200) ------------------------------------------
@@ -672,6 +731,32 @@ static ncrystal_scatter_t createScatter( const char* cfgstr, uint64_t seed )
   o->cfg = cfgstr;
   o->seed = seed;
   return makeHandle( o.release() );
+}
+
+int ncgb_create_scatters( const char* const* cfgstrs, unsigned long n, unsigned long seed, ncrystal_scatter_t* out )
+{
+  try {
+    if ( !out || ( n && !cfgstrs ) )
+      throw TypedError( "BadInput", "ncgb_create_scatters: null array" );
+    std::vector<std::string> cfgs;
+    for ( unsigned long i = 0; i < n; ++i ) {
+      if ( !cfgstrs[i] )
+        throw TypedError( "BadInput", "ncgb_create_scatters: null cfg-string" );
+      cfgs.push_back( cfgstrs[i] );
+    }
+    auto mats = getMaterials( cfgs );
+    for ( unsigned long i = 0; i < n; ++i ) {
+      std::unique_ptr<ScatterObj> o( new ScatterObj );
+      o->mat = mats[i];
+      o->cfg = cfgs[i];
+      o->seed = seed;
+      out[i] = makeHandle( o.release() );
+    }
+    return 0;
+  } NCGB_CATCH;
+  for ( unsigned long i = 0; i < n; ++i )
+    if ( out ) out[i].internal = nullptr;
+  return 1;
 }
 
 ncrystal_scatter_t ncrystal_create_scatter( const char* cfgstr )

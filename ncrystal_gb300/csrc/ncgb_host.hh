@@ -44,6 +44,10 @@ namespace ncgb {
     // Build from a bundle: restates NCrystal's table derivation for SAB
     // (NCSABIntegrator.cc:95-145, :352-559) on the bundle's S(alpha,beta).
     static std::shared_ptr<MaterialTables> build( const Bundle& );
+    // The same with the S(alpha,beta) samplers of some components derived
+    // already (component index -> derived tables, e.g. from a batched device
+    // derivation over many materials).
+    static std::shared_ptr<MaterialTables> build( const Bundle&, const std::map<int, struct SABDerived>* pre );
 
     const std::vector<char>& arena() const { return m_arena; }
     std::size_t arenaBytes() const { return m_arena.size(); }
@@ -83,9 +87,12 @@ namespace ncgb {
     std::vector<ncgb_alpha_info> info;  // same offsets as bx (one unused slot per sampler)
   };
   SABDerived deriveSAB( const SABInput& );
+  // The S(alpha,beta) inputs of every S(alpha,beta) component of a bundle.
+  std::map<int, SABInput> sabInputs( const Bundle& );
   // The same on the current CUDA device (ncgb_sabderive.cu); used by build()
   // when NCGB_TABLES_BUILD=device.
   SABDerived deriveSABDevice( const SABInput& );
+  std::vector<SABDerived> deriveSABDeviceMany( const std::vector<const SABInput*>& );
 
   // Free-gas cross-section shape (NCFreeGasUtils.cc:64-84):
   double freeGasXSShapeASq( double a_squared );

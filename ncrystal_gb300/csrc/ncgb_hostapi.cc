@@ -227,43 +227,12 @@ namespace {
     for ( std::size_t i = 0; i < a.size(); ++i )
       cmpDbl( a[i], b[i], maxrel, ndiff );
   }
-}
 
-extern "C" {
-
-/* Derives the sampling tables of S(alpha,beta) component 'comp' of a bundle
- * with the host builder and with the device builder, and compares them:
- * integer arrays (sampler kinds, offsets, beta counts and offsets) must be
- * identical (n_int_mismatch counts differences); doubles are reported as the
- * number that differ and their largest relative difference.  Also returns
- * both derivation times (milliseconds, wall clock; the device's includes its
- * copies).  Returns 0, or 1 with ncgb_tables_lasterror set. */
-int ncgb_sab_derive_compare( const char* bundle_path, int comp, double* max_rel_diff, long long* n_double_diff,
-                             long long* n_int_mismatch, double* ms_host, double* ms_device )
-{
-  try {
-    auto b = ncgb::Bundle::load( bundle_path );
-    const std::string p = "c" + std::to_string( comp ) + ".";
-    if ( !b.has( p + "sab" ) )
-      throw ncgb::Error( "component " + std::to_string( comp ) + " is not an S(alpha,beta) component" );
-    ncgb::SABInput in;
-    in.alpha = b.f64( p + "alpha" );
-    in.beta = b.f64( p + "beta" );
-    in.sab = b.f64( p + "sab" );
-    in.egrid = b.f64( p + "egrid" );
-    in.kT = b.f64s( p + "sab_kT" );
-    in.sigma_bound = b.f64s( p + "sigma_bound" );
-    in.ext_sigma_free = b.f64s( p + "ext_sigma_free" );
-    in.ext_ca = b.f64s( p + "ext_ca" );
-    auto t0 = std::chrono::steady_clock::now();
-    ncgb::SABDerived h = ncgb::deriveSAB( in );
-    auto t1 = std::chrono::steady_clock::now();
-    ncgb::SABDerived d = ncgb::deriveSABDevice( in );
-    auto t2 = std::chrono::steady_clock::now();
-    if ( ms_host ) *ms_host = std::chrono::duration<double, std::milli>( t1 - t0 ).count();
-    if ( ms_device ) *ms_device = std::chrono::duration<double, std::milli>( t2 - t1 ).count();
-    long long bad = 0, ndiff = 0;
-    double maxrel = 0.0;
+  // Host and device derivations of one component compared: integer arrays
+  // must be identical; doubles are counted where they differ.
+  void compareDerived( const ncgb::SABDerived& h, const ncgb::SABDerived& d, double& maxrel, long long& ndiff,
+                       long long& bad )
+  {
     cmpInt( h.kind, d.kind, bad );
     cmpInt( h.ibetaoffset, d.ibetaoffset, bad );
     cmpInt( h.nbeta, d.nbeta, bad );
@@ -280,24 +249,97 @@ int ncgb_sab_derive_compare( const char* bundle_path, int comp, double* max_rel_
     cmpDbl( h.k2, d.k2, maxrel, ndiff );
     if ( h.info.size() != d.info.size() ) {
       ++bad;
-    } else {
-      for ( std::size_t i = 0; i < h.info.size(); ++i ) {
-        const ncgb_alpha_info &x = h.info[i], &y = d.info[i];
-        if ( x.front_idx != y.front_idx || x.back_idx != y.back_idx )
-          ++bad;
-        cmpDbl( x.front_alpha, y.front_alpha, maxrel, ndiff );
-        cmpDbl( x.front_sval, y.front_sval, maxrel, ndiff );
-        cmpDbl( x.front_logsval, y.front_logsval, maxrel, ndiff );
-        cmpDbl( x.back_alpha, y.back_alpha, maxrel, ndiff );
-        cmpDbl( x.back_sval, y.back_sval, maxrel, ndiff );
-        cmpDbl( x.back_logsval, y.back_logsval, maxrel, ndiff );
-        cmpDbl( x.prob_front, y.prob_front, maxrel, ndiff );
-        cmpDbl( x.prob_notback, y.prob_notback, maxrel, ndiff );
-      }
+      return;
     }
+    for ( std::size_t i = 0; i < h.info.size(); ++i ) {
+      const ncgb_alpha_info &x = h.info[i], &y = d.info[i];
+      if ( x.front_idx != y.front_idx || x.back_idx != y.back_idx )
+        ++bad;
+      cmpDbl( x.front_alpha, y.front_alpha, maxrel, ndiff );
+      cmpDbl( x.front_sval, y.front_sval, maxrel, ndiff );
+      cmpDbl( x.front_logsval, y.front_logsval, maxrel, ndiff );
+      cmpDbl( x.back_alpha, y.back_alpha, maxrel, ndiff );
+      cmpDbl( x.back_sval, y.back_sval, maxrel, ndiff );
+      cmpDbl( x.back_logsval, y.back_logsval, maxrel, ndiff );
+      cmpDbl( x.prob_front, y.prob_front, maxrel, ndiff );
+      cmpDbl( x.prob_notback, y.prob_notback, maxrel, ndiff );
+    }
+  }
+}
+
+extern "C" {
+
+/* Derives the sampling tables of S(alpha,beta) component 'comp' of a bundle
+ * with the host builder and with the device builder, and compares them:
+ * integer arrays (sampler kinds, offsets, beta counts and offsets) must be
+ * identical (n_int_mismatch counts differences); doubles are reported as the
+ * number that differ and their largest relative difference.  Also returns
+ * both derivation times (milliseconds, wall clock; the device's includes its
+ * copies).  Returns 0, or 1 with ncgb_tables_lasterror set. */
+int ncgb_sab_derive_compare( const char* bundle_path, int comp, double* max_rel_diff, long long* n_double_diff,
+                             long long* n_int_mismatch, double* ms_host, double* ms_device )
+{
+  try {
+    auto b = ncgb::Bundle::load( bundle_path );
+    auto all = ncgb::sabInputs( b );
+    auto it = all.find( comp );
+    if ( it == all.end() )
+      throw ncgb::Error( "component " + std::to_string( comp ) + " is not an S(alpha,beta) component" );
+    const ncgb::SABInput& in = it->second;
+    auto t0 = std::chrono::steady_clock::now();
+    ncgb::SABDerived h = ncgb::deriveSAB( in );
+    auto t1 = std::chrono::steady_clock::now();
+    ncgb::SABDerived d = ncgb::deriveSABDevice( in );
+    auto t2 = std::chrono::steady_clock::now();
+    if ( ms_host ) *ms_host = std::chrono::duration<double, std::milli>( t1 - t0 ).count();
+    if ( ms_device ) *ms_device = std::chrono::duration<double, std::milli>( t2 - t1 ).count();
+    long long bad = 0, ndiff = 0;
+    double maxrel = 0.0;
+    compareDerived( h, d, maxrel, ndiff, bad );
     if ( max_rel_diff ) *max_rel_diff = maxrel;
     if ( n_double_diff ) *n_double_diff = ndiff;
     if ( n_int_mismatch ) *n_int_mismatch = bad;
+    return 0;
+  } catch ( std::exception& e ) {
+    t_lasterr = e.what();
+    return 1;
+  }
+}
+
+/* The same over every S(alpha,beta) component of n bundles, the device side
+ * as one batched derivation (ncgb_create_scatters' path).  ncomp receives
+ * the number of components; the times are the totals over all of them. */
+int ncgb_sab_derive_compare_many( const char* const* bundle_paths, unsigned long n, double* max_rel_diff,
+                                  long long* n_double_diff, long long* n_int_mismatch, long long* ncomp,
+                                  double* ms_host, double* ms_device )
+{
+  try {
+    std::vector<std::map<int, ncgb::SABInput>> inputs;
+    std::vector<const ncgb::SABInput*> flat;
+    for ( unsigned long i = 0; i < n; ++i )
+      inputs.push_back( ncgb::sabInputs( ncgb::Bundle::load( bundle_paths[i] ) ) );
+    for ( auto& m : inputs )
+      for ( auto& kv : m )
+        flat.push_back( &kv.second );
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<ncgb::SABDerived> h;
+    for ( auto* in : flat )
+      h.push_back( ncgb::deriveSAB( *in ) );
+    auto t1 = std::chrono::steady_clock::now();
+    std::vector<ncgb::SABDerived> d = ncgb::deriveSABDeviceMany( flat );
+    auto t2 = std::chrono::steady_clock::now();
+    if ( ms_host ) *ms_host = std::chrono::duration<double, std::milli>( t1 - t0 ).count();
+    if ( ms_device ) *ms_device = std::chrono::duration<double, std::milli>( t2 - t1 ).count();
+    long long bad = 0, ndiff = 0;
+    double maxrel = 0.0;
+    if ( d.size() != h.size() )
+      ++bad;
+    for ( std::size_t i = 0; i < h.size() && i < d.size(); ++i )
+      compareDerived( h[i], d[i], maxrel, ndiff, bad );
+    if ( max_rel_diff ) *max_rel_diff = maxrel;
+    if ( n_double_diff ) *n_double_diff = ndiff;
+    if ( n_int_mismatch ) *n_int_mismatch = bad;
+    if ( ncomp ) *ncomp = static_cast<long long>( flat.size() );
     return 0;
   } catch ( std::exception& e ) {
     t_lasterr = e.what();

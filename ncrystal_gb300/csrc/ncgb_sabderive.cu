@@ -294,15 +294,36 @@ namespace {
 
 namespace ncgb {
 
-  // deriveSAB on the current CUDA device: same outputs as the host builder.
-  SABDerived deriveSABDevice( const SABInput& in )
+  // deriveSAB on the current CUDA device for many components at once (one
+  // allocation, one copy per array type each way, the kernels launched per
+  // component on one stream): same outputs as the host builder.
+  std::vector<SABDerived> deriveSABDeviceMany( const std::vector<const SABInput*>& ins )
   {
-    const size_t na = in.alpha.size(), nb = in.beta.size(), ne = in.egrid.size();
-    if ( na < 2 || nb < 2 || in.sab.size() != na * nb )
-      throw Error( "SAB kernel with inconsistent grid sizes" );
-    if ( ne < 2 )
-      throw Error( "SAB energy grid too small" );
-    const size_t nslot = ne * ( nb + 1 );
+    const size_t nc = ins.size();
+    std::vector<SABDerived> out( nc );
+    if ( nc == 0 )
+      return out;
+    struct Sz { size_t na, nb, ne, nslot; };
+    std::vector<Sz> sz( nc );
+    for ( size_t k = 0; k < nc; ++k ) {
+      const SABInput& in = *ins[k];
+      sz[k] = { in.alpha.size(), in.beta.size(), in.egrid.size(), in.egrid.size() * ( in.beta.size() + 1 ) };
+      if ( sz[k].na < 2 || sz[k].nb < 2 || in.sab.size() != sz[k].na * sz[k].nb )
+        throw Error( "SAB kernel with inconsistent grid sizes" );
+      if ( sz[k].ne < 2 )
+        throw Error( "SAB energy grid too small" );
+    }
+    // per-component element offsets into the concatenated arrays
+    std::vector<size_t> oa( nc + 1, 0 ), ob( nc + 1, 0 ), os( nc + 1, 0 ), oe( nc + 1, 0 ), orw( nc + 1, 0 ),
+                        osl( nc + 1, 0 );
+    for ( size_t k = 0; k < nc; ++k ) {
+      oa[k + 1] = oa[k] + sz[k].na;
+      ob[k + 1] = ob[k] + sz[k].nb;
+      os[k + 1] = os[k] + sz[k].na * sz[k].nb;
+      oe[k + 1] = oe[k] + sz[k].ne;
+      orw[k + 1] = orw[k] + sz[k].ne * sz[k].nb;
+      osl[k + 1] = osl[k] + sz[k].nslot;
+    }
     double *d_alpha, *d_beta, *d_sab, *d_egrid, *d_log, *d_cum, *d_bx, *d_by, *d_bcdf, *d_xs, *d_fbkep;
     double *c_bx, *c_by, *c_bcdf;
     ncgb_alpha_info *d_info, *c_info;
@@ -314,96 +335,133 @@ namespace ncgb {
       Carve c;
       if ( pass == 1 )
         c.base = static_cast<char*>( blk.p );
-      d_alpha = c.take<double>( na );
-      d_beta = c.take<double>( nb );
-      d_sab = c.take<double>( na * nb );
-      d_egrid = c.take<double>( ne );
-      d_log = c.take<double>( na * nb );
-      d_cum = c.take<double>( na * nb );
-      d_rows = c.take<BetaRow>( ne * nb );
-      d_bx = c.take<double>( nslot );
-      d_by = c.take<double>( nslot );
-      d_bcdf = c.take<double>( nslot );
-      d_info = c.take<ncgb_alpha_info>( nslot );
-      c_bx = c.take<double>( nslot );
-      c_by = c.take<double>( nslot );
-      c_bcdf = c.take<double>( nslot );
-      c_info = c.take<ncgb_alpha_info>( nslot );
-      d_xs = c.take<double>( ne );
-      d_fbkep = c.take<double>( ne );
-      d_kind = c.take<int32_t>( ne );
-      d_ibl = c.take<int32_t>( ne );
-      d_nbeta = c.take<int32_t>( ne );
-      d_off = c.take<int64_t>( ne );
+      d_alpha = c.take<double>( oa[nc] );
+      d_beta = c.take<double>( ob[nc] );
+      d_sab = c.take<double>( os[nc] );
+      d_egrid = c.take<double>( oe[nc] );
+      d_log = c.take<double>( os[nc] );
+      d_cum = c.take<double>( os[nc] );
+      d_rows = c.take<BetaRow>( orw[nc] );
+      d_bx = c.take<double>( osl[nc] );
+      d_by = c.take<double>( osl[nc] );
+      d_bcdf = c.take<double>( osl[nc] );
+      d_info = c.take<ncgb_alpha_info>( osl[nc] );
+      c_bx = c.take<double>( osl[nc] );
+      c_by = c.take<double>( osl[nc] );
+      c_bcdf = c.take<double>( osl[nc] );
+      c_info = c.take<ncgb_alpha_info>( osl[nc] );
+      d_xs = c.take<double>( oe[nc] );
+      d_fbkep = c.take<double>( oe[nc] );
+      d_kind = c.take<int32_t>( oe[nc] );
+      d_ibl = c.take<int32_t>( oe[nc] );
+      d_nbeta = c.take<int32_t>( oe[nc] );
+      d_off = c.take<int64_t>( oe[nc] );
       d_err = c.take<int32_t>( 1 );
       if ( pass == 0 )
         check( cudaMalloc( &blk.p, c.used ), "cudaMalloc" );
     }
-    check( cudaMemcpy( d_alpha, in.alpha.data(), na * 8, cudaMemcpyHostToDevice ), "H2D" );
-    check( cudaMemcpy( d_beta, in.beta.data(), nb * 8, cudaMemcpyHostToDevice ), "H2D" );
-    check( cudaMemcpy( d_sab, in.sab.data(), na * nb * 8, cudaMemcpyHostToDevice ), "H2D" );
-    check( cudaMemcpy( d_egrid, in.egrid.data(), ne * 8, cudaMemcpyHostToDevice ), "H2D" );
-    check( cudaMemset( d_err, 0, 4 ), "memset" );
-    k_logcumul<<<( (int)nb + 127 ) / 128, 128>>>( d_alpha, d_sab, (int)na, (int)nb, d_log, d_cum );
-    check( cudaGetLastError(), "k_logcumul" );
-    k_betarows<<<dim3( ( (unsigned)nb + 127 ) / 128, (unsigned)ne ), 128>>>( d_alpha, d_beta, d_sab, d_log, d_cum,
-                                                                           (int)na, (int)nb, d_egrid, in.kT, d_rows );
-    check( cudaGetLastError(), "k_betarows" );
-    k_epoints<<<( (int)ne + 63 ) / 64, 64>>>( d_beta, (int)nb, d_egrid, (int)ne, in.kT, in.sigma_bound, d_rows, d_bx,
-                                              d_by, d_bcdf, d_info, d_xs, d_kind, d_ibl, d_nbeta, d_fbkep, d_err );
-    check( cudaGetLastError(), "k_epoints" );
-    // per-point offsets (the scan over ~ne counts is done on the host)
-    std::vector<int32_t> kind( ne ), ibl( ne ), nbeta( ne );
-    check( cudaMemcpy( nbeta.data(), d_nbeta, ne * 4, cudaMemcpyDeviceToHost ), "D2H" );
-    std::vector<int64_t> offs( ne );
-    int64_t tot = 0;
-    for ( size_t ie = 0; ie < ne; ++ie ) {
-      offs[ie] = tot;
-      tot += nbeta[ie];
+    {
+      // inputs concatenated on the host, one copy per array type
+      std::vector<double> ha( oa[nc] ), hb( ob[nc] ), hs( os[nc] ), he( oe[nc] );
+      for ( size_t k = 0; k < nc; ++k ) {
+        std::memcpy( ha.data() + oa[k], ins[k]->alpha.data(), sz[k].na * 8 );
+        std::memcpy( hb.data() + ob[k], ins[k]->beta.data(), sz[k].nb * 8 );
+        std::memcpy( hs.data() + os[k], ins[k]->sab.data(), sz[k].na * sz[k].nb * 8 );
+        std::memcpy( he.data() + oe[k], ins[k]->egrid.data(), sz[k].ne * 8 );
+      }
+      check( cudaMemcpy( d_alpha, ha.data(), ha.size() * 8, cudaMemcpyHostToDevice ), "H2D" );
+      check( cudaMemcpy( d_beta, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice ), "H2D" );
+      check( cudaMemcpy( d_sab, hs.data(), hs.size() * 8, cudaMemcpyHostToDevice ), "H2D" );
+      check( cudaMemcpy( d_egrid, he.data(), he.size() * 8, cudaMemcpyHostToDevice ), "H2D" );
     }
-    check( cudaMemcpy( d_off, offs.data(), ne * 8, cudaMemcpyHostToDevice ), "H2D" );
-    k_compact<<<dim3( ( (unsigned)nb + 128 ) / 128, (unsigned)ne ), 128>>>( (int)ne, (int)nb, d_nbeta, d_off, d_bx,
-                                                                           d_by, d_bcdf, d_info, c_bx, c_by, c_bcdf,
-                                                                           c_info );
+    check( cudaMemset( d_err, 0, 4 ), "memset" );
+    for ( size_t k = 0; k < nc; ++k ) {
+      const int na = (int)sz[k].na, nb = (int)sz[k].nb, ne = (int)sz[k].ne;
+      k_logcumul<<<( nb + 127 ) / 128, 128>>>( d_alpha + oa[k], d_sab + os[k], na, nb, d_log + os[k], d_cum + os[k] );
+      k_betarows<<<dim3( ( (unsigned)nb + 127 ) / 128, (unsigned)ne ), 128>>>(
+        d_alpha + oa[k], d_beta + ob[k], d_sab + os[k], d_log + os[k], d_cum + os[k], na, nb, d_egrid + oe[k],
+        ins[k]->kT, d_rows + orw[k] );
+      k_epoints<<<( ne + 63 ) / 64, 64>>>( d_beta + ob[k], nb, d_egrid + oe[k], ne, ins[k]->kT, ins[k]->sigma_bound,
+                                           d_rows + orw[k], d_bx + osl[k], d_by + osl[k], d_bcdf + osl[k],
+                                           d_info + osl[k], d_xs + oe[k], d_kind + oe[k], d_ibl + oe[k],
+                                           d_nbeta + oe[k], d_fbkep + oe[k], d_err );
+    }
+    check( cudaGetLastError(), "table derivation kernels" );
+    // per-point offsets of every component (host scan over the small counts)
+    std::vector<int32_t> kind( oe[nc] ), ibl( oe[nc] ), nbeta( oe[nc] );
+    check( cudaMemcpy( nbeta.data(), d_nbeta, oe[nc] * 4, cudaMemcpyDeviceToHost ), "D2H" );
+    std::vector<int64_t> offs( oe[nc] );
+    std::vector<size_t> ot( nc + 1, 0 );   // concatenated compact totals
+    for ( size_t k = 0; k < nc; ++k ) {
+      int64_t tot = 0;
+      for ( size_t ie = 0; ie < sz[k].ne; ++ie ) {
+        offs[oe[k] + ie] = tot;
+        tot += nbeta[oe[k] + ie];
+      }
+      ot[k + 1] = ot[k] + (size_t)tot;
+    }
+    // compact positions: component k's points start at ot[k] in c_*
+    std::vector<int64_t> goffs( oe[nc] );
+    for ( size_t k = 0; k < nc; ++k )
+      for ( size_t ie = 0; ie < sz[k].ne; ++ie )
+        goffs[oe[k] + ie] = (int64_t)ot[k] + offs[oe[k] + ie];
+    check( cudaMemcpy( d_off, goffs.data(), oe[nc] * 8, cudaMemcpyHostToDevice ), "H2D" );
+    for ( size_t k = 0; k < nc; ++k ) {
+      const int nb = (int)sz[k].nb, ne = (int)sz[k].ne;
+      k_compact<<<dim3( ( (unsigned)nb + 128 ) / 128, (unsigned)ne ), 128>>>(
+        ne, nb, d_nbeta + oe[k], d_off + oe[k], d_bx + osl[k], d_by + osl[k], d_bcdf + osl[k], d_info + osl[k],
+        c_bx, c_by, c_bcdf, c_info );
+    }
     check( cudaGetLastError(), "k_compact" );
-    SABDerived d;
-    d.logsab.resize( na * nb );
-    d.cumul.resize( na * nb );
-    std::vector<double> xs( ne ), fbk( ne );
+    std::vector<double> logs( os[nc] ), cums( os[nc] ), xs( oe[nc] ), fbk( oe[nc] );
+    std::vector<double> bx( ot[nc] ), by( ot[nc] ), bcdf( ot[nc] );
+    std::vector<ncgb_alpha_info> info( ot[nc] );
     int32_t err = 0;
-    check( cudaMemcpy( d.logsab.data(), d_log, na * nb * 8, cudaMemcpyDeviceToHost ), "D2H" );
-    check( cudaMemcpy( d.cumul.data(), d_cum, na * nb * 8, cudaMemcpyDeviceToHost ), "D2H" );
-    check( cudaMemcpy( xs.data(), d_xs, ne * 8, cudaMemcpyDeviceToHost ), "D2H" );
-    check( cudaMemcpy( fbk.data(), d_fbkep, ne * 8, cudaMemcpyDeviceToHost ), "D2H" );
-    check( cudaMemcpy( kind.data(), d_kind, ne * 4, cudaMemcpyDeviceToHost ), "D2H" );
-    check( cudaMemcpy( ibl.data(), d_ibl, ne * 4, cudaMemcpyDeviceToHost ), "D2H" );
+    check( cudaMemcpy( logs.data(), d_log, os[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
+    check( cudaMemcpy( cums.data(), d_cum, os[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
+    check( cudaMemcpy( xs.data(), d_xs, oe[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
+    check( cudaMemcpy( fbk.data(), d_fbkep, oe[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
+    check( cudaMemcpy( kind.data(), d_kind, oe[nc] * 4, cudaMemcpyDeviceToHost ), "D2H" );
+    check( cudaMemcpy( ibl.data(), d_ibl, oe[nc] * 4, cudaMemcpyDeviceToHost ), "D2H" );
     check( cudaMemcpy( &err, d_err, 4, cudaMemcpyDeviceToHost ), "D2H" );
     if ( err )
       throw Error( "PointwiseDist: invalid beta distribution at an energy-grid point" );
-    d.bx.resize( tot );
-    d.by.resize( tot );
-    d.bcdf.resize( tot );
-    d.info.resize( tot );
-    if ( tot ) {
-      check( cudaMemcpy( d.bx.data(), c_bx, tot * 8, cudaMemcpyDeviceToHost ), "D2H" );
-      check( cudaMemcpy( d.by.data(), c_by, tot * 8, cudaMemcpyDeviceToHost ), "D2H" );
-      check( cudaMemcpy( d.bcdf.data(), c_bcdf, tot * 8, cudaMemcpyDeviceToHost ), "D2H" );
-      check( cudaMemcpy( d.info.data(), c_info, tot * sizeof(ncgb_alpha_info), cudaMemcpyDeviceToHost ), "D2H" );
+    if ( ot[nc] ) {
+      check( cudaMemcpy( bx.data(), c_bx, ot[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
+      check( cudaMemcpy( by.data(), c_by, ot[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
+      check( cudaMemcpy( bcdf.data(), c_bcdf, ot[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
+      check( cudaMemcpy( info.data(), c_info, ot[nc] * sizeof(ncgb_alpha_info), cudaMemcpyDeviceToHost ), "D2H" );
     }
-    // per-point arrays in the host builder's layout (NCSABIntegrator.cc:283-309)
-    d.xs = xs;
-    for ( size_t ie = 0; ie < ne; ++ie ) {
-      d.kind.push_back( kind[ie] );
-      d.offset.push_back( offs[ie] );
-      d.ibetaoffset.push_back( kind[ie] ? ibl[ie] : 0 );
-      d.nbeta.push_back( kind[ie] ? nbeta[ie] : 0 );
-      d.fbkep.push_back( kind[ie] ? fbk[ie] : 0.0 );
+    for ( size_t k = 0; k < nc; ++k ) {
+      SABDerived& d = out[k];
+      const SABInput& in = *ins[k];
+      d.logsab.assign( logs.begin() + os[k], logs.begin() + os[k + 1] );
+      d.cumul.assign( cums.begin() + os[k], cums.begin() + os[k + 1] );
+      d.xs.assign( xs.begin() + oe[k], xs.begin() + oe[k + 1] );
+      d.bx.assign( bx.begin() + ot[k], bx.begin() + ot[k + 1] );
+      d.by.assign( by.begin() + ot[k], by.begin() + ot[k + 1] );
+      d.bcdf.assign( bcdf.begin() + ot[k], bcdf.begin() + ot[k + 1] );
+      d.info.assign( info.begin() + ot[k], info.begin() + ot[k + 1] );
+      // per-point arrays in the host builder's layout (NCSABIntegrator.cc:283-309)
+      for ( size_t ie = 0; ie < sz[k].ne; ++ie ) {
+        const size_t g = oe[k] + ie;
+        d.kind.push_back( kind[g] );
+        d.offset.push_back( offs[g] );
+        d.ibetaoffset.push_back( kind[g] ? ibl[g] : 0 );
+        d.nbeta.push_back( kind[g] ? nbeta[g] : 0 );
+        d.fbkep.push_back( kind[g] ? fbk[g] : 0.0 );
+      }
+      const double emax = in.egrid.back();
+      const double extxs_emax = in.ext_sigma_free * freeGasXSShapeASq( in.ext_ca * emax );
+      d.kext = ( d.xs.back() - extxs_emax ) * emax;
+      d.k1 = d.xs.back() * emax;
+      d.k2 = extxs_emax * emax;
     }
-    const double emax = in.egrid.back();
-    const double extxs_emax = in.ext_sigma_free * freeGasXSShapeASq( in.ext_ca * emax );
-    d.kext = ( d.xs.back() - extxs_emax ) * emax;
-    d.k1 = d.xs.back() * emax;
-    d.k2 = extxs_emax * emax;
-    return d;
+    return out;
+  }
+
+  SABDerived deriveSABDevice( const SABInput& in )
+  {
+    return std::move( deriveSABDeviceMany( { &in } ).front() );
   }
 }

@@ -350,7 +350,34 @@ namespace ncgb {
     return v && std::string( v ) == "device";
   }
 
+  std::map<int, SABInput> sabInputs( const Bundle& b )
+  {
+    std::map<int, SABInput> out;
+    const int nc = static_cast<int>( b.i64s( "ncomp" ) );
+    for ( int ic = 0; ic < nc; ++ic ) {
+      const std::string p = "c" + std::to_string( ic ) + ".";
+      if ( !b.has( p + "sab" ) )
+        continue;
+      SABInput in;
+      in.alpha = b.f64( p + "alpha" );
+      in.beta = b.f64( p + "beta" );
+      in.sab = b.f64( p + "sab" );
+      in.egrid = b.f64( p + "egrid" );
+      in.kT = b.f64s( p + "sab_kT" );
+      in.sigma_bound = b.f64s( p + "sigma_bound" );
+      in.ext_sigma_free = b.f64s( p + "ext_sigma_free" );
+      in.ext_ca = b.f64s( p + "ext_ca" );
+      out.emplace( ic, std::move( in ) );
+    }
+    return out;
+  }
+
   std::shared_ptr<MaterialTables> MaterialTables::build( const Bundle& b )
+  {
+    return build( b, nullptr );
+  }
+
+  std::shared_ptr<MaterialTables> MaterialTables::build( const Bundle& b, const std::map<int, SABDerived>* pre )
   {
     auto mt = std::make_shared<MaterialTables>();
     mt->m_cfg = b.str("cfg");
@@ -414,7 +441,9 @@ namespace ncgb {
         in.sigma_bound = b.f64s(p+"sigma_bound");
         in.ext_sigma_free = b.f64s(p+"ext_sigma_free");
         in.ext_ca = b.f64s(p+"ext_ca");
-        SABDerived d = deviceDerive() ? deriveSABDevice( in ) : deriveSAB( in );
+        const auto it = pre ? pre->find( ic ) : std::map<int, SABDerived>::const_iterator();
+        SABDerived d = ( pre && it != pre->end() ) ? it->second
+                       : ( deviceDerive() ? deriveSABDevice( in ) : deriveSAB( in ) );
         ncgb_sab_view& s = c.sab;
         s.kT = b.f64s(p+"kT");
         s.egrid_margin = b.f64s(p+"egrid_margin");
