@@ -19,6 +19,9 @@
 // exp differ from the host's in the last place.
 #include <cuda_runtime.h>
 
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -297,12 +300,54 @@ namespace ncgb {
   // deriveSAB on the current CUDA device for many components at once (one
   // allocation, one copy per array type each way, the kernels launched per
   // component on one stream): same outputs as the host builder.
+  // Up to 16 non-blocking streams, handed out round-robin; destroyed at scope exit.
+  struct Streams {
+    std::vector<cudaStream_t> s;
+    explicit Streams( size_t n )
+    {
+      s.resize( n < 16 ? ( n ? n : 1 ) : 16 );
+      for ( auto& x : s )
+        check( cudaStreamCreateWithFlags( &x, cudaStreamNonBlocking ), "cudaStreamCreate" );
+    }
+    ~Streams()
+    {
+      for ( auto x : s )
+        cudaStreamDestroy( x );
+    }
+    Streams( const Streams& ) = delete;
+    Streams& operator=( const Streams& ) = delete;
+    cudaStream_t operator[]( size_t k ) const { return s[k % s.size()]; }
+    void sync() const
+    {
+      for ( auto x : s )
+        check( cudaStreamSynchronize( x ), "table derivation kernels" );
+    }
+  };
+
   std::vector<SABDerived> deriveSABDeviceMany( const std::vector<const SABInput*>& ins )
   {
     const size_t nc = ins.size();
     std::vector<SABDerived> out( nc );
     if ( nc == 0 )
       return out;
+    // NCGB_TABLES_TIMING=1: wall-clock time of each phase on stderr
+    static const bool timing = [] {
+      const char* v = std::getenv( "NCGB_TABLES_TIMING" );
+      return v && *v && *v != '0';
+    }();
+    auto tmark = std::chrono::steady_clock::now();
+    std::string tlog;
+    auto mark = [&]( const char* what ) {
+      if ( !timing )
+        return;
+      cudaDeviceSynchronize();
+      auto now = std::chrono::steady_clock::now();
+      char buf[96];
+      std::snprintf( buf, sizeof buf, " %s %.1f ms;", what,
+                     std::chrono::duration<double, std::milli>( now - tmark ).count() );
+      tlog += buf;
+      tmark = now;
+    };
     struct Sz { size_t na, nb, ne, nslot; };
     std::vector<Sz> sz( nc );
     for ( size_t k = 0; k < nc; ++k ) {
@@ -360,33 +405,40 @@ namespace ncgb {
       if ( pass == 0 )
         check( cudaMalloc( &blk.p, c.used ), "cudaMalloc" );
     }
-    {
-      // inputs concatenated on the host, one copy per array type
-      std::vector<double> ha( oa[nc] ), hb( ob[nc] ), hs( os[nc] ), he( oe[nc] );
-      for ( size_t k = 0; k < nc; ++k ) {
-        std::memcpy( ha.data() + oa[k], ins[k]->alpha.data(), sz[k].na * 8 );
-        std::memcpy( hb.data() + ob[k], ins[k]->beta.data(), sz[k].nb * 8 );
-        std::memcpy( hs.data() + os[k], ins[k]->sab.data(), sz[k].na * sz[k].nb * 8 );
-        std::memcpy( he.data() + oe[k], ins[k]->egrid.data(), sz[k].ne * 8 );
-      }
-      check( cudaMemcpy( d_alpha, ha.data(), ha.size() * 8, cudaMemcpyHostToDevice ), "H2D" );
-      check( cudaMemcpy( d_beta, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice ), "H2D" );
-      check( cudaMemcpy( d_sab, hs.data(), hs.size() * 8, cudaMemcpyHostToDevice ), "H2D" );
-      check( cudaMemcpy( d_egrid, he.data(), he.size() * 8, cudaMemcpyHostToDevice ), "H2D" );
+    mark( "allocation" );
+    // inputs straight from each component's arrays to its place on the device
+    for ( size_t k = 0; k < nc; ++k ) {
+      check( cudaMemcpy( d_alpha + oa[k], ins[k]->alpha.data(), sz[k].na * 8, cudaMemcpyHostToDevice ), "H2D" );
+      check( cudaMemcpy( d_beta + ob[k], ins[k]->beta.data(), sz[k].nb * 8, cudaMemcpyHostToDevice ), "H2D" );
+      check( cudaMemcpy( d_sab + os[k], ins[k]->sab.data(), sz[k].na * sz[k].nb * 8, cudaMemcpyHostToDevice ),
+             "H2D" );
+      check( cudaMemcpy( d_egrid + oe[k], ins[k]->egrid.data(), sz[k].ne * 8, cudaMemcpyHostToDevice ), "H2D" );
     }
+    mark( "inputs to device" );
     check( cudaMemset( d_err, 0, 4 ), "memset" );
+    // the legacy-stream copies and memset finished before the non-blocking
+    // streams below start (a pageable copy may return before its DMA ends)
+    check( cudaDeviceSynchronize(), "H2D" );
+    // Components are independent, and k_logcumul / k_epoints run a serial
+    // loop per beta row / energy point on a handful of blocks: each
+    // component's chain goes to one of several streams so that the
+    // components run side by side.
+    Streams st( nc );
     for ( size_t k = 0; k < nc; ++k ) {
       const int na = (int)sz[k].na, nb = (int)sz[k].nb, ne = (int)sz[k].ne;
-      k_logcumul<<<( nb + 127 ) / 128, 128>>>( d_alpha + oa[k], d_sab + os[k], na, nb, d_log + os[k], d_cum + os[k] );
-      k_betarows<<<dim3( ( (unsigned)nb + 127 ) / 128, (unsigned)ne ), 128>>>(
+      cudaStream_t sk = st[k];
+      k_logcumul<<<( nb + 127 ) / 128, 128, 0, sk>>>( d_alpha + oa[k], d_sab + os[k], na, nb, d_log + os[k], d_cum + os[k] );
+      k_betarows<<<dim3( ( (unsigned)nb + 127 ) / 128, (unsigned)ne ), 128, 0, sk>>>(
         d_alpha + oa[k], d_beta + ob[k], d_sab + os[k], d_log + os[k], d_cum + os[k], na, nb, d_egrid + oe[k],
         ins[k]->kT, d_rows + orw[k] );
-      k_epoints<<<( ne + 63 ) / 64, 64>>>( d_beta + ob[k], nb, d_egrid + oe[k], ne, ins[k]->kT, ins[k]->sigma_bound,
+      k_epoints<<<( ne + 63 ) / 64, 64, 0, sk>>>( d_beta + ob[k], nb, d_egrid + oe[k], ne, ins[k]->kT, ins[k]->sigma_bound,
                                            d_rows + orw[k], d_bx + osl[k], d_by + osl[k], d_bcdf + osl[k],
                                            d_info + osl[k], d_xs + oe[k], d_kind + oe[k], d_ibl + oe[k],
                                            d_nbeta + oe[k], d_fbkep + oe[k], d_err );
     }
     check( cudaGetLastError(), "table derivation kernels" );
+    st.sync();
+    mark( "derivation kernels" );
     // per-point offsets of every component (host scan over the small counts)
     std::vector<int32_t> kind( oe[nc] ), ibl( oe[nc] ), nbeta( oe[nc] );
     check( cudaMemcpy( nbeta.data(), d_nbeta, oe[nc] * 4, cudaMemcpyDeviceToHost ), "D2H" );
@@ -406,19 +458,18 @@ namespace ncgb {
       for ( size_t ie = 0; ie < sz[k].ne; ++ie )
         goffs[oe[k] + ie] = (int64_t)ot[k] + offs[oe[k] + ie];
     check( cudaMemcpy( d_off, goffs.data(), oe[nc] * 8, cudaMemcpyHostToDevice ), "H2D" );
+    check( cudaDeviceSynchronize(), "H2D" );
     for ( size_t k = 0; k < nc; ++k ) {
       const int nb = (int)sz[k].nb, ne = (int)sz[k].ne;
-      k_compact<<<dim3( ( (unsigned)nb + 128 ) / 128, (unsigned)ne ), 128>>>(
+      k_compact<<<dim3( ( (unsigned)nb + 128 ) / 128, (unsigned)ne ), 128, 0, st[k]>>>(
         ne, nb, d_nbeta + oe[k], d_off + oe[k], d_bx + osl[k], d_by + osl[k], d_bcdf + osl[k], d_info + osl[k],
         c_bx, c_by, c_bcdf, c_info );
     }
     check( cudaGetLastError(), "k_compact" );
-    std::vector<double> logs( os[nc] ), cums( os[nc] ), xs( oe[nc] ), fbk( oe[nc] );
-    std::vector<double> bx( ot[nc] ), by( ot[nc] ), bcdf( ot[nc] );
-    std::vector<ncgb_alpha_info> info( ot[nc] );
+    st.sync();
+    mark( "compaction" );
+    std::vector<double> xs( oe[nc] ), fbk( oe[nc] );
     int32_t err = 0;
-    check( cudaMemcpy( logs.data(), d_log, os[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
-    check( cudaMemcpy( cums.data(), d_cum, os[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
     check( cudaMemcpy( xs.data(), d_xs, oe[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
     check( cudaMemcpy( fbk.data(), d_fbkep, oe[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
     check( cudaMemcpy( kind.data(), d_kind, oe[nc] * 4, cudaMemcpyDeviceToHost ), "D2H" );
@@ -426,22 +477,22 @@ namespace ncgb {
     check( cudaMemcpy( &err, d_err, 4, cudaMemcpyDeviceToHost ), "D2H" );
     if ( err )
       throw Error( "PointwiseDist: invalid beta distribution at an energy-grid point" );
-    if ( ot[nc] ) {
-      check( cudaMemcpy( bx.data(), c_bx, ot[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
-      check( cudaMemcpy( by.data(), c_by, ot[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
-      check( cudaMemcpy( bcdf.data(), c_bcdf, ot[nc] * 8, cudaMemcpyDeviceToHost ), "D2H" );
-      check( cudaMemcpy( info.data(), c_info, ot[nc] * sizeof(ncgb_alpha_info), cudaMemcpyDeviceToHost ), "D2H" );
-    }
+    // results straight into each component's arrays
+    auto fetch = []( auto& vec, const auto* src, size_t n ) {
+      vec.resize( n );
+      if ( n )
+        check( cudaMemcpy( vec.data(), src, n * sizeof( *src ), cudaMemcpyDeviceToHost ), "D2H" );
+    };
     for ( size_t k = 0; k < nc; ++k ) {
       SABDerived& d = out[k];
       const SABInput& in = *ins[k];
-      d.logsab.assign( logs.begin() + os[k], logs.begin() + os[k + 1] );
-      d.cumul.assign( cums.begin() + os[k], cums.begin() + os[k + 1] );
+      fetch( d.logsab, d_log + os[k], os[k + 1] - os[k] );
+      fetch( d.cumul, d_cum + os[k], os[k + 1] - os[k] );
+      fetch( d.bx, c_bx + ot[k], ot[k + 1] - ot[k] );
+      fetch( d.by, c_by + ot[k], ot[k + 1] - ot[k] );
+      fetch( d.bcdf, c_bcdf + ot[k], ot[k + 1] - ot[k] );
+      fetch( d.info, c_info + ot[k], ot[k + 1] - ot[k] );
       d.xs.assign( xs.begin() + oe[k], xs.begin() + oe[k + 1] );
-      d.bx.assign( bx.begin() + ot[k], bx.begin() + ot[k + 1] );
-      d.by.assign( by.begin() + ot[k], by.begin() + ot[k + 1] );
-      d.bcdf.assign( bcdf.begin() + ot[k], bcdf.begin() + ot[k + 1] );
-      d.info.assign( info.begin() + ot[k], info.begin() + ot[k + 1] );
       // per-point arrays in the host builder's layout (NCSABIntegrator.cc:283-309)
       for ( size_t ie = 0; ie < sz[k].ne; ++ie ) {
         const size_t g = oe[k] + ie;
@@ -457,6 +508,10 @@ namespace ncgb {
       d.k1 = d.xs.back() * emax;
       d.k2 = extxs_emax * emax;
     }
+    mark( "results to host" );
+    if ( timing )
+      std::fprintf( stderr, "ncgb table derivation (%zu components, %.1f MB compact):%s\n", nc,
+                    ot[nc] * ( 24.0 + sizeof( ncgb_alpha_info ) ) / 1e6, tlog.c_str() );
     return out;
   }
 
