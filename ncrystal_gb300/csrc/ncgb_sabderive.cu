@@ -34,22 +34,45 @@ namespace {
 
   using namespace ncgb::sabd;
 
+  constexpr unsigned kFull = 0xffffffffu;
+
+  // One warp per beta row: log S in parallel, then the cumulative alpha
+  // integrals (NCSABIntegrator.cc:119-138).  The interval integrals are
+  // computed by the lanes side by side and added into the running sum in
+  // the host's order (lane k's partial after term k), so the sums are the
+  // host's to the bit.
   __global__ void k_logcumul( const double* alpha, const double* sab, int na, int nb, double* logsab, double* cumul )
   {
-    const int ib = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ib = ( blockIdx.x * blockDim.x + threadIdx.x ) >> 5;
+    const int lane = threadIdx.x & 31;
     if ( ib >= nb )
-      return;
+      return;   // the whole warp
     const size_t g0 = (size_t)ib * na;
-    for ( int ai = 0; ai < na; ++ai ) {
+    for ( int ai = lane; ai < na; ai += 32 ) {
       const double e = sab[g0 + ai];
       logsab[g0 + ai] = e > 0.0 ? log( e ) : -INFINITY;
     }
+    __syncwarp();
+    if ( lane == 0 )
+      cumul[g0] = 0.0;
     double c = 0.0;
-    cumul[g0] = 0.0;
-    for ( int ai = 0; ai + 1 < na; ++ai ) {
-      c += integrateAlphaIntervalFast( alpha[ai], sab[g0 + ai], alpha[ai + 1], sab[g0 + ai + 1], logsab[g0 + ai],
-                                       logsab[g0 + ai + 1] );
-      cumul[g0 + ai + 1] = c;
+    for ( int base = 0; base + 1 < na; base += 32 ) {
+      const int ai = base + lane;
+      double t = 0.0;
+      if ( ai + 1 < na )
+        t = integrateAlphaIntervalFast( alpha[ai], sab[g0 + ai], alpha[ai + 1], sab[g0 + ai + 1], logsab[g0 + ai],
+                                        logsab[g0 + ai + 1] );
+      double mine = 0.0;
+      for ( int k = 0; k < 32; ++k ) {
+        const double tk = __shfl_sync( kFull, t, k );
+        if ( base + k + 1 < na ) {
+          c += tk;
+          if ( lane == k )
+            mine = c;
+        }
+      }
+      if ( ai + 1 < na )
+        cumul[g0 + ai + 1] = mine;
     }
   }
 
@@ -144,17 +167,23 @@ namespace {
   }
 
   // The ordered part of analyseEnergyPoint (NCSABIntegrator.cc:384-559) and
-  // the PointwiseDist normalisation, one thread per energy point.  Per point
+  // the PointwiseDist normalisation, one warp per energy point.  Per point
   // the outputs occupy [ie*(nb+1), ie*(nb+1)+nbeta) of bx/by/bcdf and
-  // [ie*(nb+1), ...+nbeta-1) of info.
+  // [ie*(nb+1), ...+nbeta-1) of info.  The rows are taken 32 at a time: a
+  // lane's place in the output is its rank among the kept rows (a row equal
+  // to the lower beta limit is dropped), its trapezoid uses the previous kept
+  // row (a shuffle, or the carry from the last chunk), and the Neumaier sums
+  // add the terms in the host's order, so every value is the host's.
   __global__ void k_epoints( const double* beta, int nb, const double* egrid, int ne, double kT, double sigma_bound,
                              const BetaRow* rows, double* bx, double* by, double* bcdf, ncgb_alpha_info* info,
                              double* xs_out, int32_t* kind, int32_t* ibl_out, int32_t* nbeta_out, double* fbkep,
                              int32_t* err )
   {
-    const int ie = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ie = ( blockIdx.x * blockDim.x + threadIdx.x ) >> 5;
+    const int lane = threadIdx.x & 31;
     if ( ie >= ne )
-      return;
+      return;   // the whole warp
+    const unsigned below = ( 1u << lane ) - 1u;
     const double x = egrid[ie] / kT;
     const BetaRow* rr = rows + (size_t)ie * nb;
     const size_t o = (size_t)ie * ( nb + 1 );
@@ -168,81 +197,136 @@ namespace {
       starts = false;
     }
     int ibeta_low = nb;
-    for ( int ib = 0; ib < nb; ++ib )
-      if ( rr[ib].inrange ) { ibeta_low = ib; break; }
-    xs_out[ie] = 0.0;
-    kind[ie] = 0;
-    ibl_out[ie] = 0;
-    nbeta_out[ie] = 0;
-    fbkep[ie] = 0.0;
+    for ( int base = 0; base < nb; base += 32 ) {
+      const unsigned m = __ballot_sync( kFull, base + lane < nb && rr[base + lane].inrange );
+      if ( m ) { ibeta_low = base + __ffs( m ) - 1; break; }
+    }
+    if ( lane == 0 ) {
+      xs_out[ie] = 0.0;
+      kind[ie] = 0;
+      ibl_out[ie] = 0;
+      nbeta_out[ie] = 0;
+      fbkep[ie] = 0.0;
+    }
     if ( ibeta_low >= nb )
       return;
     if ( ibeta_low > 0 && beta_lower_limit < beta[ibeta_low - 1] ) {
       beta_lower_limit = beta[ibeta_low - 1];
       starts = false;
     }
-    double prev_first = beta_lower_limit, prev_second = 0.0;
-    int n = 0;
-    bx[o] = prev_first;
-    by[o] = prev_second;
-    ++n;
+    // carry across chunks (the same in every lane)
+    double prev_first = beta_lower_limit, prev_second = 0.0, bx0 = beta_lower_limit;
+    int n = 1;
     StableSum tot;
     bool next_ep = starts;
-    for ( int ib = ibeta_low; ib < nb; ++ib ) {
-      const double b = beta[ib];
-      if ( b == beta_lower_limit )
-        continue;
-      const double xsb = rr[ib].xs;
-      info[o + n - 1] = rr[ib].info;
-      if ( next_ep ) {
-        next_ep = false;
-        const double db_real = b - prev_first;
-        prev_first -= db_real * ( 1.0 / 3.0 );
-        bx[o] = prev_first;
+    for ( int base = ibeta_low; base < nb; base += 32 ) {
+      const int ib = base + lane;
+      double b = 0.0, xsb = 0.0;
+      bool keep = false;
+      if ( ib < nb ) {
+        b = beta[ib];
+        keep = !( b == beta_lower_limit );
+        if ( keep )
+          xsb = rr[ib].xs;
       }
-      tot.add( 0.5 * ( b - prev_first ) * ( xsb + prev_second ) );
-      prev_first = b;
-      prev_second = xsb;
-      bx[o + n] = prev_first;
-      by[o + n] = prev_second;
-      ++n;
+      const unsigned m = __ballot_sync( kFull, keep );
+      // the previous kept row: a lower lane of this chunk, else the carry
+      const unsigned lower = m & below;
+      const int pl = lower ? 31 - __clz( lower ) : 0;
+      const double sb = __shfl_sync( kFull, b, pl ), sx = __shfl_sync( kFull, xsb, pl );
+      double pf = lower ? sb : prev_first;
+      const double ps = lower ? sx : prev_second;
+      const bool first_ep = keep && next_ep && !lower;
+      if ( first_ep ) {
+        const double db_real = b - pf;
+        pf -= db_real * ( 1.0 / 3.0 );
+      }
+      double term = 0.0;
+      if ( keep ) {
+        term = 0.5 * ( b - pf ) * ( xsb + ps );
+        const int pos = n + __popc( lower );
+        info[o + pos - 1] = rr[ib].info;
+        bx[o + pos] = b;
+        by[o + pos] = xsb;
+      }
+      for ( int k = 0; k < 32; ++k ) {
+        const double tk = __shfl_sync( kFull, term, k );
+        if ( ( m >> k ) & 1u )
+          tot.add( tk );
+      }
+      if ( m ) {
+        const int fl = __ffs( m ) - 1, ll = 31 - __clz( m );
+        const double pfm = __shfl_sync( kFull, pf, fl );
+        if ( next_ep )
+          bx0 = pfm;
+        next_ep = false;
+        prev_first = __shfl_sync( kFull, b, ll );
+        prev_second = __shfl_sync( kFull, xsb, ll );
+        n += __popc( m );
+      }
+    }
+    if ( lane == 0 ) {
+      bx[o] = bx0;
+      by[o] = 0.0;
     }
     double xs_total = tot.sum() * sigma_bound / ( 4 * x );
     if ( !( xs_total >= 0.0 ) )
       xs_total = 0.0;
-    xs_out[ie] = xs_total;
+    if ( lane == 0 )
+      xs_out[ie] = xs_total;
     if ( xs_total == 0.0 )
       return;
-    kind[ie] = 1;
-    ibl_out[ie] = ibeta_low;
-    nbeta_out[ie] = n;
-    fbkep[ie] = starts ? beta_lower_limit : 1.0;
+    if ( lane == 0 ) {
+      kind[ie] = 1;
+      ibl_out[ie] = ibeta_low;
+      nbeta_out[ie] = n;
+      fbkep[ie] = starts ? beta_lower_limit : 1.0;
+    }
+    __syncwarp();
     // PointwiseDist (NCPointwiseDist.cc:28-74)
-    StableSum area;
-    bcdf[o] = 0.0;
-    for ( int i = 0; i < n; ++i ) {
+    for ( int i = lane; i < n; i += 32 ) {
       const double y = by[o + i];
       if ( y < 0.0 || isinf( y ) || ( i > 0 && bx[o + i] < bx[o + i - 1] ) )
         atomicExch( err, 1 );
     }
-    for ( int i = 1; i < n; ++i ) {
-      const double a = ( bx[o + i] - bx[o + i - 1] ) * 0.5 * ( by[o + i] + by[o + i - 1] );
-      if ( a < 0 )
-        atomicExch( err, 1 );
-      area.add( a );
-      bcdf[o + i] = area.sum();
+    StableSum area;
+    if ( lane == 0 )
+      bcdf[o] = 0.0;
+    for ( int base = 1; base < n; base += 32 ) {
+      const int i = base + lane;
+      double a = 0.0;
+      if ( i < n ) {
+        a = ( bx[o + i] - bx[o + i - 1] ) * 0.5 * ( by[o + i] + by[o + i - 1] );
+        if ( a < 0 )
+          atomicExch( err, 1 );
+      }
+      double mine = 0.0;
+      for ( int k = 0; k < 32; ++k ) {
+        const double ak = __shfl_sync( kFull, a, k );
+        if ( base + k < n ) {
+          area.add( ak );
+          if ( lane == k )
+            mine = area.sum();
+        }
+      }
+      if ( i < n )
+        bcdf[o + i] = mine;
     }
     const double tarea = area.sum();
     if ( !( tarea > 0.0 ) ) {
-      atomicExch( err, 1 );
+      if ( lane == 0 )
+        atomicExch( err, 1 );
       return;
     }
     const double nf = 1.0 / tarea;
-    for ( int i = 0; i < n; ++i ) {
+    __syncwarp();
+    for ( int i = lane; i < n; i += 32 ) {
       bcdf[o + i] *= nf;
       by[o + i] *= nf;
     }
-    bcdf[o + n - 1] = 1.0;
+    __syncwarp();
+    if ( lane == 0 )
+      bcdf[o + n - 1] = 1.0;
   }
 
   // Compaction into the host builder's layout: energy point ie's nbeta beta
@@ -427,11 +511,11 @@ namespace ncgb {
     for ( size_t k = 0; k < nc; ++k ) {
       const int na = (int)sz[k].na, nb = (int)sz[k].nb, ne = (int)sz[k].ne;
       cudaStream_t sk = st[k];
-      k_logcumul<<<( nb + 127 ) / 128, 128, 0, sk>>>( d_alpha + oa[k], d_sab + os[k], na, nb, d_log + os[k], d_cum + os[k] );
+      k_logcumul<<<( nb + 3 ) / 4, 128, 0, sk>>>( d_alpha + oa[k], d_sab + os[k], na, nb, d_log + os[k], d_cum + os[k] );
       k_betarows<<<dim3( ( (unsigned)nb + 127 ) / 128, (unsigned)ne ), 128, 0, sk>>>(
         d_alpha + oa[k], d_beta + ob[k], d_sab + os[k], d_log + os[k], d_cum + os[k], na, nb, d_egrid + oe[k],
         ins[k]->kT, d_rows + orw[k] );
-      k_epoints<<<( ne + 63 ) / 64, 64, 0, sk>>>( d_beta + ob[k], nb, d_egrid + oe[k], ne, ins[k]->kT, ins[k]->sigma_bound,
+      k_epoints<<<( ne + 3 ) / 4, 128, 0, sk>>>( d_beta + ob[k], nb, d_egrid + oe[k], ne, ins[k]->kT, ins[k]->sigma_bound,
                                            d_rows + orw[k], d_bx + osl[k], d_by + osl[k], d_bcdf + osl[k],
                                            d_info + osl[k], d_xs + oe[k], d_kind + oe[k], d_ibl + oe[k],
                                            d_nbeta + oe[k], d_fbkep + oe[k], d_err );
