@@ -335,7 +335,7 @@ class SingleRunner:
                 "api": "ncgb_xs_scatter_many%s (C ABI, pinned host arrays; %s)"
                        % ("_f32" if self.f32 else "",
                           "the kernels read the energies from and write the results to host memory over "
-                          "NVLink-C2C" if zc else "chunked copies on two streams")}
+                          "NVLink-C2C" if zc else "chunked copies: copy-in, kernel and copy-out streams")}
 
     def launches_per_step(self):
         return 2
@@ -390,7 +390,7 @@ class BatchRunner:
                 "gpu_launches_per_step": 2,
                 "api": "ncgb_batch_xs_scatter_many (C ABI, pinned host arrays; %s)"
                        % ("kernels read and write host memory over NVLink-C2C" if zc
-                          else "chunked copies on two streams"),
+                          else "chunked copies: copy-in, kernel and copy-out streams"),
                 "autotuned_shape": {"pick_block": self.shape[0], "sab_blocks_per_sm": self.shape[1]}}
 
     def launches_per_step(self):

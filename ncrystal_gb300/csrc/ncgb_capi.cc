@@ -367,8 +367,10 @@ namespace {
   struct Scratch {
     int device = -1;
     cudaStream_t stream = nullptr;
-    cudaStream_t stream2 = nullptr;
+    cudaStream_t stream2 = nullptr;   // host -> device copies of chunked calls
+    cudaStream_t stream3 = nullptr;   // device -> host copies of chunked calls
     cudaEvent_t done = nullptr;
+    cudaEvent_t ev_in[2] = {}, ev_k[2] = {}, ev_out[2] = {};   // per buffer slot of chunked calls
     void* d_in = nullptr; std::size_t cap_in = 0;
     void* d_a = nullptr; std::size_t cap_a = 0;
     void* d_b = nullptr; std::size_t cap_b = 0;
@@ -408,7 +410,13 @@ namespace {
       s.device = dm.device;
       checkCuda( cudaStreamCreateWithFlags( &s.stream, cudaStreamNonBlocking ), "cudaStreamCreate" );
       checkCuda( cudaStreamCreateWithFlags( &s.stream2, cudaStreamNonBlocking ), "cudaStreamCreate" );
+      checkCuda( cudaStreamCreateWithFlags( &s.stream3, cudaStreamNonBlocking ), "cudaStreamCreate" );
       checkCuda( cudaEventCreateWithFlags( &s.done, cudaEventDisableTiming ), "cudaEventCreate" );
+      for ( int h = 0; h < 2; ++h ) {
+        checkCuda( cudaEventCreateWithFlags( &s.ev_in[h], cudaEventDisableTiming ), "cudaEventCreate" );
+        checkCuda( cudaEventCreateWithFlags( &s.ev_k[h], cudaEventDisableTiming ), "cudaEventCreate" );
+        checkCuda( cudaEventCreateWithFlags( &s.ev_out[h], cudaEventDisableTiming ), "cudaEventCreate" );
+      }
       checkCuda( cudaEventRecord( s.done, s.stream ), "cudaEventRecord" );
       void* w = nullptr;
       checkCuda( cudaMalloc( &w, sizeof(ncgb::Work) ), "cudaMalloc" );
@@ -418,6 +426,34 @@ namespace {
   }
 
   uint32_t nextCall( ScatterObj& o ) { return o.callseq.fetch_add( 1, std::memory_order_relaxed ); }
+
+  // Host arrays through the device in chunks of 'chunk' neutrons with two
+  // buffer slots: copies in on stream2, kernels on the handle's stream,
+  // copies out on stream3.  The copy-in of chunk k+2 waits only for the
+  // kernels of chunk k (which read its slot), and the kernels of chunk k+2
+  // for the copy-out of chunk k (which reads theirs), so that both copy
+  // directions and the kernels overlap.  copyIn / launch / copyOut get
+  // (offset, count, slot, stream).  Returns after the last copy-out.
+  template<class CopyIn, class Launch, class CopyOut>
+  void chunkPipeline( Scratch& s, uint64_t n, uint64_t chunk, CopyIn copyIn, Launch launch, CopyOut copyOut )
+  {
+    uint64_t k = 0;
+    for ( uint64_t off = 0; off < n; off += chunk, ++k ) {
+      const uint64_t m = std::min<uint64_t>( chunk, n - off );
+      const int h = static_cast<int>( k & 1 );
+      checkCuda( cudaStreamWaitEvent( s.stream2, s.ev_k[h], 0 ), "cudaStreamWaitEvent" );
+      copyIn( off, m, h, s.stream2 );
+      checkCuda( cudaEventRecord( s.ev_in[h], s.stream2 ), "cudaEventRecord" );
+      checkCuda( cudaStreamWaitEvent( s.stream, s.ev_in[h], 0 ), "cudaStreamWaitEvent" );
+      checkCuda( cudaStreamWaitEvent( s.stream, s.ev_out[h], 0 ), "cudaStreamWaitEvent" );
+      launch( off, m, h, s.stream );
+      checkCuda( cudaEventRecord( s.ev_k[h], s.stream ), "cudaEventRecord" );
+      checkCuda( cudaStreamWaitEvent( s.stream3, s.ev_k[h], 0 ), "cudaStreamWaitEvent" );
+      copyOut( off, m, h, s.stream3 );
+      checkCuda( cudaEventRecord( s.ev_out[h], s.stream3 ), "cudaEventRecord" );
+    }
+    checkCuda( cudaStreamSynchronize( s.stream3 ), "scatter kernels" );
+  }
 
   void checkSize( unsigned long n_ekin, unsigned long repeat )
   {
@@ -586,11 +622,10 @@ namespace {
     return c;
   }
 
-  // Chunked H2D / kernels / D2H pipeline over two streams for the host-array
-  // fused entry points.  Chunk k runs on stream k%2 with the k%2 half of the
-  // staging buffers; the SAB queue and counters are shared, so the kernels of
-  // consecutive chunks are ordered through the 'done' event while the copies
-  // of one chunk overlap the kernels of the other.
+  // The host-array fused entry points: the caller's pinned arrays directly
+  // (zero-copy), or chunkPipeline's H2D / kernels / D2H over two halves of
+  // the staging buffers.  The SAB queue and counters are shared by the
+  // chunks, whose kernels run in order on the handle's stream.
   template<class T>
   void xsScatterHost( ScatterObj& o, const T* ekin, unsigned long n, T* xs, T* ef, T* mu )
   {
@@ -624,32 +659,29 @@ namespace {
     ensure( s.d_c, s.cap_c, 2 * chunk * sizeof(T) );
     ensure( s.d_queue, s.cap_queue, chunk * sizeof(ncgb::QEntry) );
     const uint32_t call = nextCall( o );
-    cudaStream_t st[2] = { s.stream, s.stream2 };
     resetNFail( s, s.stream );
-    uint64_t k = 0;
-    for ( uint64_t off = 0; off < n; off += chunk, ++k ) {
-      const uint64_t m = std::min<uint64_t>( chunk, n - off );
-      const int h = static_cast<int>( k & 1 );
-      cudaStream_t cs = st[h];
-      T* din = static_cast<T*>( s.d_in ) + h * chunk;
-      T* da = static_cast<T*>( s.d_a ) + h * chunk;
-      T* db = static_cast<T*>( s.d_b ) + h * chunk;
-      T* dc = static_cast<T*>( s.d_c ) + h * chunk;
-      checkCuda( cudaMemcpyAsync( din, ekin + off, m * sizeof(T), cudaMemcpyHostToDevice, cs ), "H2D" );
-      ncgb::Batch b = makeBatch( o, s, call );
-      b.ekin = din;
-      b.in_f32 = b.out_f32 = ( sizeof(T) == 4 );
-      b.n_ekin = b.n_out = m;
-      b.index_offset = static_cast<uint32_t>( off );
-      b.out_xs = xs ? da : nullptr;
-      b.out_a = ef ? db : nullptr;
-      b.out_b = mu ? dc : nullptr;
-      runBatch( dm, s, b, cs );
-      if ( xs ) checkCuda( cudaMemcpyAsync( xs + off, da, m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
-      if ( ef ) checkCuda( cudaMemcpyAsync( ef + off, db, m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
-      if ( mu ) checkCuda( cudaMemcpyAsync( mu + off, dc, m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
-    }
-    checkCuda( cudaStreamSynchronize( s.stream2 ), "scatter kernels" );
+    auto slot = [&]( void* base, int h ) { return static_cast<T*>( base ) + h * chunk; };
+    chunkPipeline(
+      s, n, chunk,
+      [&]( uint64_t off, uint64_t m, int h, cudaStream_t cs ) {
+        checkCuda( cudaMemcpyAsync( slot( s.d_in, h ), ekin + off, m * sizeof(T), cudaMemcpyHostToDevice, cs ), "H2D" );
+      },
+      [&]( uint64_t off, uint64_t m, int h, cudaStream_t cs ) {
+        ncgb::Batch b = makeBatch( o, s, call );
+        b.ekin = slot( s.d_in, h );
+        b.in_f32 = b.out_f32 = ( sizeof(T) == 4 );
+        b.n_ekin = b.n_out = m;
+        b.index_offset = static_cast<uint32_t>( off );
+        b.out_xs = xs ? slot( s.d_a, h ) : nullptr;
+        b.out_a = ef ? slot( s.d_b, h ) : nullptr;
+        b.out_b = mu ? slot( s.d_c, h ) : nullptr;
+        runBatch( dm, s, b, cs );
+      },
+      [&]( uint64_t off, uint64_t m, int h, cudaStream_t cs ) {
+        if ( xs ) checkCuda( cudaMemcpyAsync( xs + off, slot( s.d_a, h ), m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
+        if ( ef ) checkCuda( cudaMemcpyAsync( ef + off, slot( s.d_b, h ), m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
+        if ( mu ) checkCuda( cudaMemcpyAsync( mu + off, slot( s.d_c, h ), m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
+      } );
     const unsigned long bad = readNFail( s, s.stream );
     if ( bad )
       throwSamplingFailure( bad );
@@ -1601,7 +1633,7 @@ void ncgb_batch_xs_scatter_many( ncgb_batch_t bt, const double* ekin, const int6
     checkSize( n, 1 );
     if ( n == 0 )
       return;
-    // Chunked H2D / kernels / D2H over two streams, as xsScatterHost: chunk k
+    // Chunked H2D / kernels / D2H (chunkPipeline), as xsScatterHost: chunk k
     // is a launch over neutrons [off, off+m) of the whole batch (the kernels
     // locate materials and random streams from the global index off + o); one
     // call sequence number for the whole call.
@@ -1636,31 +1668,30 @@ void ncgb_batch_xs_scatter_many( ncgb_batch_t bt, const double* ekin, const int6
     ensure( s.d_queue, s.cap_queue, chunk * sizeof(ncgb::QEntry) );
     int64_t* d_off = reinterpret_cast<int64_t*>( static_cast<char*>( s.d_in ) + 2 * chunk * sizeof(double) );
     const uint32_t call = bo.callseq.fetch_add( 1, std::memory_order_relaxed );
-    cudaStream_t st[2] = { s.stream, s.stream2 };
     resetNFail( s, s.stream );
     checkCuda( cudaMemcpyAsync( d_off, offsets, offbytes, cudaMemcpyHostToDevice, s.stream ), "H2D" );
     checkCuda( cudaEventRecord( s.done, s.stream ), "cudaEventRecord" );
-    uint64_t k = 0;
-    for ( uint64_t off = 0; off < n; off += chunk, ++k ) {
-      const uint64_t m = std::min<uint64_t>( chunk, n - off );
-      const int h = static_cast<int>( k & 1 );
-      cudaStream_t cs = st[h];
-      double* din = static_cast<double*>( s.d_in ) + h * chunk;
-      double* da = static_cast<double*>( s.d_a ) + h * chunk;
-      double* db = static_cast<double*>( s.d_b ) + h * chunk;
-      double* dc = static_cast<double*>( s.d_c ) + h * chunk;
-      checkCuda( cudaMemcpyAsync( din, ekin + off, m * sizeof(double), cudaMemcpyHostToDevice, cs ), "H2D" );
-      ncgb::Batch b = multiBatch( bo, s, din, m, xs ? da : nullptr, ef ? db : nullptr, mu ? dc : nullptr, nullptr );
-      b.callseq = call;
-      b.index_offset = static_cast<uint32_t>( off );
-      checkCuda( cudaStreamWaitEvent( cs, s.done, 0 ), "cudaStreamWaitEvent" );
-      checkCuda( ncgb::launchScatterMulti( bo.d_slots, d_off, bo.nmat, b, bo.cfg, cs ), "batch kernels" );
-      checkCuda( cudaEventRecord( s.done, cs ), "cudaEventRecord" );
-      if ( xs ) checkCuda( cudaMemcpyAsync( xs + off, da, m * sizeof(double), cudaMemcpyDeviceToHost, cs ), "D2H" );
-      if ( ef ) checkCuda( cudaMemcpyAsync( ef + off, db, m * sizeof(double), cudaMemcpyDeviceToHost, cs ), "D2H" );
-      if ( mu ) checkCuda( cudaMemcpyAsync( mu + off, dc, m * sizeof(double), cudaMemcpyDeviceToHost, cs ), "D2H" );
-    }
-    checkCuda( cudaStreamSynchronize( s.stream2 ), "batch kernels" );
+    auto slot = [&]( void* base, int h ) { return static_cast<double*>( base ) + h * chunk; };
+    chunkPipeline(
+      s, n, chunk,
+      [&]( uint64_t off, uint64_t m, int h, cudaStream_t cs ) {
+        checkCuda( cudaMemcpyAsync( slot( s.d_in, h ), ekin + off, m * sizeof(double), cudaMemcpyHostToDevice, cs ),
+                   "H2D" );
+      },
+      [&]( uint64_t off, uint64_t m, int h, cudaStream_t cs ) {
+        ncgb::Batch b = multiBatch( bo, s, slot( s.d_in, h ), m, xs ? slot( s.d_a, h ) : nullptr,
+                                    ef ? slot( s.d_b, h ) : nullptr, mu ? slot( s.d_c, h ) : nullptr, nullptr );
+        b.callseq = call;
+        b.index_offset = static_cast<uint32_t>( off );
+        checkCuda( cudaStreamWaitEvent( cs, s.done, 0 ), "cudaStreamWaitEvent" );
+        checkCuda( ncgb::launchScatterMulti( bo.d_slots, d_off, bo.nmat, b, bo.cfg, cs ), "batch kernels" );
+        checkCuda( cudaEventRecord( s.done, cs ), "cudaEventRecord" );
+      },
+      [&]( uint64_t off, uint64_t m, int h, cudaStream_t cs ) {
+        if ( xs ) checkCuda( cudaMemcpyAsync( xs + off, slot( s.d_a, h ), m * sizeof(double), cudaMemcpyDeviceToHost, cs ), "D2H" );
+        if ( ef ) checkCuda( cudaMemcpyAsync( ef + off, slot( s.d_b, h ), m * sizeof(double), cudaMemcpyDeviceToHost, cs ), "D2H" );
+        if ( mu ) checkCuda( cudaMemcpyAsync( mu + off, slot( s.d_c, h ), m * sizeof(double), cudaMemcpyDeviceToHost, cs ), "D2H" );
+      } );
     const unsigned long bad = readNFail( s, s.stream );
     if ( bad )
       throwSamplingFailure( bad );
