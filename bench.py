@@ -133,8 +133,48 @@ def profiled_traffic(kernel, workload_name, key="dram_bytes_per_launch"):
     return None
 
 
+class NvmlClocks:
+    """Read-only NVML queries through ctypes (no Python NVML package needed):
+    the SM clock, its maximum and the clocks-event reasons of one GPU."""
+
+    SM = 1  # NVML_CLOCK_SM
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown",
+               0x4: "sw_power_cap", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index):
+        import ctypes
+        self.C = ctypes
+        lib = None
+        for name in ("libnvidia-ml.so.1", "libnvidia-ml.so"):
+            try:
+                lib = ctypes.CDLL(name)
+                break
+            except OSError:
+                pass
+        if lib is None or lib.nvmlInit_v2() != 0:
+            raise OSError("NVML unavailable")
+        self.lib = lib
+        self.dev = ctypes.c_void_p()
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        nvml_index = int(vis) if vis.strip().isdigit() else index
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(nvml_index), ctypes.byref(self.dev)) != 0:
+            raise OSError("NVML device %d unavailable" % nvml_index)
+        self.max_mhz = self._clock(lib.nvmlDeviceGetMaxClockInfo)
+
+    def _clock(self, fn):
+        v = self.C.c_uint(0)
+        return float(v.value) if fn(self.dev, self.SM, self.C.byref(v)) == 0 else None
+
+    def sample(self):
+        r = self.C.c_ulonglong(0)
+        ok = self.lib.nvmlDeviceGetCurrentClocksEventReasons(self.dev, self.C.byref(r)) == 0
+        names = [nm for bit, nm in self.REASONS.items() if ok and r.value & bit]
+        return self._clock(self.lib.nvmlDeviceGetClockInfo), names
+
+
 class ClockSampler:
-    """nvidia-smi samples (200 ms) during the timed region."""
+    """Clock samples during the timed region: NVML every 2 ms where the
+    driver's NVML library loads, else nvidia-smi every 200 ms."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -146,6 +186,15 @@ class ClockSampler:
         self.lines = []
 
     def __enter__(self):
+        self.nvml, self.samples, self.stop = None, [], threading.Event()
+        try:
+            self.nvml = NvmlClocks(self.index)
+            self.samples.append(self.nvml.sample())
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            return self
+        except (OSError, AttributeError, ValueError):
+            self.nvml = None
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -160,7 +209,15 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def _poll(self):
+        while not self.stop.wait(0.002):
+            self.samples.append(self.nvml.sample())
+
     def __exit__(self, *a):
+        if self.nvml is not None:
+            self.stop.set()
+            self.t.join(timeout=5)
+            self.samples.append(self.nvml.sample())
         if self.proc:
             self.proc.terminate()
             try:
@@ -169,6 +226,12 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml is not None:
+            sm = [c for c, _ in self.samples if c is not None]
+            reasons = sorted({nm for _, names in self.samples for nm in names})
+            if sm:
+                return {"sm_mhz": statistics.median(sm), "sm_max_mhz": self.nvml.max_mhz, "reasons": reasons,
+                        "samples": len(sm), "source": "nvml, 2 ms"}
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
@@ -186,7 +249,7 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi, 200 ms"}
 
 
 def cpu_baseline(wl, seconds, threads=None):
