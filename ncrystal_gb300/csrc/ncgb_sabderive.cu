@@ -408,7 +408,8 @@ namespace ncgb {
     }
   };
 
-  std::vector<SABDerived> deriveSABDeviceMany( const std::vector<const SABInput*>& ins )
+  // One group of components in one device allocation (deriveSABDeviceMany).
+  std::vector<SABDerived> deriveGroup( const std::vector<const SABInput*>& ins )
   {
     const size_t nc = ins.size();
     std::vector<SABDerived> out( nc );
@@ -596,6 +597,43 @@ namespace ncgb {
     if ( timing )
       std::fprintf( stderr, "ncgb table derivation (%zu components, %.1f MB compact):%s\n", nc,
                     ot[nc] * ( 24.0 + sizeof( ncgb_alpha_info ) ) / 1e6, tlog.c_str() );
+    return out;
+  }
+
+  // Device bytes of one component in deriveGroup's allocation (inputs, logS
+  // and cumulative integrals, per-row results, per-point results before and
+  // after compaction, per-point scalars).
+  size_t groupBytes( const SABInput& in )
+  {
+    const size_t na = in.alpha.size(), nb = in.beta.size(), ne = in.egrid.size(), slots = ne * ( nb + 1 );
+    return 8 * ( na + nb + 3 * na * nb + ne ) + sizeof( BetaRow ) * ne * nb
+           + 2 * slots * ( 24 + sizeof( ncgb_alpha_info ) ) + ne * 32 + 4096;
+  }
+
+  // Components in groups whose allocation stays under NCGB_TABLES_DEVICE_MB
+  // (default 16384 MB; a component larger than that is a group of its own),
+  // so that a large temperature grid does not need its whole derivation
+  // resident at once.
+  std::vector<SABDerived> deriveSABDeviceMany( const std::vector<const SABInput*>& ins )
+  {
+    static const size_t budget = [] {
+      const char* v = std::getenv( "NCGB_TABLES_DEVICE_MB" );
+      const long long mb = v ? std::atoll( v ) : 0;
+      return (size_t)( mb > 0 ? mb : 16384 ) << 20;
+    }();
+    std::vector<SABDerived> out;
+    out.reserve( ins.size() );
+    size_t k = 0;
+    while ( k < ins.size() ) {
+      std::vector<const SABInput*> g;
+      size_t bytes = 0;
+      while ( k < ins.size() && ( g.empty() || bytes + groupBytes( *ins[k] ) <= budget ) ) {
+        bytes += groupBytes( *ins[k] );
+        g.push_back( ins[k++] );
+      }
+      for ( auto& d : deriveGroup( g ) )
+        out.push_back( std::move( d ) );
+    }
     return out;
   }
 

@@ -120,3 +120,30 @@ def test_create_scatters_errors():
     with pytest.raises(NC.NCException):
         NC.core.createScatters([W.PE293, "NoSuchMaterial_sg1.ncmat"])
     assert NC.core.createScatters([]) == []
+
+
+_CHILD_GROUPS = r"""
+import json, sys
+import ncrystal_gb300 as NC
+print(json.dumps(NC.core.sab_derive_compare_many(json.loads(sys.argv[1]))))
+"""
+
+
+def test_batched_derivation_in_memory_bounded_groups():
+    """A device budget below one allocation for all components
+    (NCGB_TABLES_DEVICE_MB) splits the derivation into groups with the same
+    results: the same doubles differ from the host builder, by the same
+    largest amount."""
+    cfgs = [W.pe_cfg(T) for T in W.PE_TRAIN_TEMPS] + [W.WATER, W.AL2O3]
+    paths = [bundle_path(c) for c in cfgs]
+    out = {}
+    for mb in ("200", "16384"):
+        env = dict(os.environ, NCGB_TABLES_DEVICE_MB=mb, PYTHONPATH=ROOT)
+        r = subprocess.run([sys.executable, "-c", _CHILD_GROUPS, json.dumps(paths)], env=env, check=True,
+                           cwd=ROOT, capture_output=True, text=True)
+        out[mb] = json.loads(r.stdout.strip().splitlines()[-1])
+        print(mb, "MB", out[mb])
+    a, b = out["200"], out["16384"]
+    assert a["n_int_mismatch"] == 0 and b["n_int_mismatch"] == 0
+    for k in ("ncomp", "n_double_diff", "max_rel_diff"):
+        assert a[k] == b[k], (k, a, b)
