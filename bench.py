@@ -105,6 +105,10 @@ def parse():
                          "and alpha inversion, FP64 elsewhere)")
     ap.add_argument("--cpu-seconds", type=float, default=8.0,
                     help="wall-clock budget of the CPU baseline sample")
+    ap.add_argument("--phase-profile", action="store_true",
+                    help="instead of the benchmark line, print the S(alpha,beta) pass's phase shares "
+                         "(SM-clock cycles per phase, ncgb_sab_phase_profile) for the plain sampler and, "
+                         "where trained, the learned one (single-material workloads)")
     return ap.parse_args()
 
 
@@ -345,9 +349,13 @@ def run_reference(args):
             base = b
     v = statistics.median(vals)
     base["value"] = v
+    cfgd = config_of(args, wl, 1)
+    # the CPU arm runs the reference's algorithm: FP64 throughout, plain sampler
+    cfgd["mode"] = "exact"
+    cfgd["sampler"] = "plain (Alg.1 tables)"
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_of(args, wl, 1),
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfgd,
             "impl": "reference", "cpu_baseline": base,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -518,6 +526,8 @@ def run_gb300(args):
     nbad = R.gate(stream)   # correctness gate before timing: no neutron may fail
     if nbad:
         raise SystemExit("bench: %d neutrons failed to sample" % nbad)
+    if args.phase_profile:
+        return phase_profile(args, R, learned is not None, torch)
 
     def barrier():
         if dist:
@@ -644,6 +654,31 @@ def run_gb300(args):
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+    return 0
+
+
+def phase_profile(args, R, learned, torch):
+    """Phase shares of the S(alpha,beta) pass (cycles summed over lanes) for
+    the plain sampler and the learned one, on the workload's device arrays;
+    the profiled pass's own duration (CUDA events) beside the plain pass's."""
+    if not isinstance(R, SingleRunner) or R.f32:
+        raise SystemExit("bench: --phase-profile needs a single-material FP64 workload")
+    out = {"metric": "S(alpha,beta) pass phase shares (lane cycles)", "workload": args.workload,
+           "mode": args.mode, "neutrons": R.n, "samplers": {}}
+    for sampler in (["plain", "learned"] if learned else ["plain"]):
+        R.set_sampler(sampler)
+        for _ in range(2):
+            R.sc.sab_phase_profile(R.d_e, R.d_xs, R.d_ef, R.d_mu)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        cyc, attempts = R.sc.sab_phase_profile(R.d_e, R.d_xs, R.d_ef, R.d_mu)
+        b.record()
+        torch.cuda.synchronize()
+        tot = sum(cyc.values())
+        out["samplers"][sampler] = {"shares": {k: v / tot for k, v in cyc.items()}, "lane_cycles": tot,
+                                    "alg1_attempts": attempts, "profiled_batch_ms": a.elapsed_time(b)}
+    print(json.dumps(out), flush=True)
     return 0
 
 

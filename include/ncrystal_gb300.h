@@ -178,12 +178,31 @@ int ncgb_scatter_dir_device( ncrystal_scatter_t, const double* d_ekin, const dou
  * in a framework that owns all device memory through its own pool, or one that
  * cannot take cudaMalloc's device-wide synchronisation inside its loop.  All
  * calls share that array: calls that overlap on the GPU race.  The first call
- * on a device looks up the array's address (do it before any stream capture);
- * the device holding the material must be current. */
+ * on a device looks up the array's address (do it before any stream capture)
+ * and keeps it for the life of the device's primary context (do not call it
+ * again after cudaDeviceReset); the device holding the material must be
+ * current.  It computes in the handle's mode with the handle's sampler, like
+ * ncgb_scatter_device, and an empty or refused call consumes no call sequence
+ * number.  Phase timing (ncgb_phase_timing) never applies to its launches. */
 #define NCGB_NOALLOC_MAX_NEUTRONS 1048576u
 int ncgb_scatter_device_noalloc( ncrystal_scatter_t, const double* d_ekin, unsigned long n,
                                  double* d_xs, double* d_ekin_final, double* d_mu,
                                  int32_t* d_status, void* stream );
+
+/* Measurement instrument (no counterpart in the reference): the same batch
+ * as ncgb_scatter_device on FP64 device arrays (synchronous; on the library's
+ * own stream), with the S(alpha,beta) pass replaced by a copy of it that reads
+ * the SM clock at its phase boundaries.  cycles[0..NCGB_SAB_NPHASES) receive
+ * the lanes' summed clock cycles per phase -- claiming a queued neutron and
+ * setting up its sampler, the beta draw, the alpha draw from two rows, the
+ * acceptance tests, the conversion to (E', mu) and its write, and lanes idle
+ * at the end of the pass -- and cycles[NCGB_SAB_NPHASES] the number of Alg.1
+ * attempts.  The clock reads themselves cost registers, so the profiled pass
+ * is slower than the product one; its shares are what it is for.  Returns 0,
+ * or non-zero after setting the error state. */
+#define NCGB_SAB_NPHASES 6
+int ncgb_sab_phase_profile( ncrystal_scatter_t, const double* d_ekin, unsigned long n, double* d_xs,
+                            double* d_ekin_final, double* d_mu, unsigned long long* cycles );
 
 /* Same with FP32 energies in and FP32 results out; all arithmetic in the
  * kernel stays FP64. */
@@ -209,8 +228,7 @@ void ncgb_samplescatterisotropic_many_f32( ncrystal_scatter_t, const float* ekin
  * differ for a small fraction of neutrons (the sampled distributions are
  * unchanged).  New handles start in the mode named by the environment
  * variable NCGB_MODE ("exact" or "mixed"; unset = exact); clones inherit the
- * mode.  ncgb_scatter_device_noalloc always computes in the exact mode.
- * ncgb_set_mode returns 0, or non-zero after setting the error state;
+ * mode.  ncgb_set_mode returns 0, or non-zero after setting the error state;
  * ncgb_get_mode returns the mode, or -1 on error. */
 #define NCGB_MODE_EXACT 0
 #define NCGB_MODE_MIXED 1

@@ -27,7 +27,9 @@ ORACLE = os.path.join(ROOT, "oracle")
 ORACLE_BUILD = os.path.join(ORACLE, "_build")
 REF_OUT = os.path.join(ORACLE, "_ref")
 BUNDLES = os.path.join(PKG, "bundles")
-REFDIR = os.environ.get("NCGB_REFERENCE_DIR", "/root/reference")
+# NCrystal source tree (test oracle and bundle export only): NCGB_REFERENCE_DIR,
+# else a checkout named "reference" beside this repository.
+REFDIR = os.environ.get("NCGB_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
 
 LIBNAME = "libncrystal_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -93,6 +93,8 @@ def lib():
         "ncrystal_lasterrortype": (_C.c_char_p, []),
         "ncrystal_clearerror": (None, []),
         "ncrystal_version": (_C.c_int, []),
+        "ncgb_sab_phase_profile": (_C.c_int, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p, _C.c_void_p,
+                                              _C.c_void_p]),
         "ncgb_scatter_device": (_C.c_int, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p,
                                            _C.c_void_p, _C.c_void_p, _C.c_void_p]),
         "ncgb_scatter_device_f32": (_C.c_int, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p,
@@ -332,6 +334,19 @@ class Scatter(Process):
         if lib().ncgb_sab_egrid(self._h, comp, out.ctypes.data):
             _check()
         return out
+
+    SAB_PHASES = ("claim", "beta", "alpha", "accept", "convert", "idle")
+
+    def sab_phase_profile(self, ekin, xs=None, ekin_final=None, mu=None):
+        """One scatter batch on the float64 CUDA tensor 'ekin' (synchronous)
+        with the S(alpha,beta) pass's phase clocks (ncgb_sab_phase_profile):
+        -> ({phase: summed lane cycles}, Alg.1 attempts)."""
+        out = (_C.c_ulonglong * (len(self.SAB_PHASES) + 1))()
+        p = (lambda t: 0 if t is None else t.data_ptr())
+        if lib().ncgb_sab_phase_profile(self._h, ekin.data_ptr(), ekin.numel(), p(xs), p(ekin_final), p(mu),
+                                        _C.cast(out, _C.c_void_p)):
+            _check()
+        return dict(zip(self.SAB_PHASES, [int(v) for v in out[:-1]])), int(out[-1])
 
     def sab_sample_device(self, comp, ekin, alpha, beta, status=None, stream=None):
         """(alpha, beta) of S(alpha,beta) component 'comp' at the energies of the

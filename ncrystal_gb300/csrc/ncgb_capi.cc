@@ -376,6 +376,7 @@ namespace {
     void* d_b = nullptr; std::size_t cap_b = 0;
     void* d_c = nullptr; std::size_t cap_c = 0;
     void* d_queue = nullptr; std::size_t cap_queue = 0;
+    void* d_phase = nullptr; std::size_t cap_phase = 0;   // phase-profile counters
     ncgb::Work* d_work = nullptr;
     unsigned long last_nfailed = 0;
   };
@@ -1337,20 +1338,61 @@ unsigned long ncgb_device_bytes( ncrystal_scatter_t sc )
 
 }
 
+int ncgb_sab_phase_profile( ncrystal_scatter_t sc, const double* d_ekin, unsigned long n, double* d_xs,
+                            double* d_ef, double* d_mu, unsigned long long* cycles )
+{
+  try {
+    ScatterObj& o = extract( sc.internal, "ncgb_sab_phase_profile" );
+    checkSize( n, 1 );
+    const std::size_t nc = NCGB_SAB_NPHASES + 1;
+    for ( std::size_t k = 0; k < nc; ++k )
+      cycles[k] = 0;
+    if ( n == 0 )
+      return 0;
+    DeviceMaterial& dm = *o.mat;
+    Scratch& s = scratchFor( dm );
+    ensure( s.d_phase, s.cap_phase, nc * sizeof(unsigned long long) );
+    checkCuda( cudaMemsetAsync( s.d_phase, 0, nc * sizeof(unsigned long long), s.stream ), "cudaMemsetAsync" );
+    ncgb::Batch b = makeBatch( o, s, nextCall( o ) );
+    b.ekin = d_ekin;
+    b.n_ekin = b.n_out = n;
+    b.out_xs = d_xs;
+    b.out_a = d_ef;
+    b.out_b = d_mu;
+    b.untimed = 1;
+    b.phase_cycles = static_cast<unsigned long long*>( s.d_phase );
+    runBatch( dm, s, b, s.stream );
+    checkCuda( cudaMemcpyAsync( cycles, s.d_phase, nc * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                s.stream ), "D2H" );
+    checkCuda( cudaStreamSynchronize( s.stream ), "phase-profiled scatter" );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
 // ---- internal hooks for ncgb_noalloc.cu (C++ linkage) ---------------------------------
 namespace ncgb {
 
-  // Validates a handle and returns what a batch launch needs; the call
-  // sequence number is consumed as by any scatter call.  Throws on a bad handle.
+  // Validates a handle and returns what a batch launch needs: the material,
+  // its device, the random-stream key and the arithmetic mode and sampler.
+  // Consumes no call sequence number (handleNextCall does, just before a
+  // launch).  Throws on a bad handle.
   void handleBatchInfo( ncrystal_scatter_t sc, const char* fct, ncgb_material_view* view, int* device,
-                        uint64_t* seed, uint32_t* streamidx, uint32_t* callseq )
+                        uint64_t* seed, uint32_t* streamidx, int* fast, int* learned )
   {
     ScatterObj& o = extract( sc.internal, fct );
     *view = o.mat->view;
     *device = o.mat->device;
     *seed = o.seed;
     *streamidx = o.streamidx;
-    *callseq = nextCall( o );
+    *fast = ( o.mode == NCGB_MODE_MIXED );
+    *learned = ( o.sampler == NCGB_SAMPLER_LEARNED );
+  }
+
+  // The handle's next call sequence number, as every scatter call takes one.
+  uint32_t handleNextCall( ncrystal_scatter_t sc, const char* fct )
+  {
+    return nextCall( extract( sc.internal, fct ) );
   }
 
   // What the MiniMC engine needs of a scatter handle.

@@ -611,6 +611,38 @@ namespace ncgb_dev {
     return elincMuMono<Fast>( rng, ekin, v.msd[pick], status );
   }
 
+  // ---- phase clocks of the S(alpha,beta) pass -----------------------------------------
+  // A measurement instrument: the phase-profiling kernel passes a PhaseClock
+  // through the sampler, every other caller a NoPhases, whose marks compile
+  // to nothing.  end<P>() charges the SM clock cycles since the previous mark
+  // to phase P (per lane: a lane's cycles in a divergent region include the
+  // time its warp spends on the other lanes' paths, so the per-phase sums are
+  // shares of the lanes' wall time).
+  enum { PH_CLAIM = 0, PH_BETA, PH_ALPHA, PH_ACCEPT, PH_CONVERT, PH_IDLE, PH_N };
+  static_assert( PH_N == NCGB_SAB_NPHASES, "phase count of the C ABI" );
+  struct NoPhases {
+    template<int P> __device__ __forceinline__ void end() {}
+    __device__ __forceinline__ void attempt() {}
+  };
+  struct PhaseClock {
+    uint32_t t, attempts;
+    uint32_t acc[PH_N];
+    __device__ __forceinline__ void start()
+    {
+      for ( int i = 0; i < PH_N; ++i )
+        acc[i] = 0;
+      attempts = 0;
+      t = (uint32_t)clock();
+    }
+    template<int P> __device__ __forceinline__ void end()
+    {
+      const uint32_t n = (uint32_t)clock();
+      acc[P] += n - t;
+      t = n;
+    }
+    __device__ __forceinline__ void attempt() { ++attempts; }
+  };
+
   // ---- S(alpha,beta) sampling (Alg.1) -----------------------------------------------
 
   // PointwiseDist::percentileWithIndex, NCPointwiseDist.cc:76-110, with the
@@ -897,10 +929,11 @@ namespace ncgb_dev {
   // (alpha, beta) accepted, 0 if the attempt is rejected, -1 if the learned
   // proposal hit its cap.  Learned: the beta percentile inversion of samplers
   // with an enabled learned proposal is replaced by lpBeta (same distribution).
-  template<bool Fast, bool Learned>
+  template<bool Fast, bool Learned, class Ph>
   __device__ __forceinline__ int alg1Attempt( const ncgb_sab_view& s, int64_t ie, double x, ncgb_rng& rng,
-                                              double& alpha_out, double& beta_out )
+                                              double& alpha_out, double& beta_out, Ph& ph )
   {
+    ph.attempt();
     const int64_t off = __ldg( s.smp_offset + ie );
     const int64_t nbs = __ldg( s.smp_nbeta + ie );
     const double* bx = s.bx + off;
@@ -912,15 +945,22 @@ namespace ncgb_dev {
     if ( Learned && s.lp_hdr && __ldg( &s.lp_hdr[ie].enabled ) ) {
       // the special first bin keeps its probability bcdf[1]; the regular
       // range is drawn from the learned proposal
-      if ( rand_u32( rng ) < __ldg( &s.lp_hdr[ie].c1_thr ) )
-        return alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+      if ( rand_u32( rng ) < __ldg( &s.lp_hdr[ie].c1_thr ) ) {
+        const int r = alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+        ph.template end<PH_BETA>();
+        return r;
+      }
       if ( !lpBeta( s, ie, rng, beta, ibs ) )
         return -1;
     } else {
       beta = percentile( bx, s.bcdf + off, s.bbin + off, nbs, rand01( rng ), ibs );
-      if ( ibs == 0 && fbkep <= 0.0 )
-        return alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+      if ( ibs == 0 && fbkep <= 0.0 ) {
+        const int r = alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+        ph.template end<PH_BETA>();
+        return r;
+      }
     }
+    ph.template end<PH_BETA>();
     if ( beta <= maxd( -x, ldg( s.beta ) ) )
       return 0;
     const double rp = rand01( rng );
@@ -934,6 +974,7 @@ namespace ncgb_dev {
       const float al = sampleAlphaF( s, s.info_f + off, ioff, ibeta - 1, rpf );
       const float ah = sampleAlphaF( s, s.info_f + off, ioff, ibeta, rpf );
       const float af = fmaf( ah - al, (float)( beta - bl ) * __ldg( s.inv_dbeta_f + ibeta - 1 ), al );
+      ph.template end<PH_ALPHA>();
       const ALimF lim = alphaLimitsF( (float)x, (float)( x + beta ), (float)beta );
       if ( af >= lim.lo && af <= lim.hi ) {
         alpha_out = (double)af;
@@ -945,6 +986,7 @@ namespace ncgb_dev {
       const double alphal = sampleAlpha<Fast>( s, infos, ioff, ibeta - 1, rp );
       const double alphah = sampleAlpha<Fast>( s, infos, ioff, ibeta, rp );
       alpha = alphal + ( alphah - alphal ) * ( ( beta - bl ) * ldg( s.inv_dbeta + ibeta - 1 ) );
+      ph.template end<PH_ALPHA>();
     }
     const ALim al = alphaLimits( x, beta );
     if ( inInterval( al.lo, al.hi, alpha ) ) {
@@ -1018,9 +1060,9 @@ namespace ncgb_dev {
 
   // One step of the flattened loops.  Returns -1 to continue, NCGB_ST_OK when
   // (alpha, beta) are final, or an error status.
-  template<bool Fast, bool Learned>
+  template<bool Fast, bool Learned, class Ph = NoPhases>
   __device__ __forceinline__ int sabStepAB( const ncgb_sab_view& s, SABLane& L, ncgb_rng& rng, double& alpha,
-                                            double& beta )
+                                            double& beta, Ph&& ph = Ph() )
   {
     alpha = 0.0;
     beta = 0.0;
@@ -1029,7 +1071,7 @@ namespace ncgb_dev {
       beta = L.pre_beta;
     } else {
       if ( __ldg( s.smp_kind + L.ie ) != 0 ) {
-        const int a = alg1Attempt<Fast, Learned>( s, L.ie, L.xsamp, rng, alpha, beta );
+        const int a = alg1Attempt<Fast, Learned>( s, L.ie, L.xsamp, rng, alpha, beta, ph );
         if ( a < 0 )
           return NCGB_ST_LOOPCAP;
         if ( a == 0 ) {
@@ -1060,15 +1102,17 @@ namespace ncgb_dev {
         return -1;
       }
     }
+    ph.template end<PH_ACCEPT>();
     return NCGB_ST_OK;
   }
 
   // sabStepAB, then (alpha, beta) -> (E', mu).
-  template<bool Fast, bool Learned>
-  __device__ __forceinline__ int sabStep( const ncgb_sab_view& s, SABLane& L, ncgb_rng& rng, double& ef, double& mu )
+  template<bool Fast, bool Learned, class Ph = NoPhases>
+  __device__ __forceinline__ int sabStep( const ncgb_sab_view& s, SABLane& L, ncgb_rng& rng, double& ef, double& mu,
+                                          Ph&& ph = Ph() )
   {
     double alpha, beta;
-    const int st = sabStepAB<Fast, Learned>( s, L, rng, alpha, beta );
+    const int st = sabStepAB<Fast, Learned>( s, L, rng, alpha, beta, ph );
     if ( st != NCGB_ST_OK )
       return st;
     // SABSampler::sampleDeltaEMu (NCSABSampler.cc:229-236), SABScatter

@@ -226,14 +226,12 @@ namespace {
   }
 
   // ---- phase 2: persistent S(alpha,beta) sampling ---------------------------
-  // Full occupancy (8 blocks of 256 per SM, 32 registers): the sampler waits
-  // on table gathers, and more resident warps hide that latency better than
-  // registers avoid spills (measured: 4 blocks 1.64 ms, 6 blocks 1.48 ms,
-  // 8 blocks 1.39 ms per 2^24-neutron polyethylene batch, mixed mode).
-  template<class Src, bool Fast, bool Learned, bool Dir>
-  __global__ void __launch_bounds__(256, 8)
-  k_sab( const __grid_constant__ Src src, const ncgb::Batch b )
+  // The pass over the queue, shared by k_sab and its phase-profiling copy
+  // (Ph: NoPhases, whose marks compile to nothing, or PhaseClock).
+  template<class Src, bool Fast, bool Learned, bool Dir, class Ph>
+  __device__ __forceinline__ void sabPass( const Src& src, const ncgb::Batch& b, Ph& ph )
   {
+    constexpr bool kClocked = !std::is_same<Ph, NoPhases>::value;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned qcount = *(volatile unsigned*)&b.work->qcount;
@@ -279,16 +277,56 @@ namespace {
           }
         }
       }
+      if constexpr ( kClocked ) {
+        if ( done && !has )
+          ph.template end<PH_IDLE>();
+        else
+          ph.template end<PH_CLAIM>();
+      }
       if ( __all_sync( FULL, done && !has ) )
         break;
       if ( has ) {
         double ef = 0.0, mu = 0.0;
-        const int st = sabStep<Fast, Learned>( src.mat( q.mat ).comp[q.comp].sab, L, rng, ef, mu );
+        const int st = sabStep<Fast, Learned>( src.mat( q.mat ).comp[q.comp].sab, L, rng, ef, mu, ph );
         if ( st >= 0 ) {
           writeScatter<Dir>( b, q.idx, q.ekin, st, ef, mu, rng );
           has = false;
+          if constexpr ( kClocked )
+            ph.template end<PH_CONVERT>();
+        } else if constexpr ( kClocked ) {
+          ph.template end<PH_ACCEPT>();
         }
       }
+    }
+  }
+
+  // Full occupancy (8 blocks of 256 per SM, 32 registers): the sampler waits
+  // on table gathers, and more resident warps hide that latency better than
+  // registers avoid spills (measured: 4 blocks 1.64 ms, 6 blocks 1.48 ms,
+  // 8 blocks 1.39 ms per 2^24-neutron polyethylene batch, mixed mode).
+  template<class Src, bool Fast, bool Learned, bool Dir>
+  __global__ void __launch_bounds__(256, 8)
+  k_sab( const __grid_constant__ Src src, const ncgb::Batch b )
+  {
+    NoPhases ph;
+    sabPass<Src, Fast, Learned, Dir>( src, b, ph );
+  }
+
+  // The same pass with per-lane phase clocks (a measurement instrument,
+  // launched by ncgb_sab_phase_profile only): the lanes' SM-clock cycles per
+  // phase and their Alg.1 attempts, summed into b.phase_cycles[PH_N + 1].
+  template<bool Fast, bool Learned>
+  __global__ void __launch_bounds__(256, 8)
+  k_sab_phases( const __grid_constant__ SingleSrc src, const ncgb::Batch b )
+  {
+    PhaseClock ph;
+    ph.start();
+    sabPass<SingleSrc, Fast, Learned, false>( src, b, ph );
+    const int lane = threadIdx.x & 31;
+    for ( int i = 0; i <= PH_N; ++i ) {
+      const unsigned v = __reduce_add_sync( 0xffffffffu, i < PH_N ? ph.acc[i] : ph.attempts );
+      if ( lane == 0 )
+        atomicAdd( b.phase_cycles + i, (unsigned long long)v );
     }
   }
 
@@ -407,6 +445,22 @@ namespace {
   template<class Src, bool Dir>
   void launchSab( const Src& src, const ncgb::Batch& b, int grid, cudaStream_t s )
   {
+    if constexpr ( std::is_same<Src, SingleSrc>::value && !Dir ) {
+      if ( b.phase_cycles ) {
+        if ( b.fast ) {
+          if ( b.learned )
+            k_sab_phases<true, true><<<grid, 256, 0, s>>>( src, b );
+          else
+            k_sab_phases<true, false><<<grid, 256, 0, s>>>( src, b );
+        } else {
+          if ( b.learned )
+            k_sab_phases<false, true><<<grid, 256, 0, s>>>( src, b );
+          else
+            k_sab_phases<false, false><<<grid, 256, 0, s>>>( src, b );
+        }
+        return;
+      }
+    }
     if ( b.fast ) {
       if ( b.learned )
         k_sab<Src, true, true, Dir><<<grid, 256, 0, s>>>( src, b );
@@ -429,7 +483,7 @@ namespace {
     if ( e != cudaSuccess )
       return e;
     PhaseEvents ev{ nullptr, nullptr, nullptr };
-    const bool timing = g_timing;
+    const bool timing = g_timing && !b.untimed;
     if ( timing ) {
       cudaEventCreate( &ev.a );
       cudaEventCreate( &ev.b );

@@ -64,6 +64,11 @@ namespace ncgb {
     int32_t* status;   // may be null
     const uint32_t* rng_index;   // if set (with directions only): neutron o draws from stream
                                  // (seed, rng_index[o], callseq, stream) instead
+    int untimed;       // never record phase-timing events for this batch
+    unsigned long long* phase_cycles;  // non-null (single material, no directions): run the
+                                       // S(alpha,beta) pass with phase clocks, summing the
+                                       // lanes' cycles per phase and their Alg.1 attempts here
+                                       // (ncgb_dev::PH_N + 1 counters)
     Work* work;        // scratch, sizeof(Work)
     QEntry* queue;     // scratch, n_out entries
   };

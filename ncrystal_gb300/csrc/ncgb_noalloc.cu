@@ -20,7 +20,17 @@
 // Set-up: the first call on a device, with that device current, looks up the
 // array's device address with cudaGetSymbolAddress (host code cannot use the
 // array's name as a device address).  Make that first call before any stream
-// capture.
+// capture.  The address is kept for the life of the device's primary context:
+// after cudaDeviceReset (or after the primary context is released and
+// created anew) the cached address is stale, so such a caller must not call
+// this entry point again in the same process.
+//
+// Like ncgb_scatter_device it computes in the handle's arithmetic mode with
+// the handle's sampler (the learned proposal needs no extra working memory),
+// and an empty call or a refused call consumes no call sequence number, so a
+// handle draws from the same random streams as with ncgb_scatter_device.  The
+// library's optional phase timing (ncgb_phase_timing) creates CUDA events; it
+// is never applied to this entry point's launches.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -34,7 +44,8 @@
 
 namespace ncgb {
   void handleBatchInfo( ncrystal_scatter_t sc, const char* fct, ncgb_material_view* view, int* device,
-                        uint64_t* seed, uint32_t* streamidx, uint32_t* callseq );
+                        uint64_t* seed, uint32_t* streamidx, int* fast, int* learned );
+  uint32_t handleNextCall( ncrystal_scatter_t sc, const char* fct );
   void reportError( const std::exception& e );
   void reportError( const char* type, const std::string& msg );
 }
@@ -83,11 +94,12 @@ int ncgb_scatter_device_noalloc( ncrystal_scatter_t sc, const double* d_ekin, un
                          + " per call (split the batch, or use ncgb_scatter_device)" );
       return 1;
     }
+    static const char* kFct = "ncgb_scatter_device_noalloc";
     ncgb_material_view view;
-    int matdev = -1;
+    int matdev = -1, fast = 0, learned = 0;
     uint64_t seed = 0;
-    uint32_t streamidx = 0, callseq = 0;
-    ncgb::handleBatchInfo( sc, "ncgb_scatter_device_noalloc", &view, &matdev, &seed, &streamidx, &callseq );
+    uint32_t streamidx = 0;
+    ncgb::handleBatchInfo( sc, kFct, &view, &matdev, &seed, &streamidx, &fast, &learned );
     if ( n == 0 )
       return 0;
     int cur = -1;
@@ -109,8 +121,11 @@ int ncgb_scatter_device_noalloc( ncrystal_scatter_t sc, const double* d_ekin, un
     b.ekin = d_ekin;
     b.n_ekin = b.n_out = n;
     b.seed = seed;
-    b.callseq = callseq;
+    b.callseq = ncgb::handleNextCall( sc, kFct );
     b.stream = streamidx;
+    b.fast = fast;
+    b.learned = learned;
+    b.untimed = 1;
     b.out_xs = d_xs;
     b.out_a = d_ef;
     b.out_b = d_mu;

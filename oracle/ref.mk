@@ -8,7 +8,7 @@
 # Outputs go to oracle/_ref/ only (git-ignored).  The reference sources are read
 # where they lie; nothing is copied into the repository.
 #
-#   make -f oracle/ref.mk -j8 REFDIR=/root/reference
+#   make -f oracle/ref.mk -j8 REFDIR=<NCrystal source tree>
 #
 # The only configure-time file of the reference is include/NCrystal/ncapi.h,
 # made from ncapi.h.in by replacing the @NCRYSTAL_HOOK_FOR_ADDING_DEFINES@
@@ -18,7 +18,9 @@
 # One source (utils/NCCFileUtils.cc) relies on <stdexcept> arriving transitively,
 # which this libstdc++ does not do, hence the forced include.
 
-REFDIR ?= /root/reference
+ifndef REFDIR
+$(error REFDIR must name the NCrystal source tree)
+endif
 OUT    ?= oracle/_ref
 CORE   := $(REFDIR)/ncrystal_core
 CXX    ?= g++

@@ -174,33 +174,34 @@ def test_learned_alpha_beta_vs_plain(nets):
         assert ks_2samp(out[0][0], out[1][0]).pvalue > 1e-3
 
 
-@pytest.mark.parametrize("e0", [0.001, 0.0253, 0.5])
-def test_learned_1e8_distributions_vs_plain_oracle(nets, e0):
+LEARNED_1E8 = [(0.001, "exact"), (0.0253, "exact"), (0.5, "exact"), (None, "mixed")]
+# comparisons of the module's 1e8-event tests (chi-square, KS on E', KS on mu each)
+ALPHA_1E8 = 0.01 / (3 * len(LEARNED_1E8))
+
+
+@pytest.mark.parametrize("e0,mode", LEARNED_1E8,
+                         ids=["%s-%s" % ("loguniform" if e is None else "%g" % e, m) for e, m in LEARNED_1E8])
+def test_learned_1e8_distributions_vs_plain_oracle(nets, e0, mode):
     """1e8 events: the learned GPU sampler against the plain sampler (the CPU
-    oracle, pinned to the reference), binned chi-square + KS, p > 0.01 with a
-    Bonferroni correction over the module's comparisons."""
+    oracle, pinned to the reference), binned chi-square + exact KS, p > 0.01
+    with a Bonferroni correction over the module's comparisons.  e0 None: the
+    benchmark's own configuration (energies log-uniform in [1e-4, 1] eV, the
+    mixed-precision mode with the learned proposal), the GPU and the oracle
+    each on their own draw of 1e8 energies."""
     pytest.importorskip("scipy")
-    from test_gpu_statistics import chi2_two_sample, ks_two_sample_large, oracle_samples
+    from test_gpu_statistics import LOGU, check_same_distribution, oracle_samples, scatter_device
     import torch
     N = 10 ** 8
-    alpha = 0.01 / 9
-    sc = _attached(nets, W.PE293, 1001)
-    e = torch.full((N,), e0, dtype=torch.float64, device="cuda")
-    ef = torch.empty_like(e)
-    mu = torch.empty_like(e)
-    st = torch.empty((N,), dtype=torch.int32, device="cuda")
-    sc.scatter_device(e, None, ef, mu, st)
-    torch.cuda.synchronize()
-    assert int((st != 0).sum()) == 0
-    gef, gmu = ef.cpu().numpy(), mu.cpu().numpy()
-    del e, ef, mu, st
-    oef, omu = oracle_samples(W.PE293, e0, N, seed=2002)
-    lg = np.log(np.maximum(gef, 1e-30) / e0)
-    lo = np.log(np.maximum(oef, 1e-30) / e0)
-    edges = np.unique(np.quantile(np.concatenate([lg[:10 ** 6], lo[:10 ** 6]]), np.linspace(0, 1, 61)))
-    hg, _, _ = np.histogram2d(lg, gmu, bins=[edges, np.linspace(-1, 1, 51)])
-    ho, _, _ = np.histogram2d(lo, omu, bins=[edges, np.linspace(-1, 1, 51)])
-    stat, dof, p = chi2_two_sample(hg.ravel(), ho.ravel())
-    assert p > alpha, "chi2=%.1f dof=%d p=%.3g" % (stat, dof, p)
-    assert ks_two_sample_large(gef, oef) > alpha
-    assert ks_two_sample_large(gmu, omu, seed=1) > alpha
+    sc = _attached(nets, W.PE293, 1001).set_mode(mode)
+    if e0 is None:
+        ge = W.loguniform_energies(N, LOGU[0], LOGU[1], 0x57A7011)
+        oe = W.loguniform_energies(N, LOGU[0], LOGU[1], 0x57A7012)
+        e = torch.as_tensor(ge, device="cuda")
+    else:
+        ge = oe = None
+        e = torch.full((N,), e0, dtype=torch.float64, device="cuda")
+    gef, gmu = scatter_device(sc, e)
+    gef, gmu = gef.cpu().numpy(), gmu.cpu().numpy()
+    del e
+    oef, omu = oracle_samples(W.PE293, e0, N, seed=2002, energies=oe)
+    print(check_same_distribution(gef, gmu, oef, omu, e0, ALPHA_1E8, ge=ge, oe=oe))

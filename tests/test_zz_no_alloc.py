@@ -72,6 +72,30 @@ def test_noalloc_matches_allocating_entry_point(cfg):
         np.testing.assert_allclose(am.cpu().numpy(), rm.cpu().numpy(), rtol=0, atol=1e-12)
 
 
+def test_noalloc_follows_mode_and_skips_empty_calls():
+    """A handle in the mixed mode gets the mixed mode here too, and an empty
+    call consumes no call sequence number: after one, the next call draws the
+    same random streams as the allocating entry point's first call."""
+    import torch
+    bundle_path(W.PE293)
+    L = _lib()
+    n = 100000
+    e = torch.as_tensor(W.loguniform_energies(n, 1e-4, 1.0, 78), dtype=torch.float64, device="cuda")
+    ref = NC.createScatter(W.PE293, seed=SEED).set_mode("mixed")
+    na = NC.createScatter(W.PE293, seed=SEED).set_mode("mixed")
+    stream = torch.cuda.current_stream().cuda_stream
+    rx, ref_ef, rm, rs = _outputs(torch, n)
+    ax, af, am, ast = _outputs(torch, n)
+    assert L.ncgb_scatter_device_noalloc(na._h, e.data_ptr(), 0, None, None, None, None, stream) == 0
+    assert L.ncgb_scatter_device(ref._h, e.data_ptr(), n, rx.data_ptr(), ref_ef.data_ptr(), rm.data_ptr(),
+                                 rs.data_ptr(), stream) == 0
+    assert L.ncgb_scatter_device_noalloc(na._h, e.data_ptr(), n, ax.data_ptr(), af.data_ptr(), am.data_ptr(),
+                                         ast.data_ptr(), stream) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(ast, rs) and int((ast != 0).sum()) == 0
+    assert torch.equal(ax, rx) and torch.equal(af, ref_ef) and torch.equal(am, rm)
+
+
 def test_noalloc_refuses_batches_above_capacity():
     import torch
     bundle_path(W.AL)
