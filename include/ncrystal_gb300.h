@@ -366,6 +366,37 @@ int ncgb_tables_build_proposal( void* tables, int comp, const float* knots, cons
 int ncgb_tables_set_proposal( void* tables, int comp, const void* hdr, const void* slot, const void* cell,
                               const void* seg, unsigned long nseg );
 
+/* Material bundles.  ncrystal_create_scatter looks a cfg-string's bundle up
+ * in NCGB_BUNDLE_PATH, NCGB_BUNDLE_CACHE and the package's bundles/
+ * directory.  If there is none and an exporter library can be loaded
+ * (NCGB_EXPORT_LIB, else libncgb_export.so beside this library; it links the
+ * NCrystal library, whose host-side material loading -- NCMAT parsing, hkl
+ * planes, VDOS expansion, energy grids -- it runs in-process, the way
+ * ncrystal_create_scatter does at ncrystal.cc:1510-1516), the bundle is
+ * exported into the cache directory first, so any cfg-string NCrystal accepts
+ * can be loaded.  Without an exporter a missing bundle is FileNotFound; a
+ * cfg-string NCrystal rejects gives NCrystal's error.  (No counterpart in the
+ * reference, which has no bundles.)
+ *
+ * ncgb_bundle_path writes the path of a cfg-string's bundle (exporting it if
+ * need be) into out[outlen]; ncgb_bundle_cache_dir writes the directory
+ * on-demand exports go to (NCGB_BUNDLE_CACHE, else the package's bundles/).
+ * ncgb_create_scatter_bundle creates a scatter handle for the material of an
+ * explicit bundle file (the NCrystal plugin's bundles carry no cfg-string).
+ * All return 0 / a valid handle, or set the error state. */
+int ncgb_bundle_path( const char* cfgstr, char* out, unsigned long outlen );
+int ncgb_bundle_cache_dir( char* out, unsigned long outlen );
+ncrystal_scatter_t ncgb_create_scatter_bundle( const char* bundle_path, unsigned long seed );
+
+/* One isotropic scatter at energy ekin on the random stream of a caller's
+ * 64-bit key (stream (key, 0, 0, the handle's stream index)), leaving the
+ * handle's own call sequence alone: the scalar sampling of the NCrystal
+ * plugin, whose key comes from NCrystal's RNG (ProcImpl::sampleScatterIsotropic,
+ * NCProcImpl.hh:118-127, takes the caller's RNG).  Synchronous.  Returns 0, or
+ * non-zero with the error state set and (E', mu) = (-1, -999). */
+int ncgb_samplescatterisotropic_keyed( ncrystal_scatter_t, double ekin, unsigned long long key,
+                                       double* ekin_final, double* mu );
+
 /* Creates n scatter handles (the seed of ncrystal_create_scatter_builtinrng)
  * for materials given by cfg-strings, deriving the S(alpha,beta) samplers of
  * all of them in one batched device derivation (a temperature grid, a set of

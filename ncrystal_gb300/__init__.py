@@ -8,6 +8,7 @@ GB300 GPU (sm_103a), behind NCrystal's own C and Python interfaces.
 """
 from .core import (NCBadInput, NCCalcError, NCException, NCFileNotFound,  # noqa: F401
                    MLP, Absorption, Batch, NCLogicError, Process, Scatter, createAbsorption, createProcess,
-                   createScatter, lib, phase_times, phase_timing)
+                   createScatter, createScatterFromBundle, bundle_path, lib, phase_times,
+                   phase_timing)
 
 __version__ = "0.1.0"

@@ -110,7 +110,10 @@ def build_library(force=False, verbose=False):
                 print(o)
     lib = library_path()
     if force or jobs or not os.path.exists(lib):
-        _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart", "-ldl"])
+        # -Bsymbolic: the library's own calls to its exported NCrystal-named
+        # symbols bind inside it, even in a process that has NCrystal loaded
+        # (the plugin, the on-demand exporter)
+        _run([nvcc] + ARCH + ["-shared", "-Xlinker", "-Bsymbolic", "-o", lib] + objs + ["-lcudart", "-ldl"])
     return lib
 
 
@@ -140,23 +143,46 @@ def build_reference(jobs=None):
           "REFDIR=" + REFDIR, "OUT=" + REF_OUT], cwd=ROOT)
     core = os.path.join(REFDIR, "ncrystal_core", "include")
     gen = os.path.join(REF_OUT, "gen")
-    exp_src = os.path.join(PKG, "bundle", "ncgb_export.cc")
+    bdir = os.path.join(PKG, "bundle")
+    exp_src = os.path.join(bdir, "ncgb_export.cc")
+    exp_deps = [exp_src, os.path.join(bdir, "ncgb_export.hh")]
     exp_out = os.path.join(REF_OUT, "ncgb_export")
+    plug_src = os.path.join(PKG, "plugin", "ncgb_plugin.cc")
     rp_src = os.path.join(ORACLE, "refpin.c")
     rp_out = os.path.join(REF_OUT, "librefpin.so")
     lib = os.path.join(REF_OUT, "libNCrystal.so")
+    cxx = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-include", "stdexcept", "-I" + gen, "-I" + core,
+           "-I" + bdir]
+    link = ["-L" + REF_OUT, "-lNCrystal", "-Wl,-rpath," + REF_OUT]
     cmds = []
-    if not _newer(exp_out, [exp_src, lib]):
-        cmds.append(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-include", "stdexcept",
-                     "-I" + gen, "-I" + core, "-o", exp_out, exp_src,
-                     "-L" + REF_OUT, "-lNCrystal", "-Wl,-rpath," + REF_OUT])
+    if not _newer(exp_out, exp_deps + [lib]):
+        cmds.append(cxx + ["-DNCGB_EXPORT_TOOL", "-o", exp_out, exp_src] + link)
+    # the on-demand exporter the library loads for cfg-strings without a
+    # bundle, and the NCrystal plugin; both beside the library
+    os.makedirs(BUILD, exist_ok=True)
+    if not _newer(exporter_path(), exp_deps + [lib]):
+        cmds.append(cxx + ["-fPIC", "-shared", "-o", exporter_path(), exp_src] + link)
+    if not _newer(plugin_path(), exp_deps + [plug_src, lib]):
+        cmds.append(cxx + ["-fPIC", "-shared", "-o", plugin_path(), plug_src, exp_src] + link + ["-ldl"])
     if not _newer(rp_out, [rp_src, lib, os.path.join(INC, "ncgb_philox.h")]):
         cmds.append(["gcc", "-std=c99", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
                      "-I" + INC, "-I" + gen, "-I" + core, "-o", rp_out, rp_src,
                      "-L" + REF_OUT, "-lNCrystal", "-Wl,-rpath," + REF_OUT])
-    with ThreadPoolExecutor(max_workers=2) as ex:
+    with ThreadPoolExecutor(max_workers=max(1, len(cmds))) as ex:
         list(ex.map(_run, cmds))
     return True
+
+
+def exporter_path():
+    """libncgb_export.so: NCrystal's material loading, exported as a bundle on
+    demand (built where the NCrystal sources are)."""
+    return os.path.join(BUILD, "libncgb_export.so")
+
+
+def plugin_path():
+    """The NCrystal plugin libNCrystalPlugin_GB300.so (built where the NCrystal
+    sources are)."""
+    return os.path.join(BUILD, "libNCrystalPlugin_GB300.so")
 
 
 def bundle_file_name(cfg):

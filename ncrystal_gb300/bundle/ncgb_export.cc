@@ -28,6 +28,12 @@
 // Nothing here changes the reference's behaviour.  The tool is built only where
 // the reference sources exist.
 //
+// The same code serves three callers: the ncgb_export tool (built with
+// NCGB_EXPORT_TOOL), the shared library libncgb_export.so, through which the
+// GPU library exports a bundle on demand for a cfg-string that has none
+// (ncgb_export_bundle below), and the NCrystal plugin (ncgb_plugin.cc), which
+// exports the process tree NCrystal's standard factory made for a request.
+//
 // Usage:  ncgb_export [--with-derived] OUT.ncgb "cfg-string"
 
 #include <algorithm>
@@ -53,6 +59,8 @@
 #include <unordered_map>
 #include <utility>
 #include <vector>
+#include <thread>
+#include <unistd.h>
 
 #define private public
 #define protected public
@@ -71,6 +79,8 @@
 #include "NCrystal/internal/absoov/NCAbsOOV.hh"
 #undef private
 #undef protected
+
+#include "ncgb_export.hh"
 
 namespace NC = NCrystal;
 
@@ -93,7 +103,19 @@ namespace {
       Rec r{ n, dt, cnt, std::vector<char>( (const char*)p, (const char*)p + cnt*es ) };
       recs.push_back(std::move(r));
     }
+    // Written to a temporary name in the target's directory and renamed into
+    // place, so that concurrent readers and writers never see a partial file.
     void write( const std::string& path ) const
+    {
+      const std::string tmp = path + ".tmp" + std::to_string( (long)::getpid() ) + "_"
+                              + std::to_string( (unsigned long)std::hash<std::thread::id>()( std::this_thread::get_id() ) );
+      writeTo( tmp );
+      if ( std::rename( tmp.c_str(), path.c_str() ) != 0 ) {
+        std::remove( tmp.c_str() );
+        throw std::runtime_error("cannot rename "+tmp+" to "+path);
+      }
+    }
+    void writeTo( const std::string& path ) const
     {
       std::ofstream f(path, std::ios::binary);
       if (!f) throw std::runtime_error("cannot open "+path);
@@ -250,46 +272,31 @@ namespace {
   }
 }
 
-int main( int argc, char** argv )
-{
-  bool withDerived = false;
-  std::vector<std::string> args;
-  for ( int i = 1; i < argc; ++i ) {
-    if ( std::strcmp(argv[i],"--with-derived") == 0 )
-      withDerived = true;
-    else
-      args.push_back(argv[i]);
-  }
-  if ( args.size() != 2 ) {
-    std::fprintf(stderr,"usage: %s [--with-derived] OUT.ncgb \"cfg-string\"\n",argv[0]);
-    return 2;
-  }
-  try {
-    const std::string& out = args[0];
-    const std::string& cfgstr = args[1];
-    NC::MatCfg cfg(cfgstr);
-    auto sc = NC::createScatter(cfg);
-    const NC::ProcImpl::Process& top = sc.underlying();
+namespace ncgb_export {
+
+  void writeBundle( const std::string& path, const std::string& cfgkey, const NC::ProcImpl::Process& top,
+                    const NC::Info& info, double temperature, const NC::ProcImpl::Process* absorption,
+                    bool withDerived )
+  {
     Bundle b;
-    b.str("cfg", cfgstr);
+    b.str("cfg", cfgkey);
     b.str("ncrystal_version", NCRYSTAL_VERSION_STR);
     auto dom = top.domain();
     b.f64("elow", dom.elow.dbl());
     b.f64("ehigh", dom.ehigh.dbl());
-    b.f64("temperature", cfg.get_temp().dbl());
+    b.f64("temperature", temperature);
     // material information used by the MiniMC engine: number density
     // (macroXSFactor, NCMMC_Utils.hh:103-105), temperature if well defined, and
     // the Bragg threshold as the scenario decoder takes it (the largest over
     // the phases, NCMMC_Utils.cc:218-241); -1 where absent
+    b.f64("info.numdens", info.getNumberDensity().dbl());
+    b.f64("info.temperature", info.hasTemperature() ? info.getTemperature().dbl() : -1.0);
     {
-      auto info = NC::createInfo(cfg);
-      b.f64("info.numdens", info->getNumberDensity().dbl());
-      b.f64("info.temperature", info->hasTemperature() ? info->getTemperature().dbl() : -1.0);
       NC::Optional<NC::NeutronWavelength> bt;
-      if ( info->isSinglePhase() ) {
-        bt = info->getBraggThreshold();
+      if ( info.isSinglePhase() ) {
+        bt = info.getBraggThreshold();
       } else {
-        for ( auto& ph : info->getPhases() ) {
+        for ( auto& ph : info.getPhases() ) {
           auto pbt = ph.second->getBraggThreshold();
           if ( pbt.has_value() && ( !bt.has_value() || bt.value() < pbt.value() ) )
             bt = pbt;
@@ -308,21 +315,94 @@ int main( int argc, char** argv )
     }
     b.i64("ncomp", nc);
     // absorption: the standard factory's AbsOOV (NCStdAbsFact.cc:49-52), xs =
-    // c/sqrt(E) (NCAbsOOV.cc:33-44); c = 0 means no absorption
-    {
-      auto ab = NC::createAbsorption(cfg);
-      const NC::ProcImpl::Process& ap = ab.underlying();
-      if ( auto oov = dynamic_cast<const NC::AbsOOV*>(&ap) )
-        b.f64("abs_c", oov->m_c);
-      else if ( ap.isNull() )
-        b.f64("abs_c", 0.0);
-      else
-        throw std::runtime_error("unsupported absorption process type");
+    // c/sqrt(E) (NCAbsOOV.cc:33-44); c = 0 means no absorption; -1: not recorded
+    if ( !absorption ) {
+      b.f64("abs_c", -1.0);
+    } else if ( auto oov = dynamic_cast<const NC::AbsOOV*>(absorption) ) {
+      b.f64("abs_c", oov->m_c);
+    } else if ( absorption->isNull() ) {
+      b.f64("abs_c", 0.0);
+    } else {
+      throw std::runtime_error("unsupported absorption process type");
     }
-    b.write(out);
+    b.write(path);
+  }
+
+  void exportCfg( const std::string& cfgstr, const std::string& path, bool withDerived )
+  {
+    NC::MatCfg cfg(cfgstr);
+    auto sc = NC::createScatter(cfg);
+    auto info = NC::createInfo(cfg);
+    auto ab = NC::createAbsorption(cfg);
+    writeBundle( path, cfgstr, sc.underlying(), *info, cfg.get_temp().dbl(), &ab.underlying(), withDerived );
+  }
+
+  bool supported( const NC::ProcImpl::Process& top )
+  {
+    auto one = []( const NC::ProcImpl::Process& p ) {
+      return dynamic_cast<const NC::PowderBragg*>(&p) || dynamic_cast<const NC::ElIncScatter*>(&p)
+             || dynamic_cast<const NC::SABScatter*>(&p) || dynamic_cast<const NC::FreeGas*>(&p);
+    };
+    if ( top.isNull() )
+      return true;
+    if ( auto pc = dynamic_cast<const NC::ProcImpl::ProcComposition*>(&top) ) {
+      if ( pc->components().size() > 8 )
+        return false;
+      for ( auto& c : pc->components() )
+        if ( !one( *c.process ) )
+          return false;
+      return true;
+    }
+    return one( top );
+  }
+}
+
+// The bundle of one cfg-string written to 'path'.  Returns 0, or 1 with
+// NCrystal's error message and type name ("FileNotFound", "BadInput", ...)
+// copied into err / type.
+extern "C" int ncgb_export_bundle( const char* cfgstr, const char* path, char* err, unsigned long errlen,
+                                   char* type, unsigned long typelen )
+{
+  auto put = []( char* dst, unsigned long len, const char* src ) {
+    if ( dst && len ) {
+      std::strncpy( dst, src, len - 1 );
+      dst[len - 1] = 0;
+    }
+  };
+  try {
+    ncgb_export::exportCfg( cfgstr, path, false );
+    return 0;
+  } catch ( NC::Error::Exception& e ) {
+    put( err, errlen, e.what() );
+    put( type, typelen, e.getTypeName() );
+  } catch ( std::exception& e ) {
+    put( err, errlen, e.what() );
+    put( type, typelen, "BadInput" );
+  }
+  return 1;
+}
+
+#ifdef NCGB_EXPORT_TOOL
+int main( int argc, char** argv )
+{
+  bool withDerived = false;
+  std::vector<std::string> args;
+  for ( int i = 1; i < argc; ++i ) {
+    if ( std::strcmp(argv[i],"--with-derived") == 0 )
+      withDerived = true;
+    else
+      args.push_back(argv[i]);
+  }
+  if ( args.size() != 2 ) {
+    std::fprintf(stderr,"usage: %s [--with-derived] OUT.ncgb \"cfg-string\"\n",argv[0]);
+    return 2;
+  }
+  try {
+    ncgb_export::exportCfg( args[1], args[0], withDerived );
   } catch ( std::exception& e ) {
     std::fprintf(stderr,"ncgb_export error: %s\n",e.what());
     return 1;
   }
   return 0;
 }
+#endif

@@ -93,6 +93,11 @@ def lib():
         "ncrystal_lasterrortype": (_C.c_char_p, []),
         "ncrystal_clearerror": (None, []),
         "ncrystal_version": (_C.c_int, []),
+        "ncgb_bundle_path": (_C.c_int, [_C.c_char_p, _C.c_char_p, _C.c_ulong]),
+        "ncgb_bundle_cache_dir": (_C.c_int, [_C.c_char_p, _C.c_ulong]),
+        "ncgb_create_scatter_bundle": (H, [_C.c_char_p, _C.c_ulong]),
+        "ncgb_samplescatterisotropic_keyed": (_C.c_int, [H, _C.c_double, _C.c_ulonglong,
+                                                         _C.POINTER(_C.c_double), _C.POINTER(_C.c_double)]),
         "ncgb_sab_phase_profile": (_C.c_int, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p, _C.c_void_p,
                                               _C.c_void_p]),
         "ncgb_scatter_device": (_C.c_int, [H, _C.c_void_p, _C.c_ulong, _C.c_void_p, _C.c_void_p,
@@ -347,6 +352,15 @@ class Scatter(Process):
                                         _C.cast(out, _C.c_void_p)):
             _check()
         return dict(zip(self.SAB_PHASES, [int(v) for v in out[:-1]])), int(out[-1])
+
+    def sample_keyed(self, ekin, key):
+        """One isotropic scatter at 'ekin' on the random stream of a 64-bit
+        key (ncgb_samplescatterisotropic_keyed): -> (E', mu)."""
+        ef, mu = _C.c_double(), _C.c_double()
+        if lib().ncgb_samplescatterisotropic_keyed(self._h, float(ekin), int(key) & 0xFFFFFFFFFFFFFFFF,
+                                                   _C.byref(ef), _C.byref(mu)):
+            _check()
+        return ef.value, mu.value
 
     def sab_sample_device(self, comp, ekin, alpha, beta, status=None, stream=None):
         """(alpha, beta) of S(alpha,beta) component 'comp' at the energies of the
@@ -710,6 +724,26 @@ def phase_times():
     if lib().ncgb_phase_times(_C.byref(a), _C.byref(b), _C.byref(n), _C.byref(q)):
         _check()
     return a.value, b.value, n.value, q.value
+
+
+def bundle_path(cfgstr):
+    """Path of the material bundle of a cfg-string (ncgb_bundle_path): found
+    in the bundle directories, or exported there on demand through NCrystal's
+    own material loading where an exporter library is available."""
+    buf = _C.create_string_buffer(8192)
+    if lib().ncgb_bundle_path(cfgstr.encode(), buf, len(buf)):
+        _check()
+    return buf.value.decode()
+
+
+def createScatterFromBundle(path, seed=0):
+    """A Scatter for the material of an explicit bundle file
+    (ncgb_create_scatter_bundle)."""
+    h = lib().ncgb_create_scatter_bundle(path.encode(), int(seed))
+    _check()
+    if not h.internal:
+        raise NCException("could not create scatter from %r" % path)
+    return Scatter(h, path)
 
 
 def createScatter(cfgstr, seed=None):

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cerrno>
 #include <initializer_list>
 #include <cmath>
 #include <cstdio>
@@ -150,6 +151,30 @@ namespace {
     return f + ".ncgb";
   }
 
+  // Directory of this library's file.
+  std::string libDir()
+  {
+    Dl_info info;
+    if ( dladdr( reinterpret_cast<void*>( &libDir ), &info ) && info.dli_fname ) {
+      std::string lib( info.dli_fname );
+      auto pos = lib.rfind( '/' );
+      return pos == std::string::npos ? std::string( "." ) : lib.substr( 0, pos );
+    }
+    return ".";
+  }
+
+  // Where bundles exported on demand are written: NCGB_BUNDLE_CACHE, else the
+  // package's bundles/ directory (created if missing).
+  std::string bundleCacheDir()
+  {
+    const char* env = std::getenv( "NCGB_BUNDLE_CACHE" );
+    std::string d = env && *env ? std::string( env ) : libDir() + "/../bundles";
+    struct stat st;
+    if ( ::stat( d.c_str(), &st ) != 0 && ::mkdir( d.c_str(), 0755 ) != 0 && errno != EEXIST )
+      throw TypedError( "FileNotFound", "cannot create the bundle cache directory " + d );
+    return d;
+  }
+
   std::vector<std::string> bundleDirs()
   {
     std::vector<std::string> dirs;
@@ -161,15 +186,43 @@ namespace {
       }
       if ( !cur.empty() ) dirs.push_back( cur );
     }
-    Dl_info info;
-    if ( dladdr( reinterpret_cast<void*>( &bundleDirs ), &info ) && info.dli_fname ) {
-      std::string lib( info.dli_fname );
-      auto pos = lib.rfind( '/' );
-      std::string libdir = pos == std::string::npos ? "." : lib.substr( 0, pos );
-      dirs.push_back( libdir + "/../bundles" );
-      dirs.push_back( libdir + "/bundles" );
-    }
+    if ( const char* env = std::getenv( "NCGB_BUNDLE_CACHE" ) )
+      if ( *env )
+        dirs.push_back( env );
+    const std::string libdir = libDir();
+    dirs.push_back( libdir + "/../bundles" );
+    dirs.push_back( libdir + "/bundles" );
     return dirs;
+  }
+
+  // A bundle for a cfg-string that has none: NCrystal's own material loading,
+  // run in this process through the exporter library (NCGB_EXPORT_LIB, else
+  // libncgb_export.so beside this library; it links the NCrystal library).
+  // Returns the bundle's path, or "" with 'why' set if no exporter can be
+  // loaded; throws NCrystal's error if the export itself fails.
+  std::string exportOnDemand( const std::string& cfg, const std::string& fn, std::string& why )
+  {
+    static std::mutex mtx;
+    std::lock_guard<std::mutex> lock( mtx );
+    const char* env = std::getenv( "NCGB_EXPORT_LIB" );
+    const std::string lib = env && *env ? std::string( env ) : libDir() + "/libncgb_export.so";
+    void* dl = dlopen( lib.c_str(), RTLD_NOW | RTLD_LOCAL );
+    if ( !dl ) {
+      const char* e = dlerror();
+      why = "no bundle exporter could be loaded (" + std::string( e ? e : lib ) + ")";
+      return "";
+    }
+    using ExportFn = int ( * )( const char*, const char*, char*, unsigned long, char*, unsigned long );
+    auto fct = reinterpret_cast<ExportFn>( dlsym( dl, "ncgb_export_bundle" ) );
+    if ( !fct ) {
+      why = "the bundle exporter " + lib + " has no ncgb_export_bundle";
+      return "";
+    }
+    const std::string path = bundleCacheDir() + "/" + fn;
+    char err[2048] = { 0 }, type[64] = { 0 };
+    if ( fct( cfg.c_str(), path.c_str(), err, sizeof( err ), type, sizeof( type ) ) != 0 )
+      throw TypedError( *type ? type : "BadInput", std::string( "exporting a bundle for \"" ) + cfg + "\": " + err );
+    return path;
   }
 
   std::string findBundle( const std::string& cfg )
@@ -182,9 +235,14 @@ namespace {
       if ( ::stat( p.c_str(), &st ) == 0 )
         return p;
     }
+    std::string why;
+    const std::string p = exportOnDemand( cfg, fn, why );
+    if ( !p.empty() )
+      return p;
     throw TypedError( "FileNotFound", "No material bundle for cfg \"" + cfg + "\" (looked for " + fn
-                      + " in NCGB_BUNDLE_PATH and the package bundles/ directory). Material bundles are"
-                      " written by ncgb_export, which runs NCrystal's host-side material loading." );
+                      + " in NCGB_BUNDLE_PATH, NCGB_BUNDLE_CACHE and the package bundles/ directory), and "
+                      + why + ". Material bundles are written by NCrystal's host-side material loading"
+                      " (ncgb_export, or libncgb_export.so on demand)." );
   }
 
   // Upload built tables as a device material of the current device and cache it.
@@ -764,6 +822,99 @@ static ncrystal_scatter_t createScatter( const char* cfgstr, uint64_t seed )
   o->cfg = cfgstr;
   o->seed = seed;
   return makeHandle( o.release() );
+}
+
+ncrystal_scatter_t ncgb_create_scatter_bundle( const char* bundle_path, unsigned long seed )
+{
+  try {
+    if ( !bundle_path )
+      throw TypedError( "BadInput", "ncgb_create_scatter_bundle: null path" );
+    const std::string key = std::string( "bundle:" ) + bundle_path;
+    int dev = 0;
+    checkCuda( cudaGetDevice( &dev ), "cudaGetDevice" );
+    std::shared_ptr<DeviceMaterial> mat;
+    {
+      std::lock_guard<std::mutex> lock( g_matmtx );
+      auto it = g_matcache.find( std::make_pair( key, dev ) );
+      if ( it != g_matcache.end() )
+        mat = it->second.lock();
+      if ( !mat ) {
+        auto bundle = ncgb::Bundle::load( bundle_path );
+        mat = uploadMaterial( key, dev, ncgb::MaterialTables::build( bundle ) );
+      }
+    }
+    std::unique_ptr<ScatterObj> o( new ScatterObj );
+    o->mat = mat;
+    o->cfg = key;
+    o->seed = static_cast<uint64_t>( seed );
+    return makeHandle( o.release() );
+  } NCGB_CATCH;
+  return ncrystal_scatter_t{ nullptr };
+}
+
+int ncgb_samplescatterisotropic_keyed( ncrystal_scatter_t sc, double ekin, unsigned long long key,
+                                       double* ekin_final, double* mu )
+{
+  try {
+    if ( !ekin_final || !mu )
+      throw TypedError( "BadInput", "ncgb_samplescatterisotropic_keyed: null output" );
+    *ekin_final = -1.0;
+    *mu = -999.0;
+    ScatterObj& o = extract( sc.internal, "ncgb_samplescatterisotropic_keyed" );
+    DeviceMaterial& dm = *o.mat;
+    Scratch& s = scratchFor( dm );
+    ensure( s.d_in, s.cap_in, sizeof(double) );
+    ensure( s.d_a, s.cap_a, sizeof(double) );
+    ensure( s.d_b, s.cap_b, sizeof(double) );
+    // the neutron's stream: (key, 0, 0, the handle's stream index); the
+    // handle's own call sequence is left alone
+    ncgb::Batch b = makeBatch( o, s, 0 );
+    b.seed = key;
+    b.ekin = s.d_in;
+    b.n_ekin = b.n_out = 1;
+    b.out_a = s.d_a;
+    b.out_b = s.d_b;
+    resetNFail( s, s.stream );
+    checkCuda( cudaMemcpyAsync( s.d_in, &ekin, sizeof(double), cudaMemcpyHostToDevice, s.stream ), "H2D" );
+    runBatch( dm, s, b, s.stream );
+    const unsigned long nfail = readNFail( s, s.stream );
+    if ( nfail )
+      throwSamplingFailure( nfail );
+    double out[2];
+    checkCuda( cudaMemcpyAsync( out, s.d_a, sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    checkCuda( cudaMemcpyAsync( out + 1, s.d_b, sizeof(double), cudaMemcpyDeviceToHost, s.stream ), "D2H" );
+    checkCuda( cudaStreamSynchronize( s.stream ), "D2H" );
+    *ekin_final = out[0];
+    *mu = out[1];
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_bundle_cache_dir( char* out, unsigned long outlen )
+{
+  try {
+    const std::string d = bundleCacheDir();
+    if ( !out || outlen <= d.size() )
+      throw TypedError( "BadInput", "ncgb_bundle_cache_dir: buffer too small" );
+    std::memcpy( out, d.c_str(), d.size() + 1 );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_bundle_path( const char* cfgstr, char* out, unsigned long outlen )
+{
+  try {
+    if ( !cfgstr )
+      throw TypedError( "BadInput", "ncgb_bundle_path: null cfg-string" );
+    const std::string p = findBundle( cfgstr );
+    if ( !out || outlen <= p.size() )
+      throw TypedError( "BadInput", "ncgb_bundle_path: buffer too small" );
+    std::memcpy( out, p.c_str(), p.size() + 1 );
+    return 0;
+  } NCGB_CATCH;
+  return 1;
 }
 
 int ncgb_create_scatters( const char* const* cfgstrs, unsigned long n, unsigned long seed, ncrystal_scatter_t* out )
