@@ -608,10 +608,12 @@ def run_gb300(args):
     achieved = kernels[dom]["achieved_gbs"]
 
     # ---- e2e: host (pinned) arrays through the C ABI, copies timed ----------
-    for _ in range(max(1, args.warmup // 2)):
+    # (as many steps as the device-timed region: a short window is at the
+    # mercy of one host-side stall)
+    for _ in range(max(2, args.warmup)):
         R.e2e_step()
     barrier()
-    e2e_steps = max(3, args.steps // 2)
+    e2e_steps = max(10, args.steps)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         R.e2e_step()
