@@ -614,12 +614,17 @@ def run_gb300(args):
         R.e2e_step()
     barrier()
     e2e_steps = max(10, args.steps)
+    step_s = []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        R.e2e_step()
+        t1 = time.perf_counter()
+        R.e2e_step()   # synchronous: copies in, kernels, copies out
+        step_s.append(time.perf_counter() - t1)
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
-    e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT, "steps": e2e_steps}
+    e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT, "steps": e2e_steps,
+           "step_ms": {"min": 1e3 * min(step_s), "median": 1e3 * statistics.median(step_s),
+                       "max": 1e3 * max(step_s)}}
     e2e.update(R.e2e_info())
 
     if not float(R.d_mu.abs().max().item()) <= 1.0:

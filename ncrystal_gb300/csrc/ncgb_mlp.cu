@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -149,6 +151,186 @@ namespace ncgb_mlp {
               g.Cb[o] = __float2bfloat16( ( g.relu && v < 0.f ) ? 0.f : v );
           }
         }
+  }
+
+  // ---- tcgen05 GEMM (sm_100 family tensor cores, accumulators in TMEM) -------
+  // One CTA of 128 threads computes a 128-row tile of C = A B (all N <= 128
+  // columns, split-K over blockIdx.z as in k_gemm, same epilogues).  Per K
+  // stage of 64, the threads stage A (128 x 64) and B^T (N x 64) as BF16 into
+  // shared memory in the K-major layout with the 128-byte swizzle (rows of
+  // 128 B, the 16-byte chunks of row r XOR-ed with r mod 8, 8-row groups 1 KB
+  // apart), then one thread issues four tcgen05.mma (K = 16 each) into a
+  // 128 x N FP32 accumulator in tensor memory and commits them to an
+  // mbarrier, which every thread waits on (bounded) before the tiles are
+  // reused.  The epilogue reads each warp's 32 accumulator rows with
+  // tcgen05.ld.  Staging is element-wise, so any strides of A and B serve:
+  // the forward (A activations, B weights), the input-gradient and the
+  // weight-gradient (A and B transposed views) products alike.
+  constexpr int TC_M = 128, TC_K = 64;
+  constexpr int TC_TMEM_COLS = 128;
+  // Dynamic shared memory per CTA: the two tiles (32 KB), the barrier and the
+  // TMEM address, 1 KB alignment slack -- and padding to 60 KB, so that at
+  // most three CTAs share an SM and their TMEM (3 x 128 of 512 columns)
+  // allocations never wait on each other.
+  constexpr int TC_SMEM = 60 * 1024;
+  constexpr long TC_WAIT_LIMIT = 1L << 20;
+
+  __device__ __forceinline__ uint32_t smemAddr( const void* p ) { return (uint32_t)__cvta_generic_to_shared( p ); }
+
+  // byte offset of element (row r, k) in a 128-byte-swizzled K-major tile of
+  // 64 BF16 per row
+  __device__ __forceinline__ uint32_t sw128( int r, int k )
+  {
+    return (uint32_t)( r * 128 + ( ( ( k >> 3 ) ^ ( r & 7 ) ) << 4 ) + ( ( k & 7 ) << 1 ) );
+  }
+
+  // Shared-memory matrix descriptor of such a tile (start address in shared
+  // memory): start >> 4 in bits 0-13, leading-dimension offset 16 B (unused by
+  // the swizzled K-major layout) in bits 16-29, stride 1024 B between 8-row
+  // groups in bits 32-45, the fixed 0b001 of bits 46-48, swizzle mode 2
+  // (128 B) in bits 61-63.
+  __device__ __forceinline__ uint64_t sw128Desc( uint32_t start )
+  {
+    return (uint64_t)( ( start & 0x3FFFFu ) >> 4 ) | ( (uint64_t)1 << 16 ) | ( (uint64_t)( 1024 >> 4 ) << 32 )
+           | ( (uint64_t)1 << 46 ) | ( (uint64_t)2 << 61 );
+  }
+
+  // Instruction descriptor of kind::f16: FP32 accumulators (bits 4-5 = 1),
+  // BF16 A and B (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 in bits
+  // 17-22, M >> 4 in bits 24-28.
+  __host__ __device__ constexpr uint32_t tcIdesc( int m, int n )
+  {
+    return ( 1u << 4 ) | ( 1u << 7 ) | ( 1u << 10 ) | ( (uint32_t)( n >> 3 ) << 17 ) | ( (uint32_t)( m >> 4 ) << 24 );
+  }
+
+  __global__ void __launch_bounds__(128, 1) k_gemm_tc( const GemmArgs g, int* err )
+  {
+    extern __shared__ unsigned char tc_smem_raw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>(
+      ( reinterpret_cast<uintptr_t>( tc_smem_raw ) + 1023 ) & ~uintptr_t( 1023 ) );
+    unsigned char* sa = sm;                 // A tile: 128 rows x 128 B
+    unsigned char* sb = sm + 16384;         // B^T tile: up to 128 rows x 128 B
+    uint64_t* bar = reinterpret_cast<uint64_t*>( sm + 32768 );
+    uint32_t* tslot = reinterpret_cast<uint32_t*>( sm + 32768 + 8 );
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * TC_M;
+    const int kbeg = blockIdx.z * g.kchunk;
+    const int kend = min( g.K, kbeg + g.kchunk );
+    const int bn = ( g.N + 15 ) & ~15;      // MMA N: a multiple of 16, <= 128
+    const uint32_t idesc = tcIdesc( TC_M, bn );
+    if ( warp == 0 ) {
+      asm volatile( "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                    :: "r"( smemAddr( tslot ) ), "r"( TC_TMEM_COLS ) : "memory" );
+      asm volatile( "tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory" );
+    }
+    if ( tid == 0 )
+      asm volatile( "mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"( smemAddr( bar ) ) : "memory" );
+    asm volatile( "tcgen05.fence::before_thread_sync;" ::: "memory" );
+    __syncthreads();
+    asm volatile( "tcgen05.fence::after_thread_sync;" ::: "memory" );
+    const uint32_t tmem = *tslot;
+    const bf16 zero = __float2bfloat16( 0.f );
+    uint32_t parity = 0;
+    bool ok = true;
+    for ( int k0 = kbeg; k0 < kend && ok; k0 += TC_K ) {
+      // stage A(m, k) for m in [m0, m0+128), k in [k0, k0+64): the unit-stride
+      // dimension fastest across threads
+      for ( int i = tid; i < TC_M * TC_K; i += 128 ) {
+        int r, kk;
+        if ( g.sAk == 1 ) { r = i / TC_K; kk = i % TC_K; } else { kk = i / TC_M; r = i % TC_M; }
+        const int m = m0 + r, k = k0 + kk;
+        const bf16 v = ( m < g.M && k < kend ) ? g.A[(long)m * g.sAm + (long)k * g.sAk] : zero;
+        *reinterpret_cast<bf16*>( sa + sw128( r, kk ) ) = v;
+      }
+      // stage B^T: row n holds B(k, n) for k in [k0, k0+64)
+      for ( int i = tid; i < bn * TC_K; i += 128 ) {
+        int c, kk;
+        if ( g.sBk == 1 ) { c = i / TC_K; kk = i % TC_K; } else { kk = i / bn; c = i % bn; }
+        const int k = k0 + kk;
+        const bf16 v = ( c < g.N && k < kend ) ? g.B[(long)k * g.sBk + (long)c * g.sBn] : zero;
+        *reinterpret_cast<bf16*>( sb + sw128( c, kk ) ) = v;
+      }
+      // the tiles were written through the generic proxy; the MMA reads them
+      // through the async proxy
+      asm volatile( "fence.proxy.async.shared::cta;" ::: "memory" );
+      __syncthreads();
+      if ( tid == 0 ) {
+        asm volatile( "tcgen05.fence::after_thread_sync;" ::: "memory" );
+#pragma unroll
+        for ( int kk = 0; kk < TC_K / 16; ++kk ) {
+          const uint64_t ad = sw128Desc( smemAddr( sa ) + 32u * kk );
+          const uint64_t bd = sw128Desc( smemAddr( sb ) + 32u * kk );
+          const uint32_t acc = ( k0 > kbeg || kk > 0 ) ? 1u : 0u;
+          asm volatile( "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                        :: "r"( tmem ), "l"( ad ), "l"( bd ), "r"( idesc ), "r"( acc ) : "memory" );
+        }
+        asm volatile( "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                      :: "r"( smemAddr( bar ) ) : "memory" );
+      }
+      // every thread waits for the MMAs (the tiles are rewritten next);
+      // bounded: a wait that runs out flags the error and abandons the tile
+      uint32_t done = 0;
+      for ( long it = 0; it < TC_WAIT_LIMIT && !done; ++it )
+        asm volatile( "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                      " selp.u32 %0, 1, 0, p;\n}" : "=r"( done ) : "r"( smemAddr( bar ) ), "r"( parity ) : "memory" );
+      if ( !done ) {
+        ok = false;
+        if ( lane == 0 )
+          atomicExch( err, 1 );
+      }
+      parity ^= 1u;
+      asm volatile( "tcgen05.fence::after_thread_sync;" ::: "memory" );
+    }
+    ok = __syncthreads_and( ok );
+    if ( ok && kbeg < kend ) {
+      // epilogue: warp w holds accumulator rows 32w .. 32w+31 (TMEM lanes)
+      const int row = warp * 32 + lane;
+      const int m = m0 + row;
+      for ( int c0 = 0; c0 < bn; c0 += 32 ) {
+        uint32_t v[32];
+        const uint32_t taddr = tmem + ( (uint32_t)( warp * 32 ) << 16 ) + (uint32_t)c0;
+        asm volatile( "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                      : "=r"( v[0] ), "=r"( v[1] ), "=r"( v[2] ), "=r"( v[3] ), "=r"( v[4] ), "=r"( v[5] ),
+                        "=r"( v[6] ), "=r"( v[7] ), "=r"( v[8] ), "=r"( v[9] ), "=r"( v[10] ), "=r"( v[11] ),
+                        "=r"( v[12] ), "=r"( v[13] ), "=r"( v[14] ), "=r"( v[15] ), "=r"( v[16] ), "=r"( v[17] ),
+                        "=r"( v[18] ), "=r"( v[19] ), "=r"( v[20] ), "=r"( v[21] ), "=r"( v[22] ), "=r"( v[23] ),
+                        "=r"( v[24] ), "=r"( v[25] ), "=r"( v[26] ), "=r"( v[27] ), "=r"( v[28] ), "=r"( v[29] ),
+                        "=r"( v[30] ), "=r"( v[31] )
+                      : "r"( taddr ) : "memory" );
+        asm volatile( "tcgen05.wait::ld.sync.aligned;" ::: "memory" );
+        if ( m < g.M ) {
+#pragma unroll
+          for ( int j = 0; j < 32; ++j ) {
+            const int n = c0 + j;
+            if ( n >= g.N )
+              break;
+            float x = __uint_as_float( v[j] );
+            const long o = (long)m * g.ldc + n;
+            if ( g.mode == EPI_ATOMIC ) {
+              atomicAdd( g.Cf + o, x );
+              continue;
+            }
+            if ( g.mode == EPI_MASK ) {
+              if ( !( __bfloat162float( g.mask[(long)m * g.ldm + n] ) > 0.f ) )
+                x = 0.f;
+            } else if ( g.bias ) {
+              x += g.bias[n];
+            }
+            if ( g.Cf )
+              g.Cf[o] = x;
+            if ( g.Cb )
+              g.Cb[o] = __float2bfloat16( ( g.relu && x < 0.f ) ? 0.f : x );
+          }
+        }
+      }
+    }
+    asm volatile( "tcgen05.fence::before_thread_sync;" ::: "memory" );
+    __syncthreads();
+    if ( warp == 0 )
+      asm volatile( "tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"( tmem ), "r"( TC_TMEM_COLS ) : "memory" );
   }
 
   // ---- features of (log E, T) -------------------------------------------------
@@ -345,6 +527,9 @@ namespace ncgb_mlp {
     bf16* m_dout = nullptr;
     bf16* m_dh[2] = {};
     float* m_tgt = nullptr;
+    int* m_err = nullptr;   // set by a tcgen05 GEMM whose bounded wait ran out
+    void clearErr( cudaStream_t s );
+    void checkErr( cudaStream_t s );
   };
 
 
@@ -357,8 +542,33 @@ namespace ncgb_mlp {
 
     int cdiv( long a, long b ) { return int( ( a + b - 1 ) / b ); }
 
-    void gemm( const GemmArgs& g, cudaStream_t s )
+    // tcgen05 GEMMs unless NCGB_MLP_TC=0 (the mma.sync kernel)
+    bool useTc()
     {
+      static const bool on = [] {
+        const char* v = std::getenv( "NCGB_MLP_TC" );
+        return !( v && v[0] == '0' );
+      }();
+      return on;
+    }
+
+    void gemm( const GemmArgs& g, int* d_err, cudaStream_t s )
+    {
+      if ( useTc() ) {
+        if ( g.N > TC_TMEM_COLS )
+          throw std::runtime_error( "mlp GEMM: N above 128" );
+        static thread_local int configured = -1;
+        int dev = 0;
+        check( cudaGetDevice( &dev ), "cudaGetDevice" );
+        if ( configured != dev ) {
+          check( cudaFuncSetAttribute( k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM ),
+                 "cudaFuncSetAttribute" );
+          configured = dev;
+        }
+        dim3 grid( 1, cdiv( g.M, TC_M ), cdiv( g.K, g.kchunk ) );
+        k_gemm_tc<<<grid, 128, TC_SMEM, s>>>( g, d_err );
+        return;
+      }
       dim3 grid( cdiv( g.N, BN ), cdiv( g.M, BM ), cdiv( g.K, g.kchunk ) );
       k_gemm<<<grid, 128, 0, s>>>( g );
     }
@@ -424,6 +634,8 @@ namespace ncgb_mlp {
     check( cudaMalloc( &m_v, n * sizeof(float) ), "cudaMalloc (mlp)" );
     check( cudaMalloc( &m_g, n * sizeof(float) ), "cudaMalloc (mlp)" );
     check( cudaMalloc( &m_wb, n * sizeof(bf16) ), "cudaMalloc (mlp)" );
+    check( cudaMalloc( &m_err, sizeof(int) ), "cudaMalloc (mlp)" );
+    check( cudaMemset( m_err, 0, sizeof(int) ), "cudaMemset" );
     check( cudaMemset( m_m, 0, n * sizeof(float) ), "cudaMemset" );
     check( cudaMemset( m_v, 0, n * sizeof(float) ), "cudaMemset" );
     check( cudaMemset( m_g, 0, n * sizeof(float) ), "cudaMemset" );
@@ -434,7 +646,8 @@ namespace ncgb_mlp {
     int cur = -1;
     cudaGetDevice( &cur );
     cudaSetDevice( m_device );
-    for ( void* p : { (void*)m_w, (void*)m_m, (void*)m_v, (void*)m_g, (void*)m_wb, m_act, (void*)m_loss } )
+    for ( void* p : { (void*)m_w, (void*)m_m, (void*)m_v, (void*)m_g, (void*)m_wb, m_act, (void*)m_loss,
+                      (void*)m_err } )
       if ( p )
         cudaFree( p );
     cudaSetDevice( cur );
@@ -501,7 +714,7 @@ namespace ncgb_mlp {
       } else {
         g.Cf = m_out;
       }
-      gemm( g, s );
+      gemm( g, m_err, s );
     }
   }
 
@@ -520,7 +733,7 @@ namespace ncgb_mlp {
       gw.mode = EPI_ATOMIC;
       gw.Cf = m_g + m_L.w[l];
       gw.ldc = m_L.dout[l];
-      gemm( gw, s );
+      gemm( gw, m_err, s );
       // db_l += colsum(dz)
       const int rpb = 256;
       k_colsum<<<cdiv( batch, rpb ), 128, 0, s>>>( dz, batch, m_L.dout[l], rpb, m_g + m_L.b[l] );
@@ -535,9 +748,24 @@ namespace ncgb_mlp {
       gd.mode = EPI_MASK;
       gd.mask = m_h[l - 1]; gd.ldm = m_L.din[l];
       gd.Cb = dn; gd.ldc = m_L.din[l];
-      gemm( gd, s );
+      gemm( gd, m_err, s );
       dz = dn;
     }
+  }
+
+  void Net::clearErr( cudaStream_t s )
+  {
+    check( cudaMemsetAsync( m_err, 0, sizeof(int), s ), "memset" );
+  }
+
+  // Throws if a tcgen05 GEMM flagged a wait that ran out (results invalid).
+  void Net::checkErr( cudaStream_t s )
+  {
+    int e = 0;
+    check( cudaMemcpyAsync( &e, m_err, sizeof(int), cudaMemcpyDeviceToHost, s ), "D2H" );
+    check( cudaStreamSynchronize( s ), "mlp kernels" );
+    if ( e )
+      throw std::runtime_error( "mlp GEMM: a tensor-core completion wait ran out (results discarded)" );
   }
 
   float Net::readLoss( cudaStream_t s )
@@ -552,6 +780,7 @@ namespace ncgb_mlp {
                         cudaStream_t s )
   {
     ensureBatch( n );
+    clearErr( s );
     k_features<<<cdiv( cdiv( n, BM ) * BM, 128 ), 128, 0, s>>>( d_loge, d_temp, n, m_rg, m_x0 );
     check( cudaMemcpyAsync( m_tgt, d_target, n * sizeof(float), cudaMemcpyDeviceToDevice, s ), "D2D" );
     check( cudaMemsetAsync( m_g, 0, m_L.total * sizeof(float), s ), "memset" );
@@ -560,6 +789,7 @@ namespace ncgb_mlp {
     k_loss<<<cdiv( n, 128 ), 128, 0, s>>>( m_out, m_tgt, n, m_dout, m_loss );
     backward( n, s );
     check( cudaGetLastError(), "mlp kernels" );
+    checkErr( s );
     check( cudaMemcpyAsync( h_grad, m_g, m_L.total * sizeof(float), cudaMemcpyDeviceToHost, s ), "D2H" );
     return readLoss( s );
   }
@@ -572,6 +802,7 @@ namespace ncgb_mlp {
     if ( n == 0 )
       throw std::runtime_error( "mlp training set is empty" );
     ensureBatch( batch );
+    clearErr( s );
     check( cudaMemsetAsync( m_loss, 0, sizeof(float), s ), "memset" );
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     uint64_t traced = 0;
@@ -596,15 +827,18 @@ namespace ncgb_mlp {
     }
     check( cudaGetLastError(), "mlp training kernels" );
     check( cudaStreamSynchronize( s ), "mlp training" );
+    checkErr( s );
   }
 
   void Net::knots( const float* d_loge, const float* d_temp, int n, float* d_knots, cudaStream_t s )
   {
     ensureBatch( n );
+    clearErr( s );
     k_features<<<cdiv( cdiv( n, BM ) * BM, 128 ), 128, 0, s>>>( d_loge, d_temp, n, m_rg, m_x0 );
     forward( n, s );
     k_knots<<<cdiv( n, 128 ), 128, 0, s>>>( m_out, n, d_knots );
     check( cudaGetLastError(), "mlp inference" );
+    checkErr( s );
   }
 }
 
