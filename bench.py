@@ -506,7 +506,7 @@ def run_gb300(args):
                                   for c, i in infos.items()},
                    "final_loss": {str(c): i["loss_trace"][-1] if i["loss_trace"] else None
                                   for c, i in infos.items()},
-                   "network": "4x128 hidden, BF16 mma.sync + FP32 accumulation, trained by the library's kernels"}
+                   "network": "4x128 hidden, BF16 tcgen05 tensor-core GEMMs + FP32 accumulation in TMEM, trained by the library's kernels"}
 
         def attach(scatters):
             return [LR.attach(sc, nets) for sc, p in zip(scatters, is_pe) if p]

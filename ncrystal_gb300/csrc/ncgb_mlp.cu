@@ -7,10 +7,11 @@
 //   asinh(beta) at the levels tau_i = (i+1)/63 (quantile regression, pinball
 //   loss).
 //
-// GEMMs run on the tensor cores as mma.sync m16n8k16 with BF16 operands and
-// FP32 accumulation; master weights, Adam moments, the loss and the softplus
-// chain stay FP32.  Weights are stored [in][out] row-major, activations
-// [sample][feature] row-major, both BF16 copies for the GEMMs.
+// GEMMs run on the fifth-generation tensor cores (tcgen05.mma, BF16 operands
+// staged in shared memory, FP32 accumulators in tensor memory); master
+// weights, Adam moments, the loss and the softplus chain stay FP32.  Weights
+// are stored [in][out] row-major, activations [sample][feature] row-major,
+// both BF16 copies for the GEMMs.
 
 #include "ncgb_mlp.hh"
 #include "ncgb_philox.h"
@@ -30,9 +31,11 @@ namespace ncgb_mlp {
 
   using bf16 = __nv_bfloat16;
 
-  // ---- tiled BF16 GEMM, C[M x N] = sum_k A(m,k) B(k,n) -----------------------
+  // ---- BF16 GEMM arguments, C[M x N] = sum_k A(m,k) B(k,n) -------------------
   // A(m,k) = A[m*sAm + k*sAk], B(k,n) = B[k*sBk + n*sBn].  blockIdx.z splits K
-  // into chunks of 'kchunk' (results then added atomically).
+  // into chunks of 'kchunk' (results then added atomically).  Epilogues:
+  // store (+ bias, optional ReLU on the BF16 copy), mask (zero where the mask
+  // is not positive: the ReLU derivative), atomic add (split-K partial sums).
   enum EpiMode { EPI_STORE = 0, EPI_MASK = 1, EPI_ATOMIC = 2 };
 
   struct GemmArgs {
@@ -49,113 +52,13 @@ namespace ncgb_mlp {
     long ldm;
   };
 
-  constexpr int BM = 64, BN = 64, BK = 32, PADK = 40;
-
-  __device__ __forceinline__ uint32_t ld32( const bf16* p ) { return *reinterpret_cast<const uint32_t*>( p ); }
-
-  __global__ void __launch_bounds__(128) k_gemm( const GemmArgs g )
-  {
-    __shared__ __align__(16) bf16 As[BM][PADK];
-    __shared__ __align__(16) bf16 Bs[BN][PADK];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int gid = lane >> 2, tig = lane & 3;
-    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-    const int kbeg = blockIdx.z * g.kchunk;
-    const int kend = min( g.K, kbeg + g.kchunk );
-    const int wm = ( warp >> 1 ) * 32, wn = ( warp & 1 ) * 32;
-    float acc[2][4][4];
-#pragma unroll
-    for ( int i = 0; i < 2; ++i )
-#pragma unroll
-      for ( int j = 0; j < 4; ++j )
-#pragma unroll
-        for ( int r = 0; r < 4; ++r )
-          acc[i][j][r] = 0.f;
-    const bf16 zero = __float2bfloat16( 0.f );
-    for ( int k0 = kbeg; k0 < kend; k0 += BK ) {
-      // stage the A and B tiles, the unit-stride dimension fastest across threads
-      for ( int i = tid; i < BM * BK; i += 128 ) {
-        int r, kk;
-        if ( g.sAk == 1 ) { r = i / BK; kk = i % BK; } else { kk = i / BM; r = i % BM; }
-        const int m = m0 + r, k = k0 + kk;
-        As[r][kk] = ( m < g.M && k < kend ) ? g.A[(long)m * g.sAm + (long)k * g.sAk] : zero;
-      }
-      for ( int i = tid; i < BN * BK; i += 128 ) {
-        int c, kk;
-        if ( g.sBk == 1 ) { c = i / BK; kk = i % BK; } else { kk = i / BN; c = i % BN; }
-        const int n = n0 + c, k = k0 + kk;
-        Bs[c][kk] = ( n < g.N && k < kend ) ? g.B[(long)k * g.sBk + (long)n * g.sBn] : zero;
-      }
-      __syncthreads();
-#pragma unroll
-      for ( int ks = 0; ks < BK; ks += 16 ) {
-        uint32_t a[2][4], b[4][2];
-#pragma unroll
-        for ( int mi = 0; mi < 2; ++mi ) {
-          const int r = wm + mi * 16 + gid;
-          a[mi][0] = ld32( &As[r][ks + 2 * tig] );
-          a[mi][1] = ld32( &As[r + 8][ks + 2 * tig] );
-          a[mi][2] = ld32( &As[r][ks + 2 * tig + 8] );
-          a[mi][3] = ld32( &As[r + 8][ks + 2 * tig + 8] );
-        }
-#pragma unroll
-        for ( int ni = 0; ni < 4; ++ni ) {
-          const int c = wn + ni * 8 + gid;
-          b[ni][0] = ld32( &Bs[c][ks + 2 * tig] );
-          b[ni][1] = ld32( &Bs[c][ks + 2 * tig + 8] );
-        }
-#pragma unroll
-        for ( int mi = 0; mi < 2; ++mi )
-#pragma unroll
-          for ( int ni = 0; ni < 4; ++ni )
-            asm volatile( "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-                          "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-                          : "+f"( acc[mi][ni][0] ), "+f"( acc[mi][ni][1] ), "+f"( acc[mi][ni][2] ),
-                            "+f"( acc[mi][ni][3] )
-                          : "r"( a[mi][0] ), "r"( a[mi][1] ), "r"( a[mi][2] ), "r"( a[mi][3] ),
-                            "r"( b[ni][0] ), "r"( b[ni][1] ) );
-      }
-      __syncthreads();
-    }
-    // epilogue: acc[mi][ni][0,1] at row gid, cols 2*tig+{0,1}; [2,3] at row gid+8
-#pragma unroll
-    for ( int mi = 0; mi < 2; ++mi )
-#pragma unroll
-      for ( int ni = 0; ni < 4; ++ni )
-#pragma unroll
-        for ( int h = 0; h < 2; ++h ) {
-          const int m = m0 + wm + mi * 16 + gid + 8 * h;
-          if ( m >= g.M )
-            continue;
-#pragma unroll
-          for ( int e = 0; e < 2; ++e ) {
-            const int n = n0 + wn + ni * 8 + 2 * tig + e;
-            if ( n >= g.N )
-              continue;
-            float v = acc[mi][ni][2 * h + e];
-            const long o = (long)m * g.ldc + n;
-            if ( g.mode == EPI_ATOMIC ) {
-              atomicAdd( g.Cf + o, v );
-              continue;
-            }
-            if ( g.mode == EPI_MASK ) {
-              if ( !( __bfloat162float( g.mask[(long)m * g.ldm + n] ) > 0.f ) )
-                v = 0.f;
-            } else {
-              if ( g.bias )
-                v += g.bias[n];
-            }
-            if ( g.Cf )
-              g.Cf[o] = v;
-            if ( g.Cb )
-              g.Cb[o] = __float2bfloat16( ( g.relu && v < 0.f ) ? 0.f : v );
-          }
-        }
-  }
+  // activation rows are allocated in multiples of BM (the features kernel
+  // writes whole blocks of them)
+  constexpr int BM = 64;
 
   // ---- tcgen05 GEMM (sm_100 family tensor cores, accumulators in TMEM) -------
   // One CTA of 128 threads computes a 128-row tile of C = A B (all N <= 128
-  // columns, split-K over blockIdx.z as in k_gemm, same epilogues).  Per K
+  // columns, split-K over blockIdx.z).  Per K
   // stage of 64, the threads stage A (128 x 64) and B^T (N x 64) as BF16 into
   // shared memory in the K-major layout with the 128-byte swizzle (rows of
   // 128 B, the 16-byte chunks of row r XOR-ed with r mod 8, 8-row groups 1 KB
@@ -163,9 +66,10 @@ namespace ncgb_mlp {
   // 128 x N FP32 accumulator in tensor memory and commits them to an
   // mbarrier, which every thread waits on (bounded) before the tiles are
   // reused.  The epilogue reads each warp's 32 accumulator rows with
-  // tcgen05.ld.  Staging is element-wise, so any strides of A and B serve:
-  // the forward (A activations, B weights), the input-gradient and the
-  // weight-gradient (A and B transposed views) products alike.
+  // tcgen05.ld.  Staging takes any strides of A and B (16-byte vector loads
+  // along whichever dimension is contiguous), so the forward (A activations,
+  // B weights), the input-gradient and the weight-gradient (A and B
+  // transposed views) products all run on it.
   constexpr int TC_M = 128, TC_K = 64;
   constexpr int TC_TMEM_COLS = 128;
   // Dynamic shared memory per CTA: the two tiles (32 KB), the barrier and the
@@ -203,6 +107,73 @@ namespace ncgb_mlp {
     return ( 1u << 4 ) | ( 1u << 7 ) | ( 1u << 10 ) | ( (uint32_t)( n >> 3 ) << 17 ) | ( (uint32_t)( m >> 4 ) << 24 );
   }
 
+  // Stages X(row, k) = P[row * sR + k * sK] for rows [r0, r0 + rows) (zero
+  // at row >= R) and k in [k0, k0 + 64) (zero at k >= kend) into a 128-byte-
+  // swizzled K-major tile, with the 128 threads of the CTA.  Where the unit
+  // stride is along k, each 16-byte chunk of 8 k is one load and one swizzle
+  // unit; where it is along the rows, a 16-byte load of 8 rows is scattered
+  // into 8 tile rows.  Every thread issues all its loads (at most 8) before
+  // its stores, so that their latencies overlap.  Other strides or
+  // misaligned bases take the element-wise path.
+  __device__ __forceinline__ void stageTile( unsigned char* tile, const bf16* P, long sR, long sK, int r0, int R,
+                                             int rows, int k0, int kend, int tid )
+  {
+    const bool al = ( reinterpret_cast<uintptr_t>( P ) & 15 ) == 0 && ( kend % 8 ) == 0 && ( k0 % 8 ) == 0;
+    const bf16 zero = __float2bfloat16( 0.f );
+    const int nchunk = rows * ( TC_K / 8 );
+    if ( al && sK == 1 && ( sR % 8 ) == 0 ) {
+      uint4 v[8];
+#pragma unroll
+      for ( int j = 0; j < 8; ++j ) {
+        const int c = tid + 128 * j;
+        const int r = c >> 3, kc = c & 7;
+        const int row = r0 + r, k = k0 + 8 * kc;
+        v[j] = make_uint4( 0, 0, 0, 0 );
+        if ( c < nchunk && row < R && k < kend )
+          v[j] = __ldg( reinterpret_cast<const uint4*>( P + (long)row * sR + k ) );
+      }
+#pragma unroll
+      for ( int j = 0; j < 8; ++j ) {
+        const int c = tid + 128 * j;
+        if ( c < nchunk )
+          *reinterpret_cast<uint4*>( tile + sw128( c >> 3, 8 * ( c & 7 ) ) ) = v[j];
+      }
+      return;
+    }
+    if ( al && sR == 1 && ( sK % 8 ) == 0 && ( r0 % 8 ) == 0 && ( R % 8 ) == 0 ) {
+      const int rc = rows / 8;   // 8-row chunks per k
+      uint4 v[8];
+#pragma unroll
+      for ( int j = 0; j < 8; ++j ) {
+        const int c = tid + 128 * j;
+        const int kk = c / rc, r = 8 * ( c % rc );
+        const int row = r0 + r, k = k0 + kk;
+        v[j] = make_uint4( 0, 0, 0, 0 );
+        if ( c < nchunk && row < R && k < kend )
+          v[j] = __ldg( reinterpret_cast<const uint4*>( P + (long)k * sK + row ) );
+      }
+#pragma unroll
+      for ( int j = 0; j < 8; ++j ) {
+        const int c = tid + 128 * j;
+        if ( c < nchunk ) {
+          const int kk = c / rc, r = 8 * ( c % rc );
+          const bf16* e = reinterpret_cast<const bf16*>( &v[j] );
+#pragma unroll
+          for ( int q = 0; q < 8; ++q )
+            *reinterpret_cast<bf16*>( tile + sw128( r + q, kk ) ) = e[q];
+        }
+      }
+      return;
+    }
+    for ( int i = tid; i < rows * TC_K; i += 128 ) {
+      int r, kk;
+      if ( sK == 1 ) { r = i / TC_K; kk = i % TC_K; } else { kk = i / rows; r = i % rows; }
+      const int row = r0 + r, k = k0 + kk;
+      const bf16 x = ( row < R && k < kend ) ? P[(long)row * sR + (long)k * sK] : zero;
+      *reinterpret_cast<bf16*>( tile + sw128( r, kk ) ) = x;
+    }
+  }
+
   __global__ void __launch_bounds__(128, 1) k_gemm_tc( const GemmArgs g, int* err )
   {
     extern __shared__ unsigned char tc_smem_raw[];
@@ -223,8 +194,11 @@ namespace ncgb_mlp {
                     :: "r"( smemAddr( tslot ) ), "r"( TC_TMEM_COLS ) : "memory" );
       asm volatile( "tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory" );
     }
-    if ( tid == 0 )
+    if ( tid == 0 ) {
       asm volatile( "mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"( smemAddr( bar ) ) : "memory" );
+      // the barrier is arrived on by tcgen05.commit (async proxy)
+      asm volatile( "fence.mbarrier_init.release.cluster;" ::: "memory" );
+    }
     asm volatile( "tcgen05.fence::before_thread_sync;" ::: "memory" );
     __syncthreads();
     asm volatile( "tcgen05.fence::after_thread_sync;" ::: "memory" );
@@ -233,23 +207,10 @@ namespace ncgb_mlp {
     uint32_t parity = 0;
     bool ok = true;
     for ( int k0 = kbeg; k0 < kend && ok; k0 += TC_K ) {
-      // stage A(m, k) for m in [m0, m0+128), k in [k0, k0+64): the unit-stride
-      // dimension fastest across threads
-      for ( int i = tid; i < TC_M * TC_K; i += 128 ) {
-        int r, kk;
-        if ( g.sAk == 1 ) { r = i / TC_K; kk = i % TC_K; } else { kk = i / TC_M; r = i % TC_M; }
-        const int m = m0 + r, k = k0 + kk;
-        const bf16 v = ( m < g.M && k < kend ) ? g.A[(long)m * g.sAm + (long)k * g.sAk] : zero;
-        *reinterpret_cast<bf16*>( sa + sw128( r, kk ) ) = v;
-      }
-      // stage B^T: row n holds B(k, n) for k in [k0, k0+64)
-      for ( int i = tid; i < bn * TC_K; i += 128 ) {
-        int c, kk;
-        if ( g.sBk == 1 ) { c = i / TC_K; kk = i % TC_K; } else { kk = i / bn; c = i % bn; }
-        const int k = k0 + kk;
-        const bf16 v = ( c < g.N && k < kend ) ? g.B[(long)k * g.sBk + (long)c * g.sBn] : zero;
-        *reinterpret_cast<bf16*>( sb + sw128( c, kk ) ) = v;
-      }
+      // stage A(m, k) for m in [m0, m0+128) and B^T(n, k) = B(k, n) for
+      // n < bn, k in [k0, k0+64)
+      stageTile( sa, g.A, g.sAm, g.sAk, m0, g.M, TC_M, k0, kend, tid );
+      stageTile( sb, g.B, g.sBn, g.sBk, 0, g.N, bn, k0, kend, tid );
       // the tiles were written through the generic proxy; the MMA reads them
       // through the async proxy
       asm volatile( "fence.proxy.async.shared::cta;" ::: "memory" );
@@ -301,6 +262,35 @@ namespace ncgb_mlp {
                         "=r"( v[30] ), "=r"( v[31] )
                       : "r"( taddr ) : "memory" );
         asm volatile( "tcgen05.wait::ld.sync.aligned;" ::: "memory" );
+        // whole 32-column chunks of a plain store: 16-byte vector stores
+        if ( m < g.M && g.mode == EPI_STORE && c0 + 32 <= g.N && ( g.ldc % 8 ) == 0 ) {
+          float x[32];
+#pragma unroll
+          for ( int j = 0; j < 32; ++j )
+            x[j] = __uint_as_float( v[j] ) + ( g.bias ? g.bias[c0 + j] : 0.f );
+          const long o = (long)m * g.ldc + c0;
+          if ( g.Cf ) {
+#pragma unroll
+            for ( int q = 0; q < 8; ++q )
+              reinterpret_cast<float4*>( g.Cf + o )[q] = make_float4( x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3] );
+          }
+          if ( g.Cb ) {
+#pragma unroll
+            for ( int q = 0; q < 4; ++q ) {
+              uint4 pk;
+              uint32_t* w = reinterpret_cast<uint32_t*>( &pk );
+#pragma unroll
+              for ( int h = 0; h < 4; ++h ) {
+                float a = x[8 * q + 2 * h], b = x[8 * q + 2 * h + 1];
+                if ( g.relu ) { a = a < 0.f ? 0.f : a; b = b < 0.f ? 0.f : b; }
+                const __nv_bfloat162 t = __floats2bfloat162_rn( a, b );
+                w[h] = *reinterpret_cast<const uint32_t*>( &t );
+              }
+              reinterpret_cast<uint4*>( g.Cb + o )[q] = pk;
+            }
+          }
+          continue;
+        }
         if ( m < g.M ) {
 #pragma unroll
           for ( int j = 0; j < 32; ++j ) {
@@ -542,35 +532,20 @@ namespace ncgb_mlp {
 
     int cdiv( long a, long b ) { return int( ( a + b - 1 ) / b ); }
 
-    // tcgen05 GEMMs unless NCGB_MLP_TC=0 (the mma.sync kernel)
-    bool useTc()
-    {
-      static const bool on = [] {
-        const char* v = std::getenv( "NCGB_MLP_TC" );
-        return !( v && v[0] == '0' );
-      }();
-      return on;
-    }
-
     void gemm( const GemmArgs& g, int* d_err, cudaStream_t s )
     {
-      if ( useTc() ) {
-        if ( g.N > TC_TMEM_COLS )
-          throw std::runtime_error( "mlp GEMM: N above 128" );
-        static thread_local int configured = -1;
-        int dev = 0;
-        check( cudaGetDevice( &dev ), "cudaGetDevice" );
-        if ( configured != dev ) {
-          check( cudaFuncSetAttribute( k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM ),
-                 "cudaFuncSetAttribute" );
-          configured = dev;
-        }
-        dim3 grid( 1, cdiv( g.M, TC_M ), cdiv( g.K, g.kchunk ) );
-        k_gemm_tc<<<grid, 128, TC_SMEM, s>>>( g, d_err );
-        return;
+      if ( g.N > TC_TMEM_COLS )
+        throw std::runtime_error( "mlp GEMM: N above 128" );
+      static thread_local int configured = -1;
+      int dev = 0;
+      check( cudaGetDevice( &dev ), "cudaGetDevice" );
+      if ( configured != dev ) {
+        check( cudaFuncSetAttribute( k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM ),
+               "cudaFuncSetAttribute" );
+        configured = dev;
       }
-      dim3 grid( cdiv( g.N, BN ), cdiv( g.M, BM ), cdiv( g.K, g.kchunk ) );
-      k_gemm<<<grid, 128, 0, s>>>( g );
+      dim3 grid( 1, cdiv( g.M, TC_M ), cdiv( g.K, g.kchunk ) );
+      k_gemm_tc<<<grid, 128, TC_SMEM, s>>>( g, d_err );
     }
 
     GemmArgs base()
