@@ -38,6 +38,7 @@ Under torchrun (N>1) each rank runs an independent replica on its own GPU
 JSON line with the whole-job throughput.
 """
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -613,14 +614,16 @@ def run_gb300(args):
     for _ in range(max(2, args.warmup)):
         R.e2e_step()
     barrier()
-    e2e_steps = max(10, args.steps)
+    e2e_steps = max(30, args.steps)
     step_s = []
+    gc.disable()   # no interpreter collection pauses inside the timed host loop
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         t1 = time.perf_counter()
         R.e2e_step()   # synchronous: copies in, kernels, copies out
         step_s.append(time.perf_counter() - t1)
     barrier()
+    gc.enable()
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
     e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT, "steps": e2e_steps,
            "step_ms": {"min": 1e3 * min(step_s), "median": 1e3 * statistics.median(step_s),

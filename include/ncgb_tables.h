@@ -138,7 +138,7 @@ typedef struct {
   double ext_kT, ext_mass_amu;
   double sigma_bound;
   int32_t ne, na, nb;
-  int32_t pad0;
+  float internal_scale_f; /* FP32 copy of internal_scale (mixed-precision mode) */
   /* energy grid */
   const double* egrid;  /* [ne] */
   const double* xs;     /* [ne] */

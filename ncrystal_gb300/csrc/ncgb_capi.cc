@@ -523,6 +523,14 @@ namespace {
       throw TypedError( "BadInput", "n_ekin*repeat above 2^32 per call is not supported (neutron index of the random streams is 32 bits)" );
   }
 
+  bool hasBragg( const ncgb_material_view& v )
+  {
+    for ( int i = 0; i < v.ncomp && i < NCGB_MAX_COMP; ++i )
+      if ( v.comp[i].type == NCGB_COMP_BRAGG )
+        return true;
+    return false;
+  }
+
   ncgb::Batch makeBatch( ScatterObj& o, Scratch& s, uint32_t call )
   {
     ncgb::Batch b;
@@ -532,6 +540,7 @@ namespace {
     b.stream = o.streamidx;
     b.fast = ( o.mode == NCGB_MODE_MIXED );
     b.learned = ( o.sampler == NCGB_SAMPLER_LEARNED );
+    b.reorder = hasBragg( o.mat->view ) ? 1 : 0;
     b.work = s.d_work;
     b.queue = static_cast<ncgb::QEntry*>( s.d_queue );
     return b;
@@ -699,6 +708,7 @@ namespace {
       ensure( s.d_queue, s.cap_queue, n * sizeof(ncgb::QEntry) );
       resetNFail( s, s.stream );
       ncgb::Batch b = makeBatch( o, s, nextCall( o ) );
+      b.reorder = 0;
       b.ekin = mp[0];
       b.in_f32 = b.out_f32 = ( sizeof(T) == 4 );
       b.n_ekin = b.n_out = n;
@@ -1581,6 +1591,7 @@ namespace {
     std::vector<std::shared_ptr<DeviceMaterial>> mats;   // keeps the tables alive
     ncgb::MatSlot* d_slots = nullptr;
     int nmat = 0;
+    bool anyBragg = false;   // some material has a PowderBragg component
     ncgb::LaunchCfg cfg;
     bool tuned = false;
     int mode = defaultMode();
@@ -1619,6 +1630,7 @@ namespace {
     b.status = d_status;
     b.fast = ( bo.mode == NCGB_MODE_MIXED );
     b.learned = ( bo.sampler == NCGB_SAMPLER_LEARNED );
+    b.reorder = bo.anyBragg ? 1 : 0;
     b.work = s.d_work;
     ensure( s.d_queue, s.cap_queue, n * sizeof(ncgb::QEntry) );
     b.queue = static_cast<ncgb::QEntry*>( s.d_queue );
@@ -1644,6 +1656,8 @@ ncgb_batch_t ncgb_batch_create( const ncrystal_scatter_t* scatters, unsigned lon
       bo->mats.push_back( o.mat );
       std::memset( &slots[k], 0, sizeof(ncgb::MatSlot) );
       slots[k].view = o.mat->view;
+      if ( hasBragg( o.mat->view ) )
+        bo->anyBragg = true;
       slots[k].seed = o.seed;
       slots[k].stream = o.streamidx;
     }
@@ -1845,6 +1859,7 @@ void ncgb_batch_xs_scatter_many( ncgb_batch_t bt, const double* ekin, const int6
                                   static_cast<double*>( mp[2] ), static_cast<double*>( mp[3] ), nullptr );
       b.callseq = call;
       b.index_offset = 0;
+      b.reorder = 0;
       checkCuda( cudaStreamWaitEvent( s.stream, s.done, 0 ), "cudaStreamWaitEvent" );
       checkCuda( ncgb::launchScatterMulti( bo.d_slots, d_off, bo.nmat, b, bo.cfg, s.stream ), "batch kernels" );
       checkCuda( cudaEventRecord( s.done, s.stream ), "cudaEventRecord" );

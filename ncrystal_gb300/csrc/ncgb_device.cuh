@@ -105,6 +105,16 @@ namespace ncgb_dev {
     const long long b = bits( e );
     return b >= bits( lo ) && b <= bits( hi );
   }
+  // contains( lo, hi, e ) for lo >= +0.0 and hi not NaN, on the integer pipe
+  // for any e: negative energies and NaN fall outside as with the FP64
+  // compares, and -0.0 counts as 0.0.
+  __device__ __forceinline__ bool containsFromZero( double lo, double hi, double e )
+  {
+    long long b = bits( e );
+    if ( b == (long long)0x8000000000000000ULL )
+      b = 0;
+    return b >= bits( lo ) && b <= bits( hi );
+  }
   __device__ __forceinline__ bool finited( double x ) { return ( bits(x) & 0x7FF0000000000000LL ) != 0x7FF0000000000000LL; }
   __device__ __forceinline__ double infd() { return __longlong_as_double( 0x7FF0000000000000LL ); }
 
@@ -381,7 +391,7 @@ namespace ncgb_dev {
       const float2 p = __ldg( reinterpret_cast<const float2*>( s.xsf ) + ( iu - 1 ) );
       xs = fmaf( p.y, ef - __ldg( s.egrid_f + iu - 1 ), p.x );
     }
-    return xs * (float)s.internal_scale;
+    return xs * s.internal_scale_f;
   }
 
   __device__ __forceinline__ float compXSf( const ncgb_comp_view& c, double ekin, float ef )
@@ -1122,11 +1132,6 @@ namespace ncgb_dev {
       deltaE = beta * s.kT;
       muv = rand01( rng ) * 2.0 - 1.0;
     } else if ( Fast && !( fabs( beta ) < 0.01 * L.xtrue ) ) {
-      // Mixed mode away from the elastic line (|beta| >= 0.01 E/kT, outside
-      // getAlphaLimits' Taylor region): with a = sqrt(x), b = sqrt(x+beta),
-      // alpha- = (b-a)^2 and E + E' - alpha kT = kT (2ab - (alpha - alpha-)),
-      // so mu = 1 - (alpha - alpha-)/(2ab), in FP32 without cancellation; the
-      // energy transfer beta kT and 1 - d stay FP64.
       deltaE = beta * s.kT;
       const float a = sqrtf( (float)L.xtrue ), b = sqrtf( (float)( L.xtrue + beta ) );
       const float ab = a * b;

@@ -65,6 +65,9 @@ namespace ncgb {
     const uint32_t* rng_index;   // if set (with directions only): neutron o draws from stream
                                  // (seed, rng_index[o], callseq, stream) instead
     int untimed;       // never record phase-timing events for this batch
+    int reorder;       // the pick pass may visit each tile's neutrons in energy order
+                       // (materials with PowderBragg components; never where the
+                       // kernels read and write host memory directly)
     unsigned long long* phase_cycles;  // non-null (single material, no directions): run the
                                        // S(alpha,beta) pass with phase clocks, summing the
                                        // lanes' cycles per phase and their Alg.1 attempts here

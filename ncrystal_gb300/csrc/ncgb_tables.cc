@@ -448,6 +448,7 @@ namespace ncgb {
         s.kT = b.f64s(p+"kT");
         s.egrid_margin = b.f64s(p+"egrid_margin");
         s.internal_scale = b.f64s(p+"internal_scale");
+        s.internal_scale_f = (float)s.internal_scale;
         s.kext = d.kext;
         s.k1 = d.k1;
         s.k2 = d.k2;
