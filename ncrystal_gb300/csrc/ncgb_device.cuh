@@ -1128,18 +1128,43 @@ namespace ncgb_dev {
     // SABSampler::sampleDeltaEMu (NCSABSampler.cc:229-236), SABScatter
     // (NCSABScatter.cc:92-101), with the neutron's own energy
     double deltaE, muv;
+    if ( Fast ) {
+      // Mixed mode.  x + beta stays FP64 (it cancels towards E' = 0) and
+      // gives E' = kT (x + beta); the two branch tests run in FP32 (they
+      // choose between formulas that agree where they meet, and the
+      // isotropic branch sits within 1e-14 of E' = 0).  Away from the elastic
+      // line (|beta| >= 0.01 E/kT, outside getAlphaLimits' Taylor region),
+      // with a = sqrt(x), b = sqrt(x+beta): alpha- = (b-a)^2 and
+      // E + E' - alpha kT = kT (2ab - (alpha - alpha-)), so
+      // 1 - mu = d = (alpha - alpha-)/(2ab), in FP32 without cancellation;
+      // mu = 1 - d in FP64.  Near the elastic line: the FP64 conversion.
+      const double xb = L.xtrue + beta;
+      const float xf = (float)L.xtrue, xbf = (float)xb, bf = (float)beta;
+      if ( xbf <= xf * 1e-14f ) {                 // muIsotropicAtBeta, NCKinUtils.hh:64-70
+        muv = rand01( rng ) * 2.0 - 1.0;
+      } else if ( !( fabsf( bf ) < 0.01f * xf ) ) {
+        const float a = sqrtf( xf ), b = sqrtf( xbf );
+        const float ab = a * b;
+        if ( !( ab > 0.0f ) )
+          return NCGB_ST_CALCERROR;
+        const float sab = a + b;
+        const float d = ( (float)alpha - ( bf * bf ) / ( sab * sab ) ) / ( 2.0f * ab );
+        muv = 1.0 - (double)fminf( 2.0f, fmaxf( 0.0f, d ) );
+      } else {
+        const int st = alphaBetaToDeltaEMu( alpha, beta, L.ekin, s.kT, deltaE, muv );
+        if ( st != NCGB_ST_OK )
+          return st;
+        ef = maxd( 0.0, L.ekin + deltaE );
+        mu = muv;
+        return NCGB_ST_OK;
+      }
+      ef = bits( xb ) > 0 ? s.kT * xb : 0.0;     // max(0, E'), the sign tested on the integer pipe
+      mu = muv;
+      return NCGB_ST_OK;
+    }
     if ( beta <= L.xtrue * ( -1.0 + 1e-14 ) ) { // muIsotropicAtBeta, NCKinUtils.hh:64-70
       deltaE = beta * s.kT;
       muv = rand01( rng ) * 2.0 - 1.0;
-    } else if ( Fast && !( fabs( beta ) < 0.01 * L.xtrue ) ) {
-      deltaE = beta * s.kT;
-      const float a = sqrtf( (float)L.xtrue ), b = sqrtf( (float)( L.xtrue + beta ) );
-      const float ab = a * b;
-      if ( !( ab > 0.0f ) )
-        return NCGB_ST_CALCERROR;
-      const float bf = (float)beta, sab = a + b;
-      const float d = ( (float)alpha - ( bf * bf ) / ( sab * sab ) ) / ( 2.0f * ab );
-      muv = clampd( 1.0 - (double)d, -1.0, 1.0 );
     } else {
       const int st = alphaBetaToDeltaEMu( alpha, beta, L.ekin, s.kT, deltaE, muv );
       if ( st != NCGB_ST_OK )
