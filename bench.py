@@ -614,7 +614,7 @@ def run_gb300(args):
     for _ in range(max(2, args.warmup)):
         R.e2e_step()
     barrier()
-    e2e_steps = max(30, args.steps)
+    e2e_steps = max(60, args.steps)
     step_s = []
     gc.disable()   # no interpreter collection pauses inside the timed host loop
     t0 = time.perf_counter()
@@ -624,6 +624,7 @@ def run_gb300(args):
         step_s.append(time.perf_counter() - t1)
     barrier()
     gc.enable()
+    print("e2e call times (ms): " + " ".join("%.2f" % (1e3 * t) for t in step_s), file=sys.stderr)
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
     e2e = {"value": world * n * e2e_steps / e2e_s, "unit": UNIT, "steps": e2e_steps,
            "step_ms": {"min": 1e3 * min(step_s), "median": 1e3 * statistics.median(step_s),

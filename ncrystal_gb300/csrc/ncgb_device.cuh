@@ -105,16 +105,6 @@ namespace ncgb_dev {
     const long long b = bits( e );
     return b >= bits( lo ) && b <= bits( hi );
   }
-  // contains( lo, hi, e ) for lo >= +0.0 and hi not NaN, on the integer pipe
-  // for any e: negative energies and NaN fall outside as with the FP64
-  // compares, and -0.0 counts as 0.0.
-  __device__ __forceinline__ bool containsFromZero( double lo, double hi, double e )
-  {
-    long long b = bits( e );
-    if ( b == (long long)0x8000000000000000ULL )
-      b = 0;
-    return b >= bits( lo ) && b <= bits( hi );
-  }
   __device__ __forceinline__ bool finited( double x ) { return ( bits(x) & 0x7FF0000000000000LL ) != 0x7FF0000000000000LL; }
   __device__ __forceinline__ double infd() { return __longlong_as_double( 0x7FF0000000000000LL ); }
 

@@ -170,10 +170,7 @@ namespace {
       int qcomp = 0;
       if ( b.out_xs_abs )
         store( b.out_xs_abs, b.out_f32, o, absXS( m.abs_c, e ) );
-      // (material domains start at +0.0 or above: the integer-pipe test)
-      const bool inside = bits( m.dom_elow ) >= 0 ? containsFromZero( m.dom_elow, m.dom_ehigh, e )
-                                                  : contains( m.dom_elow, m.dom_ehigh, e );
-      if ( !inside ) {
+      if ( !contains( m.dom_elow, m.dom_ehigh, e ) ) {
         // ProcComposition outside its domain: xs 0, neutron unchanged (NCProcImpl.cc:353-389)
         store( b.out_xs, b.out_f32, o, 0.0 );
         writeScatter<Dir>( b, o, e, NCGB_ST_OK, e, 1.0, rng, false );
@@ -470,9 +467,7 @@ namespace {
     for ( uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < b.n_ekin; i += stride ) {
       const double e = loadE( b, i );
       double xs = 0.0;
-      const bool inside = bits( m.dom_elow ) >= 0 ? containsFromZero( m.dom_elow, m.dom_ehigh, e )
-                                                  : contains( m.dom_elow, m.dom_ehigh, e );
-      if ( inside ) {
+      if ( contains( m.dom_elow, m.dom_ehigh, e ) ) {
         ncgb_rng dummy;
         ncgb_rng_init( &dummy, 0, 0, 0, 0 );
         xs = xsAndPick<false, Fast>( m, e, dummy ).xs;
