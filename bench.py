@@ -655,7 +655,8 @@ def run_gb300(args):
                          "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
                          "traffic": profiled_traffic(dom, args.workload), "kernel": dom, "kernels": kernels,
                          "step_bytes_per_neutron": 4 * esz,
-                         "note": "FP64-pipe bound, not HBM bound: see profiles/"},
+                         "note": "latency-bound (table gathers and spill reloads, FP64 pipe about half busy), "
+                                 "not HBM-bound: see profiles/%s_%s.md" % (dom, args.workload)},
             "cpu_baseline": base,
             "e2e": e2e,
             "clocks": clk.summary(),

@@ -429,6 +429,7 @@ namespace {
     cudaStream_t stream3 = nullptr;   // device -> host copies of chunked calls
     cudaEvent_t done = nullptr;
     cudaEvent_t ev_in[2] = {}, ev_k[2] = {}, ev_out[2] = {};   // per buffer slot of chunked calls
+    cudaEvent_t ev_pick[2] = {};   // per slot: the pick pass done (cross-sections final)
     void* d_in = nullptr; std::size_t cap_in = 0;
     void* d_a = nullptr; std::size_t cap_a = 0;
     void* d_b = nullptr; std::size_t cap_b = 0;
@@ -475,6 +476,7 @@ namespace {
         checkCuda( cudaEventCreateWithFlags( &s.ev_in[h], cudaEventDisableTiming ), "cudaEventCreate" );
         checkCuda( cudaEventCreateWithFlags( &s.ev_k[h], cudaEventDisableTiming ), "cudaEventCreate" );
         checkCuda( cudaEventCreateWithFlags( &s.ev_out[h], cudaEventDisableTiming ), "cudaEventCreate" );
+        checkCuda( cudaEventCreateWithFlags( &s.ev_pick[h], cudaEventDisableTiming ), "cudaEventCreate" );
       }
       checkCuda( cudaEventRecord( s.done, s.stream ), "cudaEventRecord" );
       void* w = nullptr;
@@ -491,10 +493,15 @@ namespace {
   // copies out on stream3.  The copy-in of chunk k+2 waits only for the
   // kernels of chunk k (which read its slot), and the kernels of chunk k+2
   // for the copy-out of chunk k (which reads theirs), so that both copy
-  // directions and the kernels overlap.  copyIn / launch / copyOut get
-  // (offset, count, slot, stream).  Returns after the last copy-out.
-  template<class CopyIn, class Launch, class CopyOut>
-  void chunkPipeline( Scratch& s, uint64_t n, uint64_t chunk, CopyIn copyIn, Launch launch, CopyOut copyOut )
+  // directions and the kernels overlap.  The launch records ev_pick[slot]
+  // between its two passes; copyOutEarly (the cross-sections, final after
+  // the pick pass) waits only for that, so it overlaps the chunk's own
+  // S(alpha,beta) pass, and copyOut (E', mu) for the whole launch.
+  // copyIn / launch / copyOutEarly / copyOut get (offset, count, slot,
+  // stream).  Returns after the last copy-out.
+  template<class CopyIn, class Launch, class CopyOutEarly, class CopyOut>
+  void chunkPipeline( Scratch& s, uint64_t n, uint64_t chunk, CopyIn copyIn, Launch launch,
+                      CopyOutEarly copyOutEarly, CopyOut copyOut )
   {
     uint64_t k = 0;
     for ( uint64_t off = 0; off < n; off += chunk, ++k ) {
@@ -507,6 +514,8 @@ namespace {
       checkCuda( cudaStreamWaitEvent( s.stream, s.ev_out[h], 0 ), "cudaStreamWaitEvent" );
       launch( off, m, h, s.stream );
       checkCuda( cudaEventRecord( s.ev_k[h], s.stream ), "cudaEventRecord" );
+      checkCuda( cudaStreamWaitEvent( s.stream3, s.ev_pick[h], 0 ), "cudaStreamWaitEvent" );
+      copyOutEarly( off, m, h, s.stream3 );
       checkCuda( cudaStreamWaitEvent( s.stream3, s.ev_k[h], 0 ), "cudaStreamWaitEvent" );
       copyOut( off, m, h, s.stream3 );
       checkCuda( cudaEventRecord( s.ev_out[h], s.stream3 ), "cudaEventRecord" );
@@ -547,12 +556,13 @@ namespace {
   }
 
   // Scatter batch on stream 'st', ordered after the thread's previous batch.
-  void runBatch( const DeviceMaterial& dm, Scratch& s, ncgb::Batch& b, cudaStream_t st )
+  void runBatch( const DeviceMaterial& dm, Scratch& s, ncgb::Batch& b, cudaStream_t st,
+                 cudaEvent_t pickDone = nullptr )
   {
     ensure( s.d_queue, s.cap_queue, b.n_out * sizeof(ncgb::QEntry) );
     b.queue = static_cast<ncgb::QEntry*>( s.d_queue );
     checkCuda( cudaStreamWaitEvent( st, s.done, 0 ), "cudaStreamWaitEvent" );
-    checkCuda( ncgb::launchScatter( dm.view, b, st ), "scatter kernels" );
+    checkCuda( ncgb::launchScatter( dm.view, b, st, pickDone ), "scatter kernels" );
     checkCuda( cudaEventRecord( s.done, st ), "cudaEventRecord" );
   }
 
@@ -744,10 +754,12 @@ namespace {
         b.out_xs = xs ? slot( s.d_a, h ) : nullptr;
         b.out_a = ef ? slot( s.d_b, h ) : nullptr;
         b.out_b = mu ? slot( s.d_c, h ) : nullptr;
-        runBatch( dm, s, b, cs );
+        runBatch( dm, s, b, cs, s.ev_pick[h] );
       },
       [&]( uint64_t off, uint64_t m, int h, cudaStream_t cs ) {
         if ( xs ) checkCuda( cudaMemcpyAsync( xs + off, slot( s.d_a, h ), m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
+      },
+      [&]( uint64_t off, uint64_t m, int h, cudaStream_t cs ) {
         if ( ef ) checkCuda( cudaMemcpyAsync( ef + off, slot( s.d_b, h ), m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
         if ( mu ) checkCuda( cudaMemcpyAsync( mu + off, slot( s.d_c, h ), m * sizeof(T), cudaMemcpyDeviceToHost, cs ), "D2H" );
       } );
@@ -1892,11 +1904,14 @@ void ncgb_batch_xs_scatter_many( ncgb_batch_t bt, const double* ekin, const int6
         b.callseq = call;
         b.index_offset = static_cast<uint32_t>( off );
         checkCuda( cudaStreamWaitEvent( cs, s.done, 0 ), "cudaStreamWaitEvent" );
-        checkCuda( ncgb::launchScatterMulti( bo.d_slots, d_off, bo.nmat, b, bo.cfg, cs ), "batch kernels" );
+        checkCuda( ncgb::launchScatterMulti( bo.d_slots, d_off, bo.nmat, b, bo.cfg, cs, s.ev_pick[h] ),
+                   "batch kernels" );
         checkCuda( cudaEventRecord( s.done, cs ), "cudaEventRecord" );
       },
       [&]( uint64_t off, uint64_t m, int h, cudaStream_t cs ) {
         if ( xs ) checkCuda( cudaMemcpyAsync( xs + off, slot( s.d_a, h ), m * sizeof(double), cudaMemcpyDeviceToHost, cs ), "D2H" );
+      },
+      [&]( uint64_t off, uint64_t m, int h, cudaStream_t cs ) {
         if ( ef ) checkCuda( cudaMemcpyAsync( ef + off, slot( s.d_b, h ), m * sizeof(double), cudaMemcpyDeviceToHost, cs ), "D2H" );
         if ( mu ) checkCuda( cudaMemcpyAsync( mu + off, slot( s.d_c, h ), m * sizeof(double), cudaMemcpyDeviceToHost, cs ), "D2H" );
       } );

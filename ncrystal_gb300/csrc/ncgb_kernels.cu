@@ -578,7 +578,8 @@ namespace {
   }
 
   template<class Src>
-  cudaError_t launchBoth( const Src& src, const ncgb::Batch& b, const ncgb::LaunchCfg& cfg, cudaStream_t s )
+  cudaError_t launchBoth( const Src& src, const ncgb::Batch& b, const ncgb::LaunchCfg& cfg, cudaStream_t s,
+                          cudaEvent_t pickDone = nullptr )
   {
     if ( b.n_out == 0 )
       return cudaSuccess;
@@ -610,6 +611,11 @@ namespace {
     e = cudaGetLastError();
     if ( e != cudaSuccess )
       return e;
+    if ( pickDone ) {
+      e = cudaEventRecord( pickDone, s );
+      if ( e != cudaSuccess )
+        return e;
+    }
     if ( timing )
       cudaEventRecord( ev.b, s );
     const int maxb = sabBlocksPerSM<Src>();
@@ -634,7 +640,7 @@ namespace {
 
 namespace ncgb {
 
-  cudaError_t launchScatter( const ncgb_material_view& m, const Batch& b, cudaStream_t s )
+  cudaError_t launchScatter( const ncgb_material_view& m, const Batch& b, cudaStream_t s, cudaEvent_t pickDone )
   {
     if ( b.rng_index ) {
       MappedSrc src;
@@ -650,18 +656,18 @@ namespace ncgb {
     src.seed = b.seed;
     src.stream = b.stream;
     src.index_offset = b.index_offset;
-    return launchBoth( src, b, LaunchCfg(), s );
+    return launchBoth( src, b, LaunchCfg(), s, pickDone );
   }
 
   cudaError_t launchScatterMulti( const MatSlot* d_slots, const int64_t* d_offsets, int nmat,
-                                  const Batch& b, const LaunchCfg& cfg, cudaStream_t s )
+                                  const Batch& b, const LaunchCfg& cfg, cudaStream_t s, cudaEvent_t pickDone )
   {
     MultiSrc src;
     src.slots = d_slots;
     src.offsets = d_offsets;
     src.nmat = nmat;
     src.base = (int64_t)b.index_offset;
-    return launchBoth( src, b, cfg, s );
+    return launchBoth( src, b, cfg, s, pickDone );
   }
 
   int maxSabBlocksPerSM() { return sabBlocksPerSM<MultiSrc>(); }

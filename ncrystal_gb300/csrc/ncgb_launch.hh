@@ -76,11 +76,15 @@ namespace ncgb {
     QEntry* queue;     // scratch, n_out entries
   };
 
-  cudaError_t launchScatter( const ncgb_material_view& m, const Batch& b, cudaStream_t s );
+  // pickDone (optional) is recorded on s between the two passes: the
+  // cross-sections are final from then on.
+  cudaError_t launchScatter( const ncgb_material_view& m, const Batch& b, cudaStream_t s,
+                             cudaEvent_t pickDone = nullptr );
   // Ragged multi-material batch: neutrons [d_offsets[k], d_offsets[k+1]) use
   // material k, drawing from stream (seed_k, o - d_offsets[k], callseq, stream_k).
   cudaError_t launchScatterMulti( const MatSlot* d_slots, const int64_t* d_offsets, int nmat,
-                                  const Batch& b, const LaunchCfg& cfg, cudaStream_t s );
+                                  const Batch& b, const LaunchCfg& cfg, cudaStream_t s,
+                                  cudaEvent_t pickDone = nullptr );
   int maxSabBlocksPerSM();
   // (alpha, beta) of component 'comp' per neutron: out_a = alpha, out_b = beta;
   // neutron i uses stream (seed, index_offset + i, callseq, stream); failures
