@@ -1004,17 +1004,26 @@ namespace ncgb_dev {
 namespace ncgb_dev {
 
   // Per-neutron state of SABSampler::sampleAlphaBeta (NCSABSampler.cc:158-227)
-  // with its two nested rejection loops flattened: 'outer' counts Alg.1 calls
-  // (<=100), 'inner' the attempts of the current call (<=100).  'x' is E/kT of
-  // the energy the table is sampled at (Emax above the grid), 'xtrue' the
-  // neutron's own; 'preset' marks an (alpha, beta) already drawn from the
-  // free-gas extender.
+  // with its two nested rejection loops flattened, kept small because it stays
+  // live across every Alg.1 attempt (the S(alpha,beta) pass runs at 32
+  // registers per thread).  'x' is E/kT of the energy the table is sampled at
+  // (Emax above the grid), 'xsamp' the one the sampler runs at (the grid's
+  // first energy below it); the neutron's own E/kT is recomputed from 'ekin'.
+  // An (alpha, beta) already drawn by the free-gas extender ('preset') needs
+  // neither, so it shares their storage.  'state' packs the flags and the two
+  // loop counters: 'outer' counts Alg.1 calls (<=100), 'inner' the attempts
+  // of the current call (<=100).
   struct SABLane {
-    double ekin, x, xsamp, xtrue;
-    double pre_alpha, pre_beta;
-    int64_t ie;
-    int inner, outer;
-    bool ultra_small, preset;
+    static constexpr int ULTRA_SMALL = 1, PRESET = 2, INNER = 1 << 8, OUTER = 1 << 16;
+    double ekin;
+    union { double x; double pre_alpha; };
+    union { double xsamp; double pre_beta; };
+    int ie;
+    int state;
+    __device__ __forceinline__ bool ultraSmall() const { return state & ULTRA_SMALL; }
+    __device__ __forceinline__ bool preset() const { return state & PRESET; }
+    __device__ __forceinline__ int inner() const { return ( state >> 8 ) & 0xff; }
+    __device__ __forceinline__ int outer() const { return ( state >> 16 ) & 0xff; }
   };
 
   // Set-up of a SAB scatter at energy ekin (NCSABSampler.cc:163-197),
@@ -1025,36 +1034,37 @@ namespace ncgb_dev {
     const int64_t ne = s.ne;
     int64_t iu = egridUpper( s, ekin );
     L.ekin = ekin;
-    L.ultra_small = false;
-    L.preset = false;
-    L.inner = 0;
-    L.outer = 0;
-    L.ie = 0;
-    L.pre_alpha = L.pre_beta = 0.0;
-    L.xtrue = ekin * s.inv_kT;
+    L.state = 0;
     double etab = ekin;
     if ( iu == ne ) {
-      const int h = sabHighE( s, fgtab, ekin, rng, L.pre_alpha, L.pre_beta );
+      double pa = 0.0, pb = 0.0;
+      const int h = sabHighE( s, fgtab, ekin, rng, pa, pb );
       if ( h == -1 )
         return NCGB_ST_CALCERROR;
       if ( h < 0 )
         return NCGB_ST_LOOPCAP;
-      L.preset = ( h == 1 );
+      L.ie = (int)( ne - 1 );
+      if ( h == 1 ) {
+        L.state = SABLane::PRESET;
+        L.pre_alpha = pa;
+        L.pre_beta = pb;
+        return NCGB_ST_OK;
+      }
       etab = ldg( s.egrid + ne - 1 );
-      L.ie = ne - 1;
     } else if ( iu == 0 ) {
       L.ie = 0;
-      L.ultra_small = ( ekin < ldg( s.egrid ) );
+      if ( ekin < ldg( s.egrid ) )
+        L.state = SABLane::ULTRA_SMALL;
     } else {
       if ( s.egrid_margin > 1.0 ) {
         const long long em = bits( ekin * s.egrid_margin );   // non-negative: integer compares
         while ( iu + 1 != ne && em > ldgbits( s.egrid + iu ) )
           ++iu;
       }
-      L.ie = iu;
+      L.ie = (int)iu;
     }
     L.x = etab * s.inv_kT;
-    L.xsamp = L.ultra_small ? ldg( s.egrid ) * s.inv_kT : L.x;
+    L.xsamp = L.ultraSmall() ? ldg( s.egrid ) * s.inv_kT : L.x;
     return NCGB_ST_OK;
   }
 
@@ -1066,7 +1076,7 @@ namespace ncgb_dev {
   {
     alpha = 0.0;
     beta = 0.0;
-    if ( L.preset ) {
+    if ( L.preset() ) {
       alpha = L.pre_alpha;
       beta = L.pre_beta;
     } else {
@@ -1075,8 +1085,9 @@ namespace ncgb_dev {
         if ( a < 0 )
           return NCGB_ST_LOOPCAP;
         if ( a == 0 ) {
-          if ( ++L.inner >= 100 )
+          if ( L.inner() + 1 >= 100 )
             return NCGB_ST_LOOPCAP;
+          L.state += SABLane::INNER;
           return -1;
         }
       } // else SABSamplerAtE_NoScatter: (alpha, beta) = (0, 0), no draws
@@ -1084,21 +1095,22 @@ namespace ncgb_dev {
       // (alpha, beta) only if beta >= -xsamp and alpha is inside the limits
       // at xsamp; unless the energy is below the grid, xsamp == x and these
       // tests repeat that computation, so their outcome is known.
-      L.inner = 0;
+      L.state &= ~( 0xff * SABLane::INNER );
       const double x = L.x;
-      bool accept = !L.ultra_small && __ldg( s.smp_kind + L.ie ) != 0;
+      bool accept = !L.ultraSmall() && __ldg( s.smp_kind + L.ie ) != 0;
       if ( !accept && !( beta < -x ) ) {
         const ALim al = alphaLimits( x, beta );
         if ( inInterval( al.lo, al.hi, alpha ) ) {
           accept = true;
-        } else if ( L.ultra_small ) {
+        } else if ( L.ultraSmall() ) {
           alpha = al.lo + rand01( rng ) * ( al.hi - al.lo );
           accept = true;
         }
       }
       if ( !accept ) {
-        if ( ++L.outer >= 100 )
+        if ( L.outer() + 1 >= 100 )
           return NCGB_ST_LOOPCAP;
+        L.state += SABLane::OUTER;
         return -1;
       }
     }
@@ -1128,8 +1140,9 @@ namespace ncgb_dev {
       // E + E' - alpha kT = kT (2ab - (alpha - alpha-)), so
       // 1 - mu = d = (alpha - alpha-)/(2ab), in FP32 without cancellation;
       // mu = 1 - d in FP64.  Near the elastic line: the FP64 conversion.
-      const double xb = L.xtrue + beta;
-      const float xf = (float)L.xtrue, xbf = (float)xb, bf = (float)beta;
+      const double xtrue = __dmul_rn( L.ekin, s.inv_kT );   // not fused into the sum below
+      const double xb = xtrue + beta;
+      const float xf = (float)xtrue, xbf = (float)xb, bf = (float)beta;
       if ( xbf <= xf * 1e-14f ) {                 // muIsotropicAtBeta, NCKinUtils.hh:64-70
         muv = rand01( rng ) * 2.0 - 1.0;
       } else if ( !( fabsf( bf ) < 0.01f * xf ) ) {
@@ -1152,7 +1165,7 @@ namespace ncgb_dev {
       mu = muv;
       return NCGB_ST_OK;
     }
-    if ( beta <= L.xtrue * ( -1.0 + 1e-14 ) ) { // muIsotropicAtBeta, NCKinUtils.hh:64-70
+    if ( beta <= __dmul_rn( L.ekin, s.inv_kT ) * ( -1.0 + 1e-14 ) ) { // muIsotropicAtBeta, NCKinUtils.hh:64-70
       deltaE = beta * s.kT;
       muv = rand01( rng ) * 2.0 - 1.0;
     } else {
