@@ -197,7 +197,9 @@ int ncgb_scatter_device_noalloc( ncrystal_scatter_t, const double* d_ekin, unsig
  * setting up its sampler, the beta draw, the alpha draw from two rows, the
  * acceptance tests, the conversion to (E', mu) and its write, and lanes idle
  * at the end of the pass -- and cycles[NCGB_SAB_NPHASES] the number of Alg.1
- * attempts.  The clock reads themselves cost registers, so the profiled pass
+ * attempts.  Neutrons on the rare list (free-gas components, energies above
+ * a component's energy grid) are sampled after the clocked loop, unclocked.
+ * The clock reads themselves cost registers, so the profiled pass
  * is slower than the product one; its shares are what it is for.  Returns 0,
  * or non-zero after setting the error state. */
 #define NCGB_SAB_NPHASES 6

@@ -1500,7 +1500,7 @@ int ncgb_phase_times( double* ms_pick, double* ms_sab, unsigned long* nbatches, 
     if ( s.d_work ) {
       ncgb::Work w;
       checkCuda( cudaMemcpy( &w, s.d_work, sizeof(w), cudaMemcpyDeviceToHost ), "D2H" );
-      *last_nsab = w.qcount;
+      *last_nsab = (unsigned long)w.qcount + w.rcount;   // both lists of the S(alpha,beta) queue
     }
     return 0;
   } NCGB_CATCH;

@@ -96,6 +96,32 @@ namespace ncgb_dev {
     return lo;
   }
 
+  // 32-bit copies for the S(alpha,beta) tables (indexed below 2^31, checked
+  // by the table loader): fewer registers in the sampling pass.
+  __device__ __forceinline__ int upper_bound_nn32( const double* a, int n, double x )
+  {
+    const long long xb = bits(x);
+    int lo = 0, len = n;
+    while ( len > 0 ) {
+      const int half = len >> 1;
+      if ( !( xb < ldgbits( a + lo + half ) ) ) { lo += half + 1; len -= half + 1; }
+      else len = half;
+    }
+    return lo;
+  }
+
+  __device__ __forceinline__ int lower_bound_nn32( const double* a, int n, double x )
+  {
+    const long long xb = bits(x);
+    int lo = 0, len = n;
+    while ( len > 0 ) {
+      const int half = len >> 1;
+      if ( ldgbits( a + lo + half ) < xb ) { lo += half + 1; len -= half + 1; }
+      else len = half;
+    }
+    return lo;
+  }
+
   __device__ __forceinline__ double clampd( double x, double lo, double hi ) { return x < lo ? lo : ( x > hi ? hi : x ); }
   __device__ __forceinline__ double maxd( double a, double b ) { return a < b ? b : a; }
   __device__ __forceinline__ bool contains( double lo, double hi, double e ) { return e >= lo && e <= hi; }
@@ -649,10 +675,10 @@ namespace ncgb_dev {
   // in-bin constants read from the sampler's ncgb_beta_bin table instead of
   // divided out (same formulas, a few ulps apart).
   __device__ __forceinline__ double percentile( const double* x, const double* cdf, const ncgb_beta_bin* bins,
-                                                int64_t n, double p, int64_t& bin )
+                                                int n, double p, int& bin )
   {
     if ( p == 1.0 ) { bin = n - 2; return ldg( x + n - 1 ); }
-    int64_t i = lower_bound_nn( cdf, n, p );
+    int i = lower_bound_nn32( cdf, n, p );
     if ( i > n - 1 ) i = n - 1;
     if ( i < 1 ) i = 1;
     const ncgb_beta_bin* bb = bins + ( i - 1 );
@@ -711,11 +737,11 @@ namespace ncgb_dev {
   // inversion uses the cell's tabulated ratio and slope.
   template<bool Fast>
   __device__ __forceinline__ double sampleAlpha( const ncgb_sab_view& s, const ncgb_alpha_info* infos,
-                                                 int64_t ioff, int64_t ibeta, double rp )
+                                                 int ioff, int ibeta, double rp )
   {
     const ncgb_alpha_info* info = infos + ( ibeta - ioff );
     const double prob_front = ldg( &info->prob_front );
-    const int64_t na = s.na;
+    const int na = s.na;
     const double* cumul = s.cumul + ibeta * na;
     const double* sab = s.sab + ibeta * na;
     const double* logsab = s.logsab + ibeta * na;
@@ -737,15 +763,15 @@ namespace ncgb_dev {
     const double prob_notback = ldg( &info->prob_notback );
     if ( rp <= prob_notback ) {
       const double p2 = clampd( ( rp - prob_front ) * ldg( &info->inv_middle ), 0.0, 1.0 );
-      const int64_t il = __ldg( &info->front_idx ), iu = __ldg( &info->back_idx );
+      const int il = __ldg( &info->front_idx ), iu = __ldg( &info->back_idx );
       const double cl = ldg( cumul + il ), cu = ldg( cumul + iu );
       const double sel = cl + p2 * ( cu - cl );
-      const int64_t e = il + upper_bound_nn( cumul + il, iu + 1 - il, sel );
+      const int e = il + upper_bound_nn32( cumul + il, iu + 1 - il, sel );
       if ( e > iu )
         return ldg( s.alpha + iu );
       if ( e <= il )
         return ldg( s.alpha + il );
-      const int64_t a0 = e - 1;
+      const int a0 = e - 1;
       const ncgb_alpha_cell* cell = s.acell + ibeta * na + a0;
       const double rr = clampRand( ( sel - ldg( cumul + a0 ) ) * ldg( &cell->inv_bin ) );
       const double slope = ldg( &cell->slope );
@@ -782,11 +808,11 @@ namespace ncgb_dev {
   __device__ __forceinline__ float clampRandF( float r ) { return fminf( 1.0f, fmaxf( 1.17549435e-38f, r ) ); }
 
   __device__ __forceinline__ float sampleAlphaF( const ncgb_sab_view& s, const ncgb_alpha_info_f* infos,
-                                                 int64_t ioff, int64_t ibeta, float rp )
+                                                 int ioff, int ibeta, float rp )
   {
     const ncgb_alpha_info_f* info = infos + ( ibeta - ioff );
     const float prob_front = __ldg( &info->prob_front );
-    const int64_t na = s.na;
+    const int na = s.na;
     const float* cumul = s.cumul_f + ibeta * na;
     const float* sab = s.sab_f + ibeta * na;
     const float* logsab = s.logsab_f + ibeta * na;
@@ -829,7 +855,7 @@ namespace ncgb_dev {
 
   // alpha of row 'ibeta' at percentile rp, in the arithmetic of the mode
   template<bool Fast>
-  __device__ __forceinline__ double rowAlpha( const ncgb_sab_view& s, int64_t off, int64_t ioff, int64_t ibeta,
+  __device__ __forceinline__ double rowAlpha( const ncgb_sab_view& s, int off, int ioff, int ibeta,
                                              double rp )
   {
     if ( Fast )
@@ -841,9 +867,9 @@ namespace ncgb_dev {
   // beta uniform in the bin, alpha from the first row, up to 30 tries.
   // Returns 1 if (alpha, beta) is accepted, 0 if the attempt is rejected.
   template<bool Fast>
-  __device__ __noinline__ int alg1FirstBin( const ncgb_sab_view& s, int64_t off, int64_t ioff,
-                                            double fbkep, double b1, double x, ncgb_rng& rng,
-                                            double& alpha_out, double& beta_out )
+  __device__ __forceinline__ int alg1FirstBin( const ncgb_sab_view& s, int off, int ioff,
+                                               double fbkep, double b1, double x, ncgb_rng& rng,
+                                               double& alpha_out, double& beta_out )
   {
     const double b0 = fbkep;
     if ( b1 < -x )
@@ -875,6 +901,18 @@ namespace ncgb_dev {
     return 0;
   }
 
+  // The same, out of line: for passes that keep the free-gas paths' calls
+  // anyway (a call more costs them nothing; inlined, it costs the lean
+  // pass's registers nothing either: measured k_sab 1.25 -> 1.20 ms on
+  // polyethylene once no other call was left in its loop).
+  template<bool Fast>
+  __device__ __noinline__ int alg1FirstBinCall( const ncgb_sab_view& s, int off, int ioff,
+                                                double fbkep, double b1, double x, ncgb_rng& rng,
+                                                double& alpha_out, double& beta_out )
+  {
+    return alg1FirstBin<Fast>( s, off, ioff, fbkep, b1, x, rng, alpha_out, beta_out );
+  }
+
   // One attempt of SABSamplerAtE_Alg1::sampleAlphaBeta's loop
   // (NCSABSamplerModels.cc:59-148) at energy-grid point ie, sampling energy
   // x = E/kT.  Returns 1 with (alpha, beta) on acceptance, 0 on rejection.
@@ -886,8 +924,8 @@ namespace ncgb_dev {
   // that entered together have reconverged (so that the FP64 work after this
   // call is not split across lanes accepting at different tries).  Returns 1
   // with (beta, ibs), or 0 if 1000 proposals were all rejected.
-  __device__ __forceinline__ int lpBeta( const ncgb_sab_view& s, int64_t ie, ncgb_rng& rng, double& beta,
-                                         int64_t& ibs )
+  __device__ __forceinline__ int lpBeta( const ncgb_sab_view& s, int ie, ncgb_rng& rng, double& beta,
+                                         int& ibs )
   {
     const unsigned lanes = __activemask();
     const ncgb_lp_slot* slots = s.lp_slot + ie * NCGB_LP_K;
@@ -929,24 +967,25 @@ namespace ncgb_dev {
   // (alpha, beta) accepted, 0 if the attempt is rejected, -1 if the learned
   // proposal hit its cap.  Learned: the beta percentile inversion of samplers
   // with an enabled learned proposal is replaced by lpBeta (same distribution).
-  template<bool Fast, bool Learned, class Ph>
-  __device__ __forceinline__ int alg1Attempt( const ncgb_sab_view& s, int64_t ie, double x, ncgb_rng& rng,
+  template<bool Fast, bool Learned, bool Full, class Ph>
+  __device__ __forceinline__ int alg1Attempt( const ncgb_sab_view& s, int ie, double x, ncgb_rng& rng,
                                               double& alpha_out, double& beta_out, Ph& ph )
   {
     ph.attempt();
-    const int64_t off = __ldg( s.smp_offset + ie );
-    const int64_t nbs = __ldg( s.smp_nbeta + ie );
+    const int off = (int)__ldg( s.smp_offset + ie );
+    const int nbs = __ldg( s.smp_nbeta + ie );
     const double* bx = s.bx + off;
     const ncgb_alpha_info* infos = s.info + off;
-    const int64_t ioff = __ldg( s.smp_ibetaoffset + ie );
-    int64_t ibs;
+    const int ioff = __ldg( s.smp_ibetaoffset + ie );
+    int ibs;
     double beta;
     const double fbkep = ldg( s.smp_fbkep + ie );
     if ( Learned && s.lp_hdr && __ldg( &s.lp_hdr[ie].enabled ) ) {
       // the special first bin keeps its probability bcdf[1]; the regular
       // range is drawn from the learned proposal
       if ( rand_u32( rng ) < __ldg( &s.lp_hdr[ie].c1_thr ) ) {
-        const int r = alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+        const int r = Full ? alg1FirstBinCall<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out )
+                           : alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
         ph.template end<PH_BETA>();
         return r;
       }
@@ -955,7 +994,8 @@ namespace ncgb_dev {
     } else {
       beta = percentile( bx, s.bcdf + off, s.bbin + off, nbs, rand01( rng ), ibs );
       if ( ibs == 0 && fbkep <= 0.0 ) {
-        const int r = alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+        const int r = Full ? alg1FirstBinCall<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out )
+                           : alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
         ph.template end<PH_BETA>();
         return r;
       }
@@ -964,7 +1004,7 @@ namespace ncgb_dev {
     if ( beta <= maxd( -x, ldg( s.beta ) ) )
       return 0;
     const double rp = rand01( rng );
-    const int64_t ibeta = ioff + ibs;
+    const int ibeta = ioff + ibs;
     if ( ibeta < 1 )
       return 0; // cannot happen (beta above the beta grid front); keeps indices in bounds
     const double bl = ldg( s.beta + ibeta - 1 );
@@ -1028,6 +1068,9 @@ namespace ncgb_dev {
 
   // Set-up of a SAB scatter at energy ekin (NCSABSampler.cc:163-197),
   // including the high-E extrapolation (NCSABSampler.cc:170-178).
+  // Full = false: a caller that never passes an energy above the grid (a
+  // lean S(alpha,beta) pass), without the extender's out-of-line call.
+  template<bool Full = true>
   __device__ __forceinline__ int sabBegin( const ncgb_sab_view& s, const double* fgtab, double ekin,
                                            ncgb_rng& rng, SABLane& L )
   {
@@ -1037,6 +1080,9 @@ namespace ncgb_dev {
     L.state = 0;
     double etab = ekin;
     if ( iu == ne ) {
+      if constexpr ( !Full ) {
+        return NCGB_ST_CALCERROR;
+      }
       double pa = 0.0, pb = 0.0;
       const int h = sabHighE( s, fgtab, ekin, rng, pa, pb );
       if ( h == -1 )
@@ -1070,7 +1116,7 @@ namespace ncgb_dev {
 
   // One step of the flattened loops.  Returns -1 to continue, NCGB_ST_OK when
   // (alpha, beta) are final, or an error status.
-  template<bool Fast, bool Learned, class Ph = NoPhases>
+  template<bool Fast, bool Learned, bool Full = true, class Ph = NoPhases>
   __device__ __forceinline__ int sabStepAB( const ncgb_sab_view& s, SABLane& L, ncgb_rng& rng, double& alpha,
                                             double& beta, Ph&& ph = Ph() )
   {
@@ -1081,7 +1127,7 @@ namespace ncgb_dev {
       beta = L.pre_beta;
     } else {
       if ( __ldg( s.smp_kind + L.ie ) != 0 ) {
-        const int a = alg1Attempt<Fast, Learned>( s, L.ie, L.xsamp, rng, alpha, beta, ph );
+        const int a = alg1Attempt<Fast, Learned, Full>( s, L.ie, L.xsamp, rng, alpha, beta, ph );
         if ( a < 0 )
           return NCGB_ST_LOOPCAP;
         if ( a == 0 ) {
@@ -1119,12 +1165,12 @@ namespace ncgb_dev {
   }
 
   // sabStepAB, then (alpha, beta) -> (E', mu).
-  template<bool Fast, bool Learned, class Ph = NoPhases>
+  template<bool Fast, bool Learned, bool Full = true, class Ph = NoPhases>
   __device__ __forceinline__ int sabStep( const ncgb_sab_view& s, SABLane& L, ncgb_rng& rng, double& ef, double& mu,
                                           Ph&& ph = Ph() )
   {
     double alpha, beta;
-    const int st = sabStepAB<Fast, Learned>( s, L, rng, alpha, beta, ph );
+    const int st = sabStepAB<Fast, Learned, Full>( s, L, rng, alpha, beta, ph );
     if ( st != NCGB_ST_OK )
       return st;
     // SABSampler::sampleDeltaEMu (NCSABSampler.cc:229-236), SABScatter

@@ -10,10 +10,17 @@ namespace ncgb {
 
   // Device-side counters.  launchScatter zeroes the queue counters at the
   // start of every batch; the caller zeroes nfail when it wants a new count.
+  // The S(alpha,beta) queue holds two lists in one buffer of n_out entries:
+  // the main list from the front (entries 0 .. qcount-1), and from the back
+  // (entries n_out-1, n_out-2, ...) the rare list: neutrons of free-gas
+  // components and neutrons above a component's energy grid, which the
+  // free-gas sampler and extender serve.  A neutron is in at most one list.
   struct Work {
     unsigned long long nfail;  // neutrons with a non-OK status
-    unsigned int qcount;       // SAB queue length
-    unsigned int qnext;        // next queue entry to claim
+    unsigned int qcount;       // main list length
+    unsigned int qnext;        // next main entry to claim
+    unsigned int rcount;       // rare list length
+    unsigned int rnext;        // next rare entry to claim
   };
 
   // A neutron queued for S(alpha,beta) sampling: 16 bytes.

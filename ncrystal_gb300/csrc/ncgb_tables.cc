@@ -457,6 +457,10 @@ namespace ncgb {
         s.ext_kT = in.kT;
         s.ext_mass_amu = b.f64s(p+"ext_mass_amu");
         s.sigma_bound = in.sigma_bound;
+        // the sampling kernels index these tables with 32-bit integers
+        if ( in.alpha.size() * in.beta.size() >= ( std::size_t( 1 ) << 31 )
+             || d.bx.size() >= ( std::size_t( 1 ) << 31 ) )
+          throw Error( "S(alpha,beta) table too large for the GPU sampler (2^31 entries)" );
         s.ne = static_cast<int32_t>( in.egrid.size() );
         s.na = static_cast<int32_t>( in.alpha.size() );
         s.nb = static_cast<int32_t>( in.beta.size() );
