@@ -463,7 +463,8 @@ class BatchRunner:
                 "api": "ncgb_batch_xs_scatter_many (C ABI, pinned host arrays; %s)"
                        % ("kernels read and write host memory over NVLink-C2C" if zc
                           else "chunked copies: copy-in, kernel and copy-out streams"),
-                "autotuned_shape": {"pick_block": self.shape[0], "sab_blocks_per_sm": self.shape[1]}}
+                "autotuned_shape": {"pick_block": self.shape[0], "sab_blocks_per_sm": self.shape[1],
+                                    "split_lists": self.batch.split_lists()}}
 
     def launches_per_step(self):
         return 2

@@ -278,10 +278,18 @@ int ncgb_batch_scatter_device( ncgb_batch_t, const double* d_ekin, const int64_t
                                double* d_xs, double* d_ekin_final, double* d_mu, int32_t* d_status,
                                void* stream );
 /* Times the launch shapes (pick block 128/256/512 x S(alpha,beta) blocks per
- * SM) on this batch's arrays and keeps the fastest for the batch. */
+ * SM x one or two lists in the S(alpha,beta) queue) on this batch's arrays and
+ * keeps the fastest for the batch.  Two lists: free-gas neutrons and energies
+ * above a component's energy grid on a list of their own, so that the other
+ * neutrons' sampler has no call in its loop.  Results do not depend on the
+ * shape. */
 int ncgb_batch_autotune( ncgb_batch_t, const double* d_ekin, const int64_t* d_offsets, unsigned long n,
                          double* d_xs, double* d_ekin_final, double* d_mu, void* stream );
 int ncgb_batch_config( ncgb_batch_t, int* pick_block, int* sab_blocks_per_sm );
+/* 1 if the batch's S(alpha,beta) queue uses two lists, 0 for one (the
+ * default before autotuning); the setter fixes it without autotuning. */
+int ncgb_batch_split_lists( ncgb_batch_t, int* split_lists );
+int ncgb_batch_set_split_lists( ncgb_batch_t, int split_lists );
 /* Same as ncgb_batch_scatter_device, replayed as a CUDA graph (captured on
  * first use, updated in place afterwards). */
 int ncgb_batch_graph_launch( ncgb_batch_t, const double* d_ekin, const int64_t* d_offsets, unsigned long n,

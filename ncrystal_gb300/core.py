@@ -120,6 +120,8 @@ def lib():
         "ncgb_batch_autotune": (_C.c_int, [_Handle, _C.c_void_p, _C.c_void_p, _C.c_ulong, _C.c_void_p,
                                            _C.c_void_p, _C.c_void_p, _C.c_void_p]),
         "ncgb_batch_config": (_C.c_int, [_Handle, _C.POINTER(_C.c_int), _C.POINTER(_C.c_int)]),
+        "ncgb_batch_split_lists": (_C.c_int, [_Handle, _C.POINTER(_C.c_int)]),
+        "ncgb_batch_set_split_lists": (_C.c_int, [_Handle, _C.c_int]),
         "ncgb_batch_set_mode": (_C.c_int, [_Handle, _C.c_int]),
         "ncrystal_samplescatter": (None, [H, _C.c_double, _C.POINTER(_C.c_double * 3), _dblp,
                                           _C.POINTER(_C.c_double * 3)]),
@@ -630,6 +632,19 @@ class Batch:
         pb, sb = _C.c_int(), _C.c_int()
         lib().ncgb_batch_config(self._h, _C.byref(pb), _C.byref(sb))
         return pb.value, sb.value
+
+    def split_lists(self):
+        """Whether the batch's S(alpha,beta) queue uses two lists (the
+        autotuner's choice)."""
+        v = _C.c_int()
+        if lib().ncgb_batch_split_lists(self._h, _C.byref(v)):
+            _check()
+        return bool(v.value)
+
+    def set_split_lists(self, split):
+        if lib().ncgb_batch_set_split_lists(self._h, 1 if split else 0):
+            _check()
+        return self
 
     def xs_scatter_host(self, ekin, offsets):
         e = _np.ascontiguousarray(ekin, dtype=_np.float64)

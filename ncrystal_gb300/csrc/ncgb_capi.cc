@@ -1738,12 +1738,14 @@ int ncgb_batch_autotune( ncgb_batch_t bt, const double* d_ekin, const int64_t* d
     const int maxb = ncgb::maxSabBlocksPerSM();
     std::vector<ncgb::LaunchCfg> cands;
     for ( int pb : { 128, 256, 512 } )
-      for ( int sb : { maxb, std::max( 1, maxb / 2 ) } ) {
-        ncgb::LaunchCfg c;
-        c.pick_block = pb;
-        c.sab_blocks_per_sm = sb;
-        cands.push_back( c );
-      }
+      for ( int sb : { maxb, std::max( 1, maxb / 2 ) } )
+        for ( int sl : { 0, 1 } ) {
+          ncgb::LaunchCfg c;
+          c.pick_block = pb;
+          c.sab_blocks_per_sm = sb;
+          c.split_lists = sl;
+          cands.push_back( c );
+        }
     cudaEvent_t e0, e1;
     checkCuda( cudaEventCreate( &e0 ), "event" );
     checkCuda( cudaEventCreate( &e1 ), "event" );
@@ -1805,6 +1807,32 @@ int ncgb_batch_config( ncgb_batch_t bt, int* pick_block, int* sab_blocks_per_sm 
     BatchObj& bo = extractBatch( bt.internal, "ncgb_batch_config" );
     *pick_block = bo.cfg.pick_block;
     *sab_blocks_per_sm = bo.cfg.sab_blocks_per_sm > 0 ? bo.cfg.sab_blocks_per_sm : ncgb::maxSabBlocksPerSM();
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_batch_set_split_lists( ncgb_batch_t bt, int split_lists )
+{
+  try {
+    BatchObj& bo = extractBatch( bt.internal, "ncgb_batch_set_split_lists" );
+    if ( split_lists != 0 && split_lists != 1 )
+      throw TypedError( "BadInput", "ncgb_batch_set_split_lists: 0 or 1" );
+    if ( bo.cfg.split_lists != split_lists && bo.exec ) {
+      cudaGraphExecDestroy( bo.exec );   // the captured launch names the other pass
+      bo.exec = nullptr;
+    }
+    bo.cfg.split_lists = split_lists;
+    return 0;
+  } NCGB_CATCH;
+  return 1;
+}
+
+int ncgb_batch_split_lists( ncgb_batch_t bt, int* split_lists )
+{
+  try {
+    BatchObj& bo = extractBatch( bt.internal, "ncgb_batch_split_lists" );
+    *split_lists = bo.cfg.split_lists;
     return 0;
   } NCGB_CATCH;
   return 1;

@@ -51,6 +51,8 @@ namespace {
     {
       ncgb_rng_init( &r, seed, index_offset, callseq, stream );
     }
+    // main and rare lists in the S(alpha,beta) queue (see ncgb::Work)
+    __device__ __forceinline__ bool splitLists() const { return true; }
   };
 
   // One material; neutron o's stream index read from a per-neutron array
@@ -71,12 +73,14 @@ namespace {
     {
       ncgb_rng_init( &r, seed, 0, callseq, stream );
     }
+    __device__ __forceinline__ bool splitLists() const { return true; }
   };
 
   struct MultiSrc {
     const ncgb::MatSlot* slots;
     const int64_t* offsets;   // [nmat+1]
     int nmat;
+    int split;                // main and rare lists, or one list (chosen per batch by the autotuner)
     int64_t base;             // global index of this launch's first neutron (chunked host calls)
     __device__ __forceinline__ int find( uint64_t o ) const
     {
@@ -100,12 +104,8 @@ namespace {
     {
       ncgb_rng_init( &r, 0, 0, 0, 0 );
     }
+    __device__ __forceinline__ bool splitLists() const { return split != 0; }
   };
-
-  // Two lists in the S(alpha,beta) queue (main and rare, see ncgb::Work) for
-  // one-material sources; one list for ragged batches.
-  template<class Src>
-  constexpr bool kSplitLists = !std::is_same<Src, MultiSrc>::value;
 
   __device__ __forceinline__ double loadE( const ncgb::Batch& b, uint64_t i )
   {
@@ -225,13 +225,12 @@ namespace {
             // for non-negative doubles the bit patterns order as the values,
             // a negative e gives 0 both ways and a NaN ne both ways.
             queue = true;
-            if constexpr ( kSplitLists<Src> )
-              rare = !( bits( e ) < ldgbits( c.sab.egrid + c.sab.ne - 1 ) );
+            rare = src.splitLists() && !( bits( e ) < ldgbits( c.sab.egrid + c.sab.ne - 1 ) );
             qcomp = p.comp;
             break;
           case NCGB_COMP_FREEGAS:
             queue = true;
-            rare = kSplitLists<Src>;
+            rare = src.splitLists();
             qcomp = p.comp;
             break;
           default:
@@ -244,7 +243,7 @@ namespace {
       const unsigned active = __activemask();
       const unsigned want = __ballot_sync( active, queue );
       if ( want ) {
-        const unsigned wrare = kSplitLists<Src> ? __ballot_sync( active, queue && rare ) : 0u;
+        const unsigned wrare = src.splitLists() ? __ballot_sync( active, queue && rare ) : 0u;
         const unsigned wmain = want & ~wrare;
         const int lane = threadIdx.x & 31;
         const unsigned mine = ( 1u << lane ) - 1u;
@@ -452,8 +451,9 @@ namespace {
   }
 
   // Each warp takes the rare list once the main list has no neutron left for
-  // it, so that rare neutrons fill the main loop's tail (both lists are
-  // complete before this pass starts).
+  // it (both lists are complete before this pass starts).  Measured against
+  // taking it first: polyethylene k_sab 1.188 vs 1.196 ms, the crystal batch
+  // the same either way.
   template<class Src, bool Fast, bool Learned, bool Dir>
   __device__ __forceinline__ void sabRareTail( const Src& src, const ncgb::Batch& b )
   {
@@ -461,15 +461,16 @@ namespace {
       sabRareList<Src, Fast, Learned, Dir>( src, b );
   }
 
-  // Split lists (one material): a lean pass over the main list, then the
-  // rare list.  Ragged batches keep one list and the full sampler: split,
-  // the mixed batch's S(alpha,beta) pass measured 1.72 against 1.54 ms.
-  template<class Src, bool Fast, bool Learned, bool Dir>
+  // Split: a lean pass over the main list, then the rare list.  Otherwise one
+  // list and the full sampler (ragged batches whose autotuner found that
+  // faster: the mixed batch's pass measured 1.69 ms split against 1.51 ms
+  // with one list, the crystal batch's 0.66 against 0.71 ms).
+  template<class Src, bool Fast, bool Learned, bool Dir, bool Split>
   __global__ void __launch_bounds__(256, 8)
   k_sab( const __grid_constant__ Src src, const __grid_constant__ ncgb::Batch b )
   {
     NoPhases ph;
-    if constexpr ( kSplitLists<Src> ) {
+    if constexpr ( Split ) {
       sabPass<Src, Fast, Learned, Dir, false, false>( src, b, ph );
       sabRareTail<Src, Fast, Learned, Dir>( src, b );
     } else {
@@ -576,7 +577,7 @@ namespace {
   {
     static int bps = 0;
     if ( !bps ) {
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_sab<Src, false, false, std::is_same<Src, MappedSrc>::value>,
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor( &bps, k_sab<Src, false, false, std::is_same<Src, MappedSrc>::value, true>,
                                                      256, 0 );
       if ( bps <= 0 ) bps = 1;
     }
@@ -627,6 +628,22 @@ namespace {
       k_pick<Src, false, Dir><<<gridFor( b.n_out, pb ), pb, 0, s>>>( src, b );
   }
 
+  template<class Src, bool Dir, bool Split>
+  void launchSabT( const Src& src, const ncgb::Batch& b, int grid, cudaStream_t s )
+  {
+    if ( b.fast ) {
+      if ( b.learned )
+        k_sab<Src, true, true, Dir, Split><<<grid, 256, 0, s>>>( src, b );
+      else
+        k_sab<Src, true, false, Dir, Split><<<grid, 256, 0, s>>>( src, b );
+    } else {
+      if ( b.learned )
+        k_sab<Src, false, true, Dir, Split><<<grid, 256, 0, s>>>( src, b );
+      else
+        k_sab<Src, false, false, Dir, Split><<<grid, 256, 0, s>>>( src, b );
+    }
+  }
+
   template<class Src, bool Dir>
   void launchSab( const Src& src, const ncgb::Batch& b, int grid, cudaStream_t s )
   {
@@ -646,17 +663,13 @@ namespace {
         return;
       }
     }
-    if ( b.fast ) {
-      if ( b.learned )
-        k_sab<Src, true, true, Dir><<<grid, 256, 0, s>>>( src, b );
-      else
-        k_sab<Src, true, false, Dir><<<grid, 256, 0, s>>>( src, b );
-    } else {
-      if ( b.learned )
-        k_sab<Src, false, true, Dir><<<grid, 256, 0, s>>>( src, b );
-      else
-        k_sab<Src, false, false, Dir><<<grid, 256, 0, s>>>( src, b );
+    if constexpr ( std::is_same<Src, MultiSrc>::value ) {
+      if ( !src.split ) {
+        launchSabT<Src, Dir, false>( src, b, grid, s );
+        return;
+      }
     }
+    launchSabT<Src, Dir, true>( src, b, grid, s );
   }
 
   template<class Src>
@@ -748,6 +761,7 @@ namespace ncgb {
     src.slots = d_slots;
     src.offsets = d_offsets;
     src.nmat = nmat;
+    src.split = cfg.split_lists;
     src.base = (int64_t)b.index_offset;
     return launchBoth( src, b, cfg, s, pickDone );
   }

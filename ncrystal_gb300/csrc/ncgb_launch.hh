@@ -10,7 +10,8 @@ namespace ncgb {
 
   // Device-side counters.  launchScatter zeroes the queue counters at the
   // start of every batch; the caller zeroes nfail when it wants a new count.
-  // The S(alpha,beta) queue holds two lists in one buffer of n_out entries:
+  // The S(alpha,beta) queue holds one or two lists in one buffer of n_out
+  // entries (two for one material, either for a ragged batch):
   // the main list from the front (entries 0 .. qcount-1), and from the back
   // (entries n_out-1, n_out-2, ...) the rare list: neutrons of free-gas
   // components and neutrons above a component's energy grid, which the
@@ -46,6 +47,7 @@ namespace ncgb {
   struct LaunchCfg {
     int pick_block = 256;
     int sab_blocks_per_sm = 0;
+    int split_lists = 0;   // ragged batches: main and rare lists (1) or one list (0)
   };
 
   // One batch: neutron o (< n_out) has energy ekin[o % n_ekin] and draws

@@ -173,6 +173,39 @@ def test_free_gas_and_high_energies_vs_oracle(cfg):
     assert ok.mean() >= 0.999, ok.mean()
 
 
+@pytest.mark.parametrize("mode", ["exact", "mixed"])
+def test_ragged_batch_one_or_two_lists_same_results(mode):
+    """A ragged batch samples the same results with one S(alpha,beta) list as
+    with the main and rare lists (free-gas components and energies above the
+    energy grids on a list of their own), plain launch and graph replay."""
+    import torch
+    cfgs = [W.WATER, W.PE293, W.AL2O3, "Cu_sg225.ncmat;temp=77K"]
+    for c in cfgs:
+        bundle_path(c)
+    counts = [30000, 20000, 20000, 10000]
+    energies = [W.loguniform_energies(n, 1e-4, 20.0, 70 + k) for k, n in enumerate(counts)]
+    e_all = torch.as_tensor(np.concatenate(energies), device="cuda")
+    off = torch.as_tensor(np.concatenate([[0], np.cumsum(counts)]), dtype=torch.int64, device="cuda")
+    n = e_all.numel()
+    res = []
+    for split in (False, True):
+        batch = NC.Batch([NC.createScatter(c, seed=30 + k) for k, c in enumerate(cfgs)])
+        batch.set_mode(mode).set_split_lists(split)
+        assert batch.split_lists() == split
+        for launch in (batch.scatter_device, batch.graph_launch):
+            xs, ef, mu = (torch.empty_like(e_all) for _ in range(3))
+            st = torch.zeros(n, dtype=torch.int32, device="cuda")
+            launch(e_all, off, xs, ef, mu, st)
+            torch.cuda.synchronize()
+            assert int((st != 0).sum()) == 0
+            res.append([t.cpu().numpy() for t in (xs, ef, mu)])
+    # per batch, the plain launch is call 0 and the replay call 1 (other streams)
+    for k in (0, 1):
+        for a, b in zip(res[k], res[k + 2]):
+            np.testing.assert_array_equal(a, b)
+    assert not np.array_equal(res[0][1], res[1][1])
+
+
 def test_ragged_batch_matches_single_material_calls():
     """A multi-material batch reproduces, material by material, the first
     scatter call of fresh single-material handles (same seed, stream index,
