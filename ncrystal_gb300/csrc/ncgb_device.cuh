@@ -410,10 +410,15 @@ namespace ncgb_dev {
     return xs * s.internal_scale_f;
   }
 
+  // Lean: a material whose components are S(alpha,beta) and incoherent
+  // elastic only (the caller checks), compiled without the other types' code.
+  template<bool Lean = false>
   __device__ __forceinline__ float compXSf( const ncgb_comp_view& c, double ekin, float ef )
   {
     if ( !containsNN( c.elow, c.ehigh, ekin ) )
       return 0.0f;
+    if constexpr ( Lean )
+      return c.type == NCGB_COMP_SAB ? sabXSf( c.sab, ekin, ef ) : elincXSf( c.elinc, ef );
     int64_t idx;
     switch ( c.type ) {
       case NCGB_COMP_ELINC: return elincXSf( c.elinc, ef );
@@ -451,7 +456,7 @@ namespace ncgb_dev {
 
   // Mixed-precision mode: the same with FP32 cumulative sums (the Bragg plane
   // search and the FP64 Bragg sums themselves are unchanged).
-  template<bool Pick>
+  template<bool Pick, bool Lean = false>
   __device__ __forceinline__ XSPick xsAndPickF( const ncgb_material_view& m, double ekin, ncgb_rng& rng )
   {
     const float ef = (float)ekin;
@@ -463,7 +468,7 @@ namespace ncgb_dev {
     for ( int i = 0; i < NCGB_MAX_COMP; ++i ) {
       if ( i >= m.ncomp )
         break;
-      tot = fmaf( m.comp[i].scale_f, compXSf( m.comp[i], ekin, ef ), tot );
+      tot = fmaf( m.comp[i].scale_f, compXSf<Lean>( m.comp[i], ekin, ef ), tot );
       commul[i] = tot;
     }
     XSPick r{ (double)tot, 0 };
@@ -487,11 +492,11 @@ namespace ncgb_dev {
     return r;
   }
 
-  template<bool Pick, bool Fast>
+  template<bool Pick, bool Fast, bool Lean = false>
   __device__ __forceinline__ XSPick xsAndPick( const ncgb_material_view& m, double ekin, ncgb_rng& rng )
   {
     if ( Fast )
-      return xsAndPickF<Pick>( m, ekin, rng );
+      return xsAndPickF<Pick, Lean>( m, ekin, rng );
     double commul[NCGB_MAX_COMP];
     double tot = 0.0;
 #pragma unroll 1
