@@ -1016,8 +1016,13 @@ namespace ncgb_dev {
     double alpha;
     if ( Fast ) {
       const float rpf = (float)rp;
-      const float al = sampleAlphaF( s, s.info_f + off, ioff, ibeta - 1, rpf );
-      const float ah = sampleAlphaF( s, s.info_f + off, ioff, ibeta, rpf );
+      // the two rows in a rolled loop: one copy of the sampler's code
+      float al = 0.0f, ah = 0.0f;
+#pragma unroll 1
+      for ( int r = 0; r < 2; ++r ) {
+        const float v = sampleAlphaF( s, s.info_f + off, ioff, ibeta - 1 + r, rpf );
+        if ( r == 0 ) al = v; else ah = v;
+      }
       const float af = fmaf( ah - al, (float)( beta - bl ) * __ldg( s.inv_dbeta_f + ibeta - 1 ), al );
       ph.template end<PH_ALPHA>();
       const ALimF lim = alphaLimitsF( (float)x, (float)( x + beta ), (float)beta );
@@ -1127,7 +1132,7 @@ namespace ncgb_dev {
   {
     alpha = 0.0;
     beta = 0.0;
-    if ( L.preset() ) {
+    if ( Full && L.preset() ) {   // set by the extender only (never in a lean pass)
       alpha = L.pre_alpha;
       beta = L.pre_beta;
     } else {
