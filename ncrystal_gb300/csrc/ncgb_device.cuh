@@ -985,25 +985,23 @@ namespace ncgb_dev {
     int ibs;
     double beta;
     const double fbkep = ldg( s.smp_fbkep + ie );
+    bool firstBin;
     if ( Learned && s.lp_hdr && __ldg( &s.lp_hdr[ie].enabled ) ) {
       // the special first bin keeps its probability bcdf[1]; the regular
       // range is drawn from the learned proposal
-      if ( rand_u32( rng ) < __ldg( &s.lp_hdr[ie].c1_thr ) ) {
-        const int r = Full ? alg1FirstBinCall<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out )
-                           : alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
-        ph.template end<PH_BETA>();
-        return r;
-      }
-      if ( !lpBeta( s, ie, rng, beta, ibs ) )
+      firstBin = rand_u32( rng ) < __ldg( &s.lp_hdr[ie].c1_thr );
+      if ( !firstBin && !lpBeta( s, ie, rng, beta, ibs ) )
         return -1;
     } else {
       beta = percentile( bx, s.bcdf + off, s.bbin + off, nbs, rand01( rng ), ibs );
-      if ( ibs == 0 && fbkep <= 0.0 ) {
-        const int r = Full ? alg1FirstBinCall<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out )
-                           : alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
-        ph.template end<PH_BETA>();
-        return r;
-      }
+      firstBin = ( ibs == 0 && fbkep <= 0.0 );
+    }
+    if ( firstBin ) {
+      // one call site for both branches (one inlined copy in a lean pass)
+      const int r = Full ? alg1FirstBinCall<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out )
+                         : alg1FirstBin<Fast>( s, off, ioff, fbkep, ldg( bx + 1 ), x, rng, alpha_out, beta_out );
+      ph.template end<PH_BETA>();
+      return r;
     }
     ph.template end<PH_BETA>();
     if ( beta <= maxd( -x, ldg( s.beta ) ) )
