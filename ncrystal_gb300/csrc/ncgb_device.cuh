@@ -940,12 +940,19 @@ namespace ncgb_dev {
     uint32_t w = 0;
     int ok = 0;
     for ( int tries = 0; tries < 1000 && !ok; ++tries ) {
-      const uint64_t prod = (uint64_t)rand_u32( rng ) * (uint64_t)NCGB_LP_K;
+      // a try's three words, drawn in order by one copy of the stream's code
+      uint32_t d0 = 0, d1 = 0, d2 = 0;
+#pragma unroll 1
+      for ( int q = 0; q < 3; ++q ) {
+        const uint32_t v = rand_u32( rng );
+        if ( q == 0 ) d0 = v; else if ( q == 1 ) d1 = v; else d2 = v;
+      }
+      const uint64_t prod = (uint64_t)d0 * (uint64_t)NCGB_LP_K;
       const int j = (int)( prod >> 32 );
       const float fr = (float)( (uint32_t)prod >> 8 ) * ( 1.0f / 16777216.0f );
       const int k = ( fr < __ldg( &slots[j].aprob ) ) ? j : __ldg( &slots[j].alias );
       c = cells + k;
-      w = rand_u32( rng );
+      w = d1;
       // last piece with w0 <= w
       int lo = __ldg( &c->seg_lo ), hi = lo + __ldg( &c->seg_n ) - 1;
       while ( lo < hi ) {
@@ -957,7 +964,7 @@ namespace ncgb_dev {
       }
       g = s.lp_seg + lo;
       const float y = fmaf( __ldg( &g->slope ), (float)( w - __ldg( &g->w0 ) ), __ldg( &g->y0 ) );
-      const float ua = (float)( rand_u32( rng ) >> 8 ) * ( 1.0f / 16777216.0f );
+      const float ua = (float)( d2 >> 8 ) * ( 1.0f / 16777216.0f );
       ok = ( ua * __ldg( &c->env ) < y );
     }
     __syncwarp( lanes );
