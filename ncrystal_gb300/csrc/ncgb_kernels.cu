@@ -86,16 +86,33 @@ namespace {
     int nmat;
     int split;                // main and rare lists, or one list (chosen per batch by the autotuner)
     int64_t base;             // global index of this launch's first neutron (chunked host calls)
-    __device__ __forceinline__ int find( uint64_t o ) const
+    // last k with offsets[k] <= g
+    __device__ __forceinline__ int search( int64_t g ) const
     {
-      // last k with offsets[k] <= base + o
-      const int64_t g = base + (int64_t)o;
       int lo = 0, hi = nmat - 1;
       while ( lo < hi ) {
         const int mid = ( lo + hi + 1 ) >> 1;
         if ( __ldg( offsets + mid ) <= g ) lo = mid; else hi = mid - 1;
       }
       return lo;
+    }
+    // The material of neutron o.  Called by all active lanes of a warp
+    // together: the first one searches, and a lane inside the same material
+    // ([offsets[k], offsets[k+1]), neutrons are grouped by material) takes
+    // its answer -- no later material starts at or below g, so it is the
+    // same k -- and only the others search.
+    __device__ __forceinline__ int find( uint64_t o ) const
+    {
+      const int64_t g = base + (int64_t)o;
+      const unsigned m = __activemask();
+      const int leader = __ffs( m ) - 1;
+      int k = 0;
+      if ( (int)( threadIdx.x & 31 ) == leader )
+        k = search( g );
+      k = __shfl_sync( m, k, leader );
+      if ( __ldg( offsets + k ) <= g && g < __ldg( offsets + k + 1 ) )
+        return k;
+      return search( g );
     }
     __device__ __forceinline__ const ncgb_material_view& mat( int k ) const { return slots[k].view; }
     __device__ __forceinline__ void rngFor( ncgb_rng& r, int k, uint64_t o, uint32_t callseq ) const
